@@ -1,0 +1,328 @@
+"""Benchmark of the immersed-boundary step on GB300.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--workload spheres3d_256|spheres3d_384|cylinder2d] [--precision fp64|mixed]
+
+One step = one time step of the whole case (snapshot, predictor, RHS,
+iter_max red-black SOR iterations, projection, boundary).  Default workload:
+the 3D drop-in case -- unit cube on a 256^3 grid, 32 seeded spheres, plain
+FP64, iter_max=100, omega=1.7 -- with synthetic (seeded) porosity.
+
+Prints one JSON line.  `value` is device time (CUDA events on the case's
+stream) with the fields resident in HBM; `e2e` is the same metric through the
+C ABI with pinned host buffers copied in (pf_set_state) and out
+(pf_get_state) every step.  With --gpus N > 1 (torchrun) every rank advances
+its own replica of the case (no exchange between ranks: the path shards by
+case), and `value` is the sum over ranks over the max-over-ranks time.
+
+--impl reference times the CPU restatement of the reference's OpenMP step
+(the oracle; the reference is Fortran and no Fortran compiler is available)
+on all host cores for the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s at max|div u|<1e-6 (batched FP32+FP64-DC vs plain FP64); p50/p99"
+UNIT = "Mcell-steps/s"
+
+
+def workload(name: str, precision: str):
+    from pixelflow_gb300 import geometry as G
+    if name in ("spheres3d_256", "spheres3d_384", "spheres3d_128"):
+        nn = int(name.split("_")[1])
+        s = G.settings_spheres_3d(precision=precision)
+        shape = (nn, nn, nn)
+        vals = G.spheres_3d(nn, nn, nn)
+        desc = dict(workload=f"3D ibm3 unit cube {nn}^3, 32 seeded spheres (seed 0), tanh edge 2 cells",
+                    grid=list(shape), nu=s.xnue, dt=s.time / s.istep_max, iter_max=s.iter_max,
+                    omega=s.relux_factor)
+    elif name == "cylinder2d":
+        s = G.settings_cylinder_2d(precision=precision)
+        shape = (512, 256)
+        vals = G.cylinder_2d()
+        desc = dict(workload="2D ibm2 cylinder 512x256, D=0.1 at (0.5,0.5), Re=100", grid=list(shape),
+                    nu=s.xnue, dt=s.time / s.istep_max, iter_max=s.iter_max, omega=s.relux_factor)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    if precision == "mixed":
+        desc.update(outer_passes=s.outer_max, inner_sweeps=s.inner_sweeps)
+    desc["precision"] = precision
+    return s, shape, vals, desc
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name: str):
+    """Per-launch DRAM bytes of the dominant kernel from a committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(name)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(settings, shape, vals, budget_s: float = 20.0, max_steps: int = 5):
+    """The oracle (OpenMP, all host threads) on a bounded sample of the workload."""
+    from oracle.oracle import OracleCase
+    c = OracleCase(settings, shape, vals)
+    c.initialize()
+    cells = int(np.prod(shape))
+    times = []
+    while len(times) < max_steps and sum(times) < budget_s:
+        t0 = time.perf_counter()
+        c.step(1)
+        times.append(time.perf_counter() - t0)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": cells * len(times) / sum(times) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(times)} full steps of the same case from the initial state "
+                      f"({sum(times):.1f} s, oracle = C restatement of the reference OpenMP step, FP64)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_setup()
+    if rank != 0:
+        barrier(world)
+        return
+    s, shape, vals, desc = workload(args.workload, "fp64")
+    from oracle.oracle import OracleCase
+    cells = int(np.prod(shape))
+    c = OracleCase(s, shape, vals)
+    c.initialize()
+    for _ in range(min(args.warmup, 1)):
+        c.step(1)
+    budget = float(os.environ.get("PF_REFERENCE_BUDGET_S", "150"))
+    times = []
+    while len(times) < args.steps and sum(times) < budget:
+        t0 = time.perf_counter()
+        c.step(1)
+        times.append(time.perf_counter() - t0)
+    value = cells * len(times) / sum(times) / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = (f"{len(times)} of {args.steps} requested steps timed (cap {budget:.0f} s), "
+              f"{min(args.warmup, 1)} warm-up; oracle = C restatement of the reference OpenMP step")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+           "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": desc,
+           "latency_ms": {"p50": 1e3 * float(np.percentile(times, 50)), "p99": 1e3 * float(np.percentile(times, 99))},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    barrier(world)
+
+
+def run_ours(args):
+    rank, world, local = dist_setup()
+    from pixelflow_gb300 import _lib
+    from pixelflow_gb300.solver import Case, host_register, host_unregister
+    _lib.check(_lib.load().pf_set_device(local))
+    s, shape, vals, desc = workload(args.workload, args.precision)
+    cells = int(np.prod(shape))
+    case = Case(s, shape, vals)
+    case.initial_conditions()
+    case.step(args.warmup)
+    case.synchronize()
+
+    # ---- device-timed region ---------------------------------------------
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    case.synchronize()
+    l0 = case.kernel_launches()
+    case.profile_begin()
+    case.step(args.steps)
+    prof = case.profile_end()  # synchronizes the case's stream
+    launches = case.kernel_launches() - l0
+    barrier(world)
+    clocks = sampler.stop()
+    step_ms = reduce_max(prof["step_ms"], world)
+    per_step = case.profile_step_times()
+    value = world * cells * args.steps / (step_ms / 1e3) / 1e6
+    max_div, sor_err = case.norms()
+
+    # ---- roofline of the dominant kernel (the red-black half-sweep) --------
+    word = 8 if args.precision == "fp64" else 4
+    sor_launch_ms = prof["sor_ms"] / max(prof["sor_launches"], 1)
+    # algorithmic bytes per half-sweep: the updated half of the cells x 5 words
+    # (own p read, neighbour p read, p write, bb, porosity)
+    alg_bytes = cells / 2 * 5 * word
+    achieved = alg_bytes / (sor_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    kname = f"sor_half_{args.precision}_{args.workload}"
+    traffic = ncu_traffic(kname)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind, "kernel": "k_sor_half",
+                "sor_share_of_step": prof["sor_ms"] / prof["step_ms"], "avg_launch_ms": sor_launch_ms,
+                "algorithmic_bytes_per_launch": alg_bytes}
+
+    # ---- end to end through the C ABI with host buffers ----------------------
+    host = case.get_state()
+    for a in host.values():
+        host_register(a)
+    out = {k: np.empty_like(a) for k, a in host.items()}
+    for a in out.values():
+        host_register(a)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        case.set_state(host["u"], host["v"], host["p"], host.get("w"))
+        case.step(1)
+        case.get_state(out)
+    t1 = time.perf_counter()
+    e2e_s = reduce_max(t1 - t0, world)
+    for a in list(host.values()) + list(out.values()):
+        host_unregister(a)
+    nbytes = sum(a.nbytes for a in host.values())
+    e2e = {"value": world * cells * args.steps / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic"}
+    desc.update(parallelism=f"replicas{world}" if world > 1 else "single",
+                l2="working set > 129 MB L2 (no flush needed)")
+    line["config"] = desc
+    line["latency_ms"] = {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))}
+    line["max_div"] = max_div
+    line["sor_error"] = sor_err
+    line["roofline"] = roofline
+    line["e2e"] = e2e
+    line["gpu_launches"] = launches
+    line["clocks"] = clocks
+    case.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)
+    barrier(world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="spheres3d_256")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

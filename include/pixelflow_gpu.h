@@ -1,0 +1,152 @@
+/*
+ * pixelflow_gpu.h -- C ABI of the GB300 immersed-boundary step.
+ *
+ * Drop-in for the step loop of PixelFlow's ibm2 / ibm3 programs
+ * (nobu-n2002/PixelFlow, src/omp_parallel/ibm_2d_uniform_omp_cpu.f90 and
+ * ibm_3d_uniform_omp_cpu.f90).  The reference has no plugin or FFI layer;
+ * its seam is the set of Fortran subroutines called from `program main`.
+ * Each entry point below names the reference routine it replaces.
+ *
+ * Conventions
+ *  - Plain C types only; every call returns PF_OK (0) or a negative PF_E_*
+ *    code, and pf_last_error() gives a message for the calling thread.
+ *  - Field arrays cross the boundary in the reference's own layout: Fortran
+ *    column-major a(0:ld1-1, 0:ld2-1[, 0:l+1]) of double, i fastest, with
+ *    the ghost layer at 0 and m+1.  ld1 >= m+2 and ld2 >= n+2 are the
+ *    caller's leading dimensions (md+1 and nd+1 of lib/global.f90:6,12).
+ *  - A case owns its device memory and one CUDA stream; calls on one case
+ *    are not thread safe, calls on different cases are.  Compute calls are
+ *    asynchronous; pf_get_state / pf_norms / pf_synchronize wait.
+ */
+#ifndef PIXELFLOW_GPU_H
+#define PIXELFLOW_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_ABI_VERSION 1
+
+enum {
+  PF_OK = 0,
+  PF_E_INVALID = -1,   /* bad argument or unsupported size */
+  PF_E_CUDA = -2,      /* CUDA runtime failure */
+  PF_E_NOMEM = -3,     /* device allocation failed or over the memory budget */
+  PF_E_NONFINITE = -4, /* NaN or Inf found in the fields */
+  PF_E_TIMEOUT = -5,   /* a bounded device wait gave up */
+  PF_E_STATE = -6,     /* call made in the wrong order / handle closed */
+  PF_E_BUSY = -7       /* no free slot (batch and serving forms) */
+};
+
+enum { PF_PREC_FP64 = 0, PF_PREC_MIXED = 1 };
+
+/* Namelist values of config/controlDict.txt (lib/global.f90:18-26, 47-54)
+ * plus the grid size from the porosity file header (lib/grid.f90:38,283).
+ * dx = width/(m-1), dy = height/(n-1), dz = depth/(l-1), dt = time/istep_max
+ * are derived as grid.f90:50-52 and :297-300 do. */
+typedef struct pf_params {
+  int32_t dim, m, n, l; /* dim 2 (ibm2) or 3 (ibm3); l ignored for dim 2 */
+  double xnue, xlambda, density, width, height, depth, time;
+  double inlet_velocity, outlet_pressure, aoa;
+  int32_t istep_max, iter_max;
+  double thickness, threshold, relux_factor;
+  int32_t nonslip, reserved;
+} pf_params;
+
+/* Options that only this library reads (the &gpu_control group). */
+typedef struct pf_options {
+  int32_t precision;       /* PF_PREC_FP64: plain step.  PF_PREC_MIXED: FP32
+                              stencils and SOR sweeps inside an FP64
+                              defect-correction loop */
+  int32_t outer_max;       /* mixed: defect-correction passes per step */
+  int32_t inner_sweeps;    /* mixed: FP32 SOR iterations per pass */
+  int32_t track_sor_error; /* 1: compute the reference's SOR max-change */
+  double dc_tol;           /* mixed: stop passes once max|r| <= dc_tol */
+  int32_t use_graph;       /* 1: replay each step from a CUDA graph */
+  int32_t reserved[5];
+} pf_options;
+
+typedef struct pf_case pf_case;
+
+/* Message for the last failed call on this thread ("" if none). */
+const char *pf_last_error(void);
+const char *pf_strerror(int code);
+int pf_abi_version(void);
+/* Select the CUDA device that later pf_create calls on this thread use. */
+int pf_set_device(int device);
+int pf_device_count(int *count);
+/* Fill *opt with defaults (plain FP64, error tracking on, graphs on). */
+void pf_default_options(pf_options *opt);
+
+/* Create a case.  porosity_values: m*n[*l] raw values in the order of the
+ * porosity CSV records (i fastest), as read by grid_conditions
+ * (lib/grid.f90:36-47 2D, :281-294 3D); the threshold clamp of grid.f90:43
+ * and the ghost fill of :92-106 / :349-378 are applied here.
+ * Replaces: read_settings + grid_conditions[_yz_periodic] set-up. */
+int pf_create(const pf_params *prm, const pf_options *opt, const double *porosity_values,
+              pf_case **out);
+int pf_destroy(pf_case *c);
+
+/* initial_conditions followed by boundary
+ * (ibm_2d_uniform_omp_cpu.f90:67-70 / ibm_3d_uniform_omp_cpu.f90:68-71). */
+int pf_initial_conditions(pf_case *c);
+
+/* Host <-> device field exchange in the Fortran layout described above.
+ * w is ignored for 2D cases (may be NULL). */
+int pf_set_state(pf_case *c, const double *u, const double *v, const double *w, const double *p,
+                 int ld1, int ld2);
+int pf_get_state(pf_case *c, double *u, double *v, double *w, double *p, int ld1, int ld2);
+int pf_get_porosity(pf_case *c, double *poro, int ld1, int ld2);
+
+/* solve_p: divergence, predictor, coefficients/RHS, boundrary_matrix and the
+ * red-black SOR (ibm_2d_uniform_omp_cpu.f90:142-286, 293-406, 410-454;
+ * ibm_3d_uniform_omp_cpu.f90:151-426, 433-614, 618-663).  Snapshots the
+ * velocities first, as the step loop does (2D :84-96, 3D :85-100). */
+int pf_solve_p(pf_case *c);
+/* Velocity projection loop (2D :103-115, 3D :109-125). */
+int pf_projection(pf_case *c);
+/* boundary (2D :460-538, 3D :669-752). */
+int pf_boundary(pf_case *c);
+/* nsteps passes of the main step loop body (2D :80-125, 3D :81-132):
+ * snapshot, solve_p, projection, boundary. */
+int pf_step(pf_case *c, int nsteps);
+int pf_synchronize(pf_case *c);
+
+/* max|div u| of the porosity-weighted divergence that output_divergent_2d/3d
+ * writes (lib/output.f90:217-224, :929-941) on the current fields, and the
+ * SOR `error` of the last solve_p (the value the reference prints at
+ * ibm_2d_uniform_omp_cpu.f90:400 / ibm_3d:608; 0 when tracking is off).
+ * Returns PF_E_NONFINITE if max_div is NaN or Inf. */
+int pf_norms(pf_case *c, double *max_div, double *sor_error);
+
+/* Pin a caller-owned host buffer so pf_set_state / pf_get_state copy it
+ * asynchronously at full link speed (cudaHostRegister); optional. */
+int pf_host_register(void *ptr, size_t bytes);
+int pf_host_unregister(void *ptr);
+
+/* Timing of the stages inside pf_step, with CUDA events on the case's
+ * stream.  While profiling is on, steps run without graph replay.
+ * pf_profile_end returns the summed device time of the SOR half-sweep
+ * kernels, their launch count, and the time of whole steps. */
+int pf_profile_begin(pf_case *c);
+int pf_profile_end(pf_case *c, double *sor_ms, int64_t *sor_launches, double *step_ms,
+                   int64_t *steps);
+
+/* Per-step durations (ms) of the last profiling session, up to max_steps
+ * values; *n receives the count written. */
+int pf_profile_step_times(pf_case *c, double *ms, int64_t max_steps, int64_t *n);
+
+/* Number of kernels this case has launched (graph replays count every
+ * kernel node), for accounting in benchmarks. */
+int pf_kernel_launches(pf_case *c, int64_t *count);
+
+/* Device memory held by the case, in bytes. */
+int pf_memory_bytes(pf_case *c, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIXELFLOW_GPU_H */

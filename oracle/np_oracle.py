@@ -1,0 +1,328 @@
+"""Independent numpy restatement of the reference step -- TEST INFRASTRUCTURE ONLY.
+
+A second, vectorised statement of the same reference routines as
+pf_oracle.c, written from the Fortran independently of the C file: whole-array
+slicing instead of loops, and red-black colours chosen by the parity
+predicate ((i+j) odd first in 2D, (i+j+k) even first in 3D) instead of the
+reference's linear-index mapping.  numpy evaluates each binary operation
+separately in IEEE arithmetic, so with the same operation order it must agree
+with the C restatement bit for bit.  Used only by tests, at small sizes.
+
+Arrays: 2D (n+2, m+2), 3D (l+2, n+2, m+2), index [k, j, i] = Fortran (i, j, k).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class NpCase:
+    def __init__(self, settings, shape, porosity_values, dtype=np.float64):
+        self.dim = len(shape)
+        self.T = np.dtype(dtype).type
+        T = self.T
+        s = settings
+        if self.dim == 2:
+            self.m, self.n = shape
+            self.l = 1
+            self.shape = (self.n + 2, self.m + 2)
+        else:
+            self.m, self.n, self.l = shape
+            self.shape = (self.l + 2, self.n + 2, self.m + 2)
+        m, n, l = self.m, self.n, self.l
+        self.xnue, self.xlambda, self.density = T(s.xnue), T(s.xlambda), T(s.density)
+        self.thickness, self.relux = T(s.thickness), T(s.relux_factor)
+        self.U, self.pout, self.aoa = T(s.inlet_velocity), T(s.outlet_pressure), T(s.aoa)
+        self.nonslip, self.iter_max = bool(s.nonslip), int(s.iter_max)
+        # grid.f90:50-52 / :297-300
+        self.dx = T(s.width) / T(m - 1)
+        self.dy = T(s.height) / T(n - 1)
+        self.dz = T(s.depth) / T(l - 1) if self.dim == 3 else T(0)
+        self.dt = T(s.time) / T(int(s.istep_max))
+        # porosity with ghosts (grid.f90)
+        po = np.zeros(self.shape, dtype=dtype)
+        vals = np.maximum(np.asarray(porosity_values, dtype=dtype), T(s.threshold))
+        if self.dim == 2:
+            po[1:n + 1, 1:m + 1] = vals
+            po[1:n + 2, 0] = po[1:n + 2, 1]
+            po[1:n + 2, m + 1] = po[1:n + 2, m]
+            po[0, :] = po[n, :]
+            po[n + 1, :] = po[1, :]
+        else:
+            po[1:l + 1, 1:n + 1, 1:m + 1] = vals
+            po[1:l + 2, 1:n + 2, 0] = po[1:l + 2, 1:n + 2, 1]
+            po[1:l + 2, 1:n + 2, m + 1] = po[1:l + 2, 1:n + 2, m]
+            po[:, 0, :] = po[:, n, :]
+            po[:, n + 1, :] = po[:, 1, :]
+            po[0, :, :] = po[l, :, :]
+            po[l + 1, :, :] = po[1, :, :]
+        self.poro = po
+        z = lambda: np.zeros(self.shape, dtype=dtype)
+        self.u, self.v, self.p = z(), z(), z()
+        self.w = z() if self.dim == 3 else None
+        self.last_error = 0.0
+
+    # ---------------------------------------------------------------
+    def initialize(self):
+        T = self.T
+        pi = T(np.arctan(T(1.0))) * T(4.0)
+        if self.dim == 2:
+            I = (slice(1, self.n + 1), slice(1, self.m + 1))
+            self.u[I] = self.U * T(np.cos(self.aoa / T(180) * pi))
+            self.v[I] = self.U * T(np.sin(self.aoa / T(180) * pi))
+            self.p[I] = self.pout
+        else:
+            I = (slice(1, self.l + 1), slice(1, self.n + 1), slice(1, self.m + 1))
+            self.u[I] = self.U * T(np.cos(self.aoa / T(360) * pi))
+            self.v[I] = self.U * T(np.sin(self.aoa / T(360) * pi))
+            self.w[I] = T(0)
+            self.p[I] = self.pout
+        self.boundary()
+
+    def boundary(self):
+        T = self.T
+        m, n, l = self.m, self.n, self.l
+        pi = T(np.arctan(T(1.0))) * T(4.0)
+        u, v, w, p = self.u, self.v, self.w, self.p
+        if self.dim == 2:
+            J = slice(1, n + 1)
+            u[J, 1] = self.U * T(np.cos(self.aoa / T(180.) * pi))
+            v[J, 1] = self.U * T(np.sin(self.aoa / T(180.) * pi))
+            u[J, 0] = u[J, 1]
+            v[J, 0] = v[J, 1]
+            p[J, 0] = p[J, 2]
+            u[J, m + 1] = u[J, m - 1]
+            v[J, m + 1] = v[J, m - 1]
+            p[J, m + 1] = self.pout
+            for a in (u, v, p):
+                a[0, :] = a[n, :]
+                a[n + 1, :] = a[1, :]
+        else:
+            J, K = slice(1, n + 1), slice(1, l + 1)
+            u[K, J, 1] = self.U * T(np.cos(self.aoa / T(1300.) * pi))
+            v[K, J, 1] = self.U * T(np.sin(self.aoa / T(1300.) * pi))
+            w[K, J, 1] = T(0)
+            u[K, J, 0] = u[K, J, 1]
+            v[K, J, 0] = v[K, J, 1]
+            w[K, J, 0] = w[K, J, 1]
+            p[K, J, 0] = p[K, J, 2]
+            u[K, J, m + 1] = u[K, J, m - 1]
+            v[K, J, m + 1] = v[K, J, m - 1]
+            w[K, J, m + 1] = w[K, J, m - 1]
+            p[K, J, m + 1] = self.pout
+            for a in (u, v, w, p):
+                a[:, 0, :] = a[:, n, :]
+                a[:, n + 1, :] = a[:, 1, :]
+            for a in (u, v, w, p):
+                a[0, :, :] = a[l, :, :]
+                a[l + 1, :, :] = a[1, :, :]
+
+    # shifted interior views ----------------------------------------
+    def _s(self, a, di=0, dj=0, dk=0):
+        m, n, l = self.m, self.n, self.l
+        if self.dim == 2:
+            return a[1 + dj:n + 1 + dj, 1 + di:m + 1 + di]
+        return a[1 + dk:l + 1 + dk, 1 + dj:n + 1 + dj, 1 + di:m + 1 + di]
+
+    def _interior(self):
+        if self.dim == 2:
+            return (slice(1, self.n + 1), slice(1, self.m + 1))
+        return (slice(1, self.l + 1), slice(1, self.n + 1), slice(1, self.m + 1))
+
+    # ---------------------------------------------------------------
+    def step(self, nsteps=1):
+        for _ in range(nsteps):
+            uo, vo = self.u.copy(), self.v.copy()
+            wo = self.w.copy() if self.dim == 3 else None
+            self.last_error = self.solve_p(uo, vo, wo)
+            self.projection()
+            self.boundary()
+        return self.last_error
+
+    def divergence(self, uo, vo, wo):
+        T, S = self.T, self._s
+        dx, dy, dz = self.dx, self.dy, self.dz
+        div = np.zeros(self.shape, dtype=self.poro.dtype)
+        m, n, l = self.m, self.n, self.l
+        if self.dim == 2:
+            div[self._interior()] = ((S(uo, 1) - S(uo, -1)) / dx * T(.5)
+                                     + (S(vo, 0, 1) - S(vo, 0, -1)) / dx * T(.5))
+            div[1:n + 1, 0] = 0
+            div[1:n + 1, m + 1] = 0
+            div[0, 1:m + 1] = div[n, 1:m + 1]
+            div[n + 1, 1:m + 1] = div[1, 1:m + 1]
+        else:
+            div[self._interior()] = ((S(uo, 1) - S(uo, -1)) / dx * T(.5)
+                                     + (S(vo, 0, 1) - S(vo, 0, -1)) / dy * T(.5)
+                                     + (S(wo, 0, 0, 1) - S(wo, 0, 0, -1)) / dz * T(.5))
+            div[1:l + 1, 1:n + 1, 0] = 0
+            div[1:l + 1, 1:n + 1, m + 1] = 0
+            div[1:l + 1, 0, 1:m + 1] = div[1:l + 1, n, 1:m + 1]
+            div[1:l + 1, n + 1, 1:m + 1] = div[1:l + 1, 1, 1:m + 1]
+            div[0, 1:n + 1, 1:m + 1] = div[l, 1:n + 1, 1:m + 1]
+            div[l + 1, 1:n + 1, 1:m + 1] = div[1, 1:n + 1, 1:m + 1]
+        return div
+
+    def predictor(self, uo, vo, wo, div):
+        T, S = self.T, self._s
+        dx, dy, dz, dt = self.dx, self.dy, self.dz, self.dt
+        nu, lam, th = self.xnue, self.xlambda, self.thickness
+        po = self.poro
+        pc = S(po)
+        two, half, one, alpha = T(2.), T(.5), T(1.), T(32.)
+        if self.dim == 2:
+            def comp(f, g_conv_x, g_conv_y, d_e, d_w, d_scale, A, B, dpx, dpy, dterm):
+                t = S(f) - dt * (S(uo) * (S(f, 1) - S(f, -1)) / dx / two)
+                t = t - dt * (S(vo) * (S(f, 0, 1) - S(f, 0, -1)) / dy / two)
+                t = t + dt * nu * (S(f, 1) - two * S(f) + S(f, -1)) / dx / dx
+                t = t + dt * nu * (S(f, 0, 1) - two * S(f) + S(f, 0, -1)) / dy / dy
+                t = t + dt * (nu + lam) * (d_e - d_w) / d_scale * half
+                t = t + dt * (A * nu * (S(po, 1) - S(po, -1)) / dx * half
+                              + B * nu * (S(po, 0, 1) - S(po, 0, -1)) / dy * half
+                              + dterm) / pc
+                if self.nonslip:
+                    t = t - dt * nu * S(f) / ((th * dx) * (th * dx)) * alpha * pc * (one - pc) * (one - pc)
+                return t
+            dux = (S(uo, 1) - S(uo, -1)) / dx * half
+            duy = (S(uo, 0, 1) - S(uo, 0, -1)) / dy * half
+            dvx = (S(vo, 1) - S(vo, -1)) / dx * half
+            dvy = (S(vo, 0, 1) - S(vo, 0, -1)) / dy * half
+            un = comp(uo, None, None, S(div, 1), S(div, -1), dx, dux + dux, duy + dvx, None, None,
+                      S(div) * (S(po, 1) - S(po, -1)) / dx * T(0.5) * lam)
+            vn = comp(vo, None, None, S(div, 0, 1), S(div, 0, -1), dy, dvx + duy, dvy + dvy, None, None,
+                      S(div) * (S(po, 0, 1) - S(po, 0, -1)) / dy * T(0.5) * lam)
+            self.u[self._interior()] = un
+            self.v[self._interior()] = vn
+        else:
+            def comp(f, d_e, d_w, d_scale, A1, A2, A3, dterm, hdamp):
+                t = S(f) - dt * S(uo) * (S(f, 1) - S(f, -1)) / dx * half
+                t = t - dt * S(vo) * (S(f, 0, 1) - S(f, 0, -1)) / dy * half
+                t = t - dt * S(wo) * (S(f, 0, 0, 1) - S(f, 0, 0, -1)) / dz * half
+                t = t + dt * nu * (S(f, 1) - two * S(f) + S(f, -1)) / dx / dx
+                t = t + dt * nu * (S(f, 0, 1) - two * S(f) + S(f, 0, -1)) / dy / dy
+                t = t + dt * nu * (S(f, 0, 0, 1) - two * S(f) + S(f, 0, 0, -1)) / dz / dz
+                t = t + dt * (nu + lam) * (d_e - d_w) / d_scale * half
+                t = t + dt * (A1 * nu * (S(po, 1) - S(po, -1)) / dx * half
+                              + A2 * nu * (S(po, 0, 1) - S(po, 0, -1)) / dy * half
+                              + A3 * nu * (S(po, 0, 0, 1) - S(po, 0, 0, -1)) / dz * half
+                              + dterm) / pc
+                if self.nonslip:
+                    t = t - dt * nu * S(f) / ((th * hdamp) * (th * hdamp)) * alpha * pc * (one - pc) * (one - pc)
+                return t
+            g = lambda f, di, dj, dk, h: (S(f, di, dj, dk) - S(f, -di, -dj, -dk)) / h * half
+            dux, duy, duz = g(uo, 1, 0, 0, dx), g(uo, 0, 1, 0, dy), g(uo, 0, 0, 1, dz)
+            dvx, dvy, dvz = g(vo, 1, 0, 0, dx), g(vo, 0, 1, 0, dy), g(vo, 0, 0, 1, dz)
+            dwx, dwy, dwz = g(wo, 1, 0, 0, dx), g(wo, 0, 1, 0, dy), g(wo, 0, 0, 1, dz)
+            un = comp(uo, S(div, 1), S(div, -1), dx, dux + dux, duy + dvx, duz + dwx,
+                      S(div) * (S(po, 1) - S(po, -1)) / dx * half * lam, dx)
+            vn = comp(vo, S(div, 0, 1), S(div, 0, -1), dy, dvx + duy, dvy + dvy, dvz + dwy,
+                      S(div) * (S(po, 0, 1) - S(po, 0, -1)) / dy * half * lam, dy)
+            wn = comp(wo, S(div, 0, 0, 1), S(div, 0, 0, -1), dz, dwx + duz, dwy + dvz, dwz + dwz,
+                      S(div) * (S(po, 0, 0, 1) - S(po, 0, 0, -1)) / dz * half * lam, dz)
+            I = self._interior()
+            self.u[I], self.v[I], self.w[I] = un, vn, wn
+
+    def coefficients(self):
+        """ae..ab, ap, bb after boundrary_matrix; dict of interior arrays."""
+        T, S = self.T, self._s
+        dx, dy, dz, dt, rho = self.dx, self.dy, self.dz, self.dt, self.density
+        small, half = T(1.e-6), T(0.5)
+        po, pc = self.poro, S(self.poro)
+        face = lambda a, b, h: dt * np.maximum(small, (a + b) * half) / h / h
+        C = {}
+        C["ae"] = face(S(po, 1), pc, dx)
+        C["aw"] = face(pc, S(po, -1), dx)
+        C["an"] = face(S(po, 0, 1), pc, dy)
+        C["as"] = face(pc, S(po, 0, -1), dy)
+        u, v, w = self.u, self.v, self.w
+        bb = (((S(po, 1) * S(u) + pc * S(u, 1)) * half - (S(po, -1) * S(u) + pc * S(u, -1)) * half) * rho / dx
+              + ((S(po, 0, 1) * S(v) + pc * S(v, 0, 1)) * half
+                 - (S(po, 0, -1) * S(v) + pc * S(v, 0, -1)) * half) * rho / dy)
+        if self.dim == 3:
+            C["at"] = face(S(po, 0, 0, 1), pc, dz)
+            C["ab"] = face(pc, S(po, 0, 0, -1), dz)
+            C["ap"] = -C["ae"] - C["aw"] - C["an"] - C["as"] - C["at"] - C["ab"]
+            bb = bb + ((S(po, 0, 0, 1) * S(w) + pc * S(w, 0, 0, 1)) * half
+                       - (S(po, 0, 0, -1) * S(w) + pc * S(w, 0, 0, -1)) * half) * rho / dz
+        else:
+            C["ap"] = -C["ae"] - C["aw"] - C["an"] - C["as"]
+        C["bb"] = bb
+        # boundrary_matrix
+        C["ae"][..., 0] = C["ae"][..., 0] + C["aw"][..., 0]
+        C["aw"][..., 0] = 0
+        C["bb"][..., -1] = C["bb"][..., -1] + C["ae"][..., -1] * S(self.p, 1)[..., -1]
+        for key in ("ae", "aw", "an", "as", "at", "ab"):
+            if key in C:
+                C[key][..., -1] = 0
+        return C
+
+    def _halo_p(self):
+        p, m, n, l = self.p, self.m, self.n, self.l
+        if self.dim == 2:
+            p[0, 1:m + 1] = p[n, 1:m + 1]
+            p[n + 1, 1:m + 1] = p[1, 1:m + 1]
+        else:
+            p[1:l + 1, 0, 1:m + 1] = p[1:l + 1, n, 1:m + 1]
+            p[1:l + 1, n + 1, 1:m + 1] = p[1:l + 1, 1, 1:m + 1]
+            p[0, 1:n + 1, 1:m + 1] = p[l, 1:n + 1, 1:m + 1]
+            p[l + 1, 1:n + 1, 1:m + 1] = p[1, 1:n + 1, 1:m + 1]
+
+    def colour_masks(self):
+        """(first, second) half-sweep masks over the interior."""
+        if self.dim == 2:
+            j, i = np.meshgrid(np.arange(1, self.n + 1), np.arange(1, self.m + 1), indexing="ij")
+            first = (i + j) % 2 == 1
+        else:
+            k, j, i = np.meshgrid(np.arange(1, self.l + 1), np.arange(1, self.n + 1),
+                                  np.arange(1, self.m + 1), indexing="ij")
+            first = (i + j + k) % 2 == 0
+        return first, ~first
+
+    def sor(self, C):
+        T, S = self.T, self._s
+        om = self.relux
+        first, second = self.colour_masks()
+        I = self._interior()
+        error = T(0)
+        for _ in range(self.iter_max):
+            for which, mask in enumerate((first, second)):
+                self._halo_p()
+                po = self.p.copy()
+                r = C["bb"] - C["ae"] * S(po, 1) - C["aw"] * S(po, -1) - C["an"] * S(po, 0, 1) - C["as"] * S(po, 0, -1)
+                if self.dim == 3:
+                    r = r - C["at"] * S(po, 0, 0, 1) - C["ab"] * S(po, 0, 0, -1)
+                new = r / C["ap"] * om + S(po) * (T(1.) - om)
+                interior = self.p[I]
+                interior[mask] = new[mask]
+                if self.dim == 2 or which == 1:
+                    d = np.abs(interior - S(po))
+                    error = max(error, d.max())
+        self._halo_p()
+        return float(error)
+
+    def solve_p(self, uo, vo, wo):
+        div = self.divergence(uo, vo, wo)
+        self.predictor(uo, vo, wo, div)
+        C = self.coefficients()
+        return self.sor(C)
+
+    def projection(self):
+        T, S = self.T, self._s
+        dt, rho, half = self.dt, self.density, T(0.5)
+        I = self._interior()
+        p = self.p
+        self.u[I] = S(self.u) - dt / rho * (S(p, 1) - S(p, -1)) / self.dx * half
+        self.v[I] = S(self.v) - dt / rho * (S(p, 0, 1) - S(p, 0, -1)) / self.dy * half
+        if self.dim == 3:
+            self.w[I] = S(self.w) - dt / rho * (S(p, 0, 0, 1) - S(p, 0, 0, -1)) / self.dz * half
+
+    def divergence_diag(self):
+        T, S = self.T, self._s
+        po, pc, u, v = self.poro, S(self.poro), self.u, self.v
+        two = T(2)
+        d = (((S(po, 1) * S(u) + pc * S(u, 1)) / two - (S(po, -1) * S(u) + pc * S(u, -1)) / two) / self.dx
+             + ((S(po, 0, 1) * S(v) + pc * S(v, 0, 1)) / two - (S(po, 0, -1) * S(v) + pc * S(v, 0, -1)) / two) / self.dy)
+        if self.dim == 3:
+            w = self.w
+            d = d + ((S(po, 0, 0, 1) * S(w) + pc * S(w, 0, 0, 1)) / two
+                     - (S(po, 0, 0, -1) * S(w) + pc * S(w, 0, 0, -1)) / two) / self.dz
+        return float(np.abs(d).max()), d

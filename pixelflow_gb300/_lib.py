@@ -1,0 +1,109 @@
+"""ctypes binding of libpixelflow_gb300.so (include/pixelflow_gpu.h).
+
+There is no fallback: if the library is missing or the CUDA runtime cannot
+run it, loading or the first call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpixelflow_gb300.so")
+
+PF_OK = 0
+PF_PREC_FP64 = 0
+PF_PREC_MIXED = 1
+ERRORS = {
+    -1: "PF_E_INVALID", -2: "PF_E_CUDA", -3: "PF_E_NOMEM", -4: "PF_E_NONFINITE",
+    -5: "PF_E_TIMEOUT", -6: "PF_E_STATE", -7: "PF_E_BUSY",
+}
+
+
+class PfParams(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32), ("m", ctypes.c_int32), ("n", ctypes.c_int32), ("l", ctypes.c_int32),
+        ("xnue", ctypes.c_double), ("xlambda", ctypes.c_double), ("density", ctypes.c_double),
+        ("width", ctypes.c_double), ("height", ctypes.c_double), ("depth", ctypes.c_double),
+        ("time", ctypes.c_double), ("inlet_velocity", ctypes.c_double),
+        ("outlet_pressure", ctypes.c_double), ("aoa", ctypes.c_double),
+        ("istep_max", ctypes.c_int32), ("iter_max", ctypes.c_int32),
+        ("thickness", ctypes.c_double), ("threshold", ctypes.c_double),
+        ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    ]
+
+
+class PfOptions(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int32), ("outer_max", ctypes.c_int32), ("inner_sweeps", ctypes.c_int32),
+        ("track_sor_error", ctypes.c_int32), ("dc_tol", ctypes.c_double), ("use_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
+class PfError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+# name -> (restype, argtypes)
+_VP, _I, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+_PROTOS = {
+    "pf_last_error": (ctypes.c_char_p, []),
+    "pf_strerror": (ctypes.c_char_p, [_I]),
+    "pf_abi_version": (_I, []),
+    "pf_set_device": (_I, [_I]),
+    "pf_device_count": (_I, [ctypes.POINTER(_I)]),
+    "pf_default_options": (None, [ctypes.POINTER(PfOptions)]),
+    "pf_create": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), _VP, ctypes.POINTER(_VP)]),
+    "pf_destroy": (_I, [_VP]),
+    "pf_initial_conditions": (_I, [_VP]),
+    "pf_set_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
+    "pf_get_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
+    "pf_get_porosity": (_I, [_VP, _VP, _I, _I]),
+    "pf_solve_p": (_I, [_VP]),
+    "pf_projection": (_I, [_VP]),
+    "pf_boundary": (_I, [_VP]),
+    "pf_step": (_I, [_VP, _I]),
+    "pf_synchronize": (_I, [_VP]),
+    "pf_norms": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "pf_host_register": (_I, [_VP, ctypes.c_size_t]),
+    "pf_host_unregister": (_I, [_VP]),
+    "pf_profile_begin": (_I, [_VP]),
+    "pf_profile_end": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_D),
+                            ctypes.POINTER(ctypes.c_int64)]),
+    "pf_profile_step_times": (_I, [_VP, _VP, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
+    "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
+}
+
+
+def exported_symbols():
+    """Names the C header declares (for the load/export test)."""
+    return list(_PROTOS)
+
+
+def load():
+    """Load the library (no compute happens here)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(rc: int) -> int:
+    if rc != PF_OK:
+        msg = load().pf_last_error().decode(errors="replace")
+        raise PfError(rc, msg)
+    return rc

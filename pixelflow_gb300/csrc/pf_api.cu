@@ -1,0 +1,633 @@
+// pf_api.cu -- the extern "C" entry points of include/pixelflow_gpu.h for
+// single cases: set-up, field exchange in the reference's Fortran layout,
+// and the step orchestration (stream-ordered launches, CUDA-graph replay,
+// profiling events).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pf_internal.cuh"
+#include "pf_case.cuh"
+
+namespace pf {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? PF_E_NOMEM : PF_E_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+int make_geo(const pf_params& p, Geo& g) {
+  if (p.dim != 2 && p.dim != 3) return fail(PF_E_INVALID, "dim must be 2 or 3");
+  if (p.m < 3 || p.n < 3 || (p.dim == 3 && p.l < 3))
+    return fail(PF_E_INVALID, "grid sizes must be >= 3 in every direction");
+  if (p.m > (1 << 20) || p.n > (1 << 20) || (p.dim == 3 && p.l > (1 << 20)))
+    return fail(PF_E_INVALID, "grid size too large");
+  g.dim = p.dim;
+  g.m = p.m;
+  g.n = p.n;
+  g.l = p.dim == 3 ? p.l : 1;
+  g.X = round_up(g.m + 2, 32);
+  g.Y = g.n + 2;
+  g.Z = p.dim == 3 ? g.l + 2 : 1;
+  g.H = round_up((g.m + 1) / 2 + 1, 32);
+  g.nat = (long long)g.X * g.Y * g.Z;
+  g.pk = (long long)g.H * g.Y * g.Z;
+  g.jn_n = (g.n % 2 == 0) ? 1 : g.n + 1;
+  g.js_1 = (g.n % 2 == 0) ? g.n : 0;
+  g.kt_l = (g.l % 2 == 0) ? 1 : g.l + 1;
+  g.kb_1 = (g.l % 2 == 0) ? g.l : 0;
+  return PF_OK;
+}
+
+int make_scal(const pf_params& p, Scal& s) {
+  if (!(p.istep_max > 0)) return fail(PF_E_INVALID, "istep_max must be > 0");
+  if (p.iter_max < 0) return fail(PF_E_INVALID, "iter_max must be >= 0");
+  if (!(p.density != 0.0)) return fail(PF_E_INVALID, "density must be nonzero");
+  if (!(p.width > 0 && p.height > 0 && (p.dim == 2 || p.depth > 0)))
+    return fail(PF_E_INVALID, "width/height/depth must be > 0");
+  s.dx = p.width / double(p.m - 1);
+  s.dy = p.height / double(p.n - 1);
+  s.dz = p.dim == 3 ? p.depth / double(p.l - 1) : 0.0;
+  s.dt = p.time / double(p.istep_max);
+  s.xnue = p.xnue;
+  s.xlambda = p.xlambda;
+  s.density = p.density;
+  s.thickness = p.thickness;
+  s.threshold = p.threshold;
+  s.outlet_pressure = p.outlet_pressure;
+  s.omega = p.relux_factor;
+  s.nonslip = p.nonslip ? 1 : 0;
+  const double pi = std::atan(1.0) * 4.0;
+  // boundary(): 2D cos(AoA/180*pi) (ibm_2d:478), 3D cos(AoA/1300*pi) (ibm_3d:695)
+  const double ab = p.dim == 3 ? p.aoa / 1300.0 * pi : p.aoa / 180.0 * pi;
+  s.inlet_u = p.inlet_velocity * std::cos(ab);
+  s.inlet_v = p.inlet_velocity * std::sin(ab);
+  s.inlet_w = 0.0;
+  // initial_conditions(): 2D AoA/180 (ibm_2d:560), 3D AoA/360 (ibm_3d:782)
+  const double ai = p.dim == 3 ? p.aoa / 360.0 * pi : p.aoa / 180.0 * pi;
+  s.init_u = p.inlet_velocity * std::cos(ai);
+  s.init_v = p.inlet_velocity * std::sin(ai);
+  return PF_OK;
+}
+
+// Porosity with ghosts in the dense staging layout, as grid_conditions does:
+// clamp max(value, threshold) (grid.f90:43), x-ghost copy, then periodic y
+// (and z) ghosts (grid.f90:92-106 2D, :349-378 3D).
+void build_porosity(const Geo& g, double threshold, const double* vals, std::vector<double>& out) {
+  const int m = g.m, n = g.n, l = g.l;
+  const long long M = m + 2, N = n + 2;
+  out.assign((size_t)M * N * g.Z, 0.0);
+  auto at = [&](int i, int j, int k) -> double& { return out[(size_t)i + M * ((size_t)j + N * k)]; };
+  const int k0 = g.dim == 3 ? 1 : 0, k1 = g.dim == 3 ? l : 0;
+  size_t q = 0;
+  for (int k = k0; k <= k1; k++)
+    for (int j = 1; j <= n; j++)
+      for (int i = 1; i <= m; i++) {
+        const double v = vals[q++];
+        at(i, j, k) = v > threshold ? v : threshold;
+      }
+  if (g.dim == 2) {
+    for (int j = 1; j <= n + 1; j++) {
+      at(0, j, 0) = at(1, j, 0);
+      at(m + 1, j, 0) = at(m, j, 0);
+    }
+    for (int i = 0; i <= m + 1; i++) {
+      at(i, 0, 0) = at(i, n, 0);
+      at(i, n + 1, 0) = at(i, 1, 0);
+    }
+  } else {
+    for (int j = 1; j <= n + 1; j++)
+      for (int k = 1; k <= l + 1; k++) {
+        at(0, j, k) = at(1, j, k);
+        at(m + 1, j, k) = at(m, j, k);
+      }
+    for (int i = 0; i <= m + 1; i++)
+      for (int k = 0; k <= l + 1; k++) {
+        at(i, 0, k) = at(i, n, k);
+        at(i, n + 1, k) = at(i, 1, k);
+      }
+    for (int i = 0; i <= m + 1; i++)
+      for (int j = 0; j <= n + 1; j++) {
+        at(i, j, 0) = at(i, j, l);
+        at(i, j, l + 1) = at(i, j, 1);
+      }
+  }
+}
+
+}  // namespace pf
+
+using namespace pf;
+
+// ---------------------------------------------------------------------------
+// Device memory of one case: one allocation carved into 256-byte aligned
+// arrays (natural fields, packed p and SOR operator, staging, reductions).
+static int case_alloc(pf_case* c) {
+  const Geo& g = c->g;
+  const size_t nat = (size_t)g.nat * sizeof(double), pk = (size_t)g.pk * sizeof(double);
+  const size_t stage = (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double);
+  const bool three = g.dim == 3;
+  struct Req {
+    double** dst;
+    size_t bytes;
+  };
+  std::vector<Req> req;
+  req.push_back({&c->poro, nat});
+  req.push_back({&c->gx, nat});
+  req.push_back({&c->gy, nat});
+  req.push_back({&c->gz, three ? nat : 0});
+  req.push_back({&c->rinv, nat});
+  req.push_back({&c->damp, nat});
+  req.push_back({&c->div, nat});
+  for (int b = 0; b < 2; b++) {
+    req.push_back({&c->U[b], nat});
+    req.push_back({&c->V[b], nat});
+    req.push_back({&c->W[b], three ? nat : 0});
+  }
+  req.push_back({&c->p[0], pk});
+  req.push_back({&c->p[1], pk});
+  for (int col = 0; col < 2; col++) {
+    for (int d = 0; d < 6; d++) req.push_back({&c->C[col].a[d], (d < 2 * g.dim) ? pk : 0});
+    req.push_back({&c->C[col].bbn, pk});
+    req.push_back({&c->C[col].wap, pk});
+    req.push_back({&c->C[col].oadd, pk});
+  }
+  req.push_back({&c->stage, stage});
+  size_t total = 0;
+  for (auto& r : req) total += (r.bytes + 255) / 256 * 256;
+  total += 256;  // reductions
+  char* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, total);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(case)");
+  c->base = base;
+  c->bytes = total;
+  size_t off = 0;
+  for (auto& r : req) {
+    *r.dst = r.bytes ? reinterpret_cast<double*>(base + off) : nullptr;
+    off += (r.bytes + 255) / 256 * 256;
+  }
+  c->red = reinterpret_cast<unsigned long long*>(base + off);
+  PF_CUDA(cudaMemsetAsync(base, 0, total, c->st));
+  return PF_OK;
+}
+
+static void case_free(pf_case* c) {
+  if (!c) return;
+  for (int b = 0; b < 2; b++)
+    if (c->gexec[b]) cudaGraphExecDestroy(c->gexec[b]);
+  for (auto& e : c->events) cudaEventDestroy(e);
+  if (c->base) cudaFree(c->base);
+  mixed_free(c);
+  if (c->hred) cudaFreeHost(c->hred);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+// solve_p on the device: snapshot (buffer swap), divergence, predictor,
+// RHS, SOR.  Only stream-ordered launches, so it can be graph-captured.
+static void enqueue_solve_p(pf_case* c, bool prof) {
+  const Geo& g = c->g;
+  const Scal& s = c->s;
+  cudaStream_t st = c->st;
+  const int o = c->cur, nw = 1 - c->cur;
+  const bool track = c->opt.track_sor_error != 0;
+  if (track) cudaMemsetAsync(&c->red[0], 0, sizeof(unsigned long long), st);
+  launch_divergence<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, st);
+  launch_predictor<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv, c->damp,
+                           c->U[nw], c->V[nw], c->W[nw], st);
+  launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
+  if (prof) cudaEventRecord(c->ev_cur[1], st);
+  const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
+  const double omw = 1.0 - s.omega;
+  for (int it = 0; it < c->prm.iter_max; it++) {
+    for (int col = 0; col < 2; col++) {
+      if (halo) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
+      // 2D tracks both half-sweeps (ibm_2d:351,385); 3D only the second (ibm_3d:575-583)
+      unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[0] : nullptr;
+      launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, st);
+    }
+  }
+  if (prof) cudaEventRecord(c->ev_cur[2], st);
+  launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
+  c->launches += 4 + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
+  c->cur = nw;
+}
+
+static void enqueue_projection(pf_case* c) {
+  const int b = c->cur;
+  c->launches += 1;
+  launch_projection<double>(c->g, c->s, c->p[0], c->p[1], c->U[b], c->V[b], c->W[b], c->st);
+}
+
+static void enqueue_boundary(pf_case* c) {
+  const int b = c->cur;
+  c->launches += c->g.dim == 3 ? 3 : 2;
+  launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
+}
+
+static void enqueue_step(pf_case* c, bool prof) {
+  if (c->opt.precision == PF_PREC_MIXED) {
+    enqueue_solve_p_mixed(c, prof);
+    enqueue_projection_mixed(c);
+    enqueue_boundary_mixed(c);
+  } else {
+    enqueue_solve_p(c, prof);
+    enqueue_projection(c);
+    enqueue_boundary(c);
+  }
+}
+
+static int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return PF_OK;
+}
+
+static int step_graph(pf_case* c) {
+  const int b = c->cur;
+  if (!c->gexec[b]) {
+    cudaGraph_t graph = nullptr;
+    PF_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = c->launches;
+    enqueue_step(c, false);
+    c->graph_kernels[b] = c->launches - before;
+    c->launches = before;
+    cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+    c->cur = b;  // capture only recorded the swap
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->gexec[b], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  PF_CUDA(cudaGraphLaunch(c->gexec[b], c->st));
+  c->launches += c->graph_kernels[b];
+  c->cur = 1 - b;
+  return PF_OK;
+}
+
+static int ensure_events(pf_case* c, size_t need) {
+  while (c->events.size() < need) {
+    cudaEvent_t e;
+    PF_CUDA(cudaEventCreate(&e));
+    c->events.push_back(e);
+  }
+  return PF_OK;
+}
+
+extern "C" {
+
+const char* pf_last_error(void) { return g_last_error.c_str(); }
+
+const char* pf_strerror(int code) {
+  switch (code) {
+    case PF_OK: return "ok";
+    case PF_E_INVALID: return "invalid argument";
+    case PF_E_CUDA: return "CUDA error";
+    case PF_E_NOMEM: return "out of device memory";
+    case PF_E_NONFINITE: return "non-finite values in the fields";
+    case PF_E_TIMEOUT: return "bounded device wait expired";
+    case PF_E_STATE: return "invalid state";
+    case PF_E_BUSY: return "no free slot";
+    default: return "unknown error";
+  }
+}
+
+int pf_abi_version(void) { return PF_ABI_VERSION; }
+
+int pf_set_device(int device) {
+  PF_CUDA(cudaSetDevice(device));
+  return PF_OK;
+}
+
+int pf_device_count(int* count) {
+  if (!count) return fail(PF_E_INVALID, "null argument");
+  PF_CUDA(cudaGetDeviceCount(count));
+  return PF_OK;
+}
+
+void pf_default_options(pf_options* opt) {
+  if (!opt) return;
+  std::memset(opt, 0, sizeof(*opt));
+  opt->precision = PF_PREC_FP64;
+  opt->outer_max = 4;
+  opt->inner_sweeps = 25;
+  opt->track_sor_error = 1;
+  opt->dc_tol = 0.0;
+  opt->use_graph = 1;
+}
+
+int pf_create(const pf_params* prm, const pf_options* opt, const double* porosity_values, pf_case** out) {
+  if (!prm || !porosity_values || !out) return fail(PF_E_INVALID, "pf_create: null argument");
+  *out = nullptr;
+  pf_case* c = new pf_case();
+  c->prm = *prm;
+  if (opt)
+    c->opt = *opt;
+  else
+    pf_default_options(&c->opt);
+  int rc = make_geo(c->prm, c->g);
+  if (rc == PF_OK) rc = make_scal(c->prm, c->s);
+  if (rc == PF_OK && c->opt.precision != PF_PREC_FP64 && c->opt.precision != PF_PREC_MIXED)
+    rc = fail(PF_E_INVALID, "unknown precision");
+  if (rc != PF_OK) {
+    delete c;
+    return rc;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  rc = case_alloc(c);
+  if (rc == PF_OK) {
+    e = cudaHostAlloc(&c->hred, 4 * sizeof(unsigned long long), cudaHostAllocDefault);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaHostAlloc");
+  }
+  if (rc == PF_OK && c->opt.precision == PF_PREC_MIXED) rc = mixed_alloc(c);
+  if (rc != PF_OK) {
+    case_free(c);
+    return rc;
+  }
+  // porosity with ghosts (host, once), then the time-invariant factors
+  std::vector<double> por;
+  build_porosity(c->g, c->prm.threshold, porosity_values, por);
+  const Geo& g = c->g;
+  e = cudaMemcpyAsync(c->stage, por.data(), por.size() * sizeof(double), cudaMemcpyHostToDevice, c->st);
+  if (e != cudaSuccess) {
+    case_free(c);
+    return cuda_fail(e, "cudaMemcpyAsync(porosity)");
+  }
+  launch_scatter_nat(g, c->stage, c->poro, c->st);
+  launch_porosity_factors(g, c->s, c->poro, c->gx, c->gy, c->gz, c->rinv, c->damp, c->st);
+  launch_setup_coef(g, c->s, c->poro, c->C[0], c->C[1], c->st);
+  if (c->opt.precision == PF_PREC_MIXED) mixed_setup(c);
+  rc = check_launch("pf_create kernels");
+  if (rc == PF_OK) {
+    e = cudaStreamSynchronize(c->st);  // `por` goes out of scope
+    if (e != cudaSuccess) rc = cuda_fail(e, "pf_create sync");
+  }
+  if (rc != PF_OK) {
+    case_free(c);
+    return rc;
+  }
+  *out = c;
+  return PF_OK;
+}
+
+int pf_destroy(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "pf_destroy: null handle");
+  cudaStreamSynchronize(c->st);
+  case_free(c);
+  return PF_OK;
+}
+
+int pf_initial_conditions(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  const Geo& g = c->g;
+  const size_t nat = (size_t)g.nat * sizeof(double), pk = (size_t)g.pk * sizeof(double);
+  c->cur = 0;
+  PF_CUDA(cudaMemsetAsync(c->U[0], 0, nat, c->st));
+  PF_CUDA(cudaMemsetAsync(c->V[0], 0, nat, c->st));
+  if (g.dim == 3) PF_CUDA(cudaMemsetAsync(c->W[0], 0, nat, c->st));
+  PF_CUDA(cudaMemsetAsync(c->p[0], 0, pk, c->st));
+  PF_CUDA(cudaMemsetAsync(c->p[1], 0, pk, c->st));
+  launch_initial<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
+  launch_boundary<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
+  c->launches += 1 + (g.dim == 3 ? 3 : 2);
+  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_from_fp64(c);
+  return check_launch("pf_initial_conditions");
+}
+
+static int check_ld(const pf_case* c, int ld1, int ld2) {
+  if (ld1 < c->g.m + 2 || ld2 < c->g.n + 2) return fail(PF_E_INVALID, "leading dimensions smaller than m+2, n+2");
+  return PF_OK;
+}
+
+static cudaMemcpy3DParms copy_params(const pf_case* c, const void* src, size_t src_pitch, int src_rows,
+                                     void* dst, size_t dst_pitch, int dst_rows, cudaMemcpyKind kind) {
+  const Geo& g = c->g;
+  cudaMemcpy3DParms P;
+  std::memset(&P, 0, sizeof(P));
+  P.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), src_pitch, (size_t)(g.m + 2) * sizeof(double), src_rows);
+  P.dstPtr = make_cudaPitchedPtr(dst, dst_pitch, (size_t)(g.m + 2) * sizeof(double), dst_rows);
+  P.extent = make_cudaExtent((size_t)(g.m + 2) * sizeof(double), g.n + 2, g.Z);
+  P.kind = kind;
+  return P;
+}
+
+int pf_set_state(pf_case* c, const double* u, const double* v, const double* w, const double* p, int ld1,
+                 int ld2) {
+  if (!c || !u || !v || !p || (c->g.dim == 3 && !w)) return fail(PF_E_INVALID, "pf_set_state: null argument");
+  int rc = check_ld(c, ld1, ld2);
+  if (rc) return rc;
+  const Geo& g = c->g;
+  const size_t hp = (size_t)ld1 * sizeof(double), dp = (size_t)g.X * sizeof(double);
+  const int b = c->cur;
+  const double* src[3] = {u, v, w};
+  double* dst[3] = {c->U[b], c->V[b], c->W[b]};
+  for (int f = 0; f < g.dim; f++) {
+    cudaMemcpy3DParms P = copy_params(c, src[f], hp, ld2, dst[f], dp, g.Y, cudaMemcpyHostToDevice);
+    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  }
+  cudaMemcpy3DParms P = copy_params(c, p, hp, ld2, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2,
+                                    cudaMemcpyHostToDevice);
+  PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  launch_scatter_pk(g, c->stage, c->p[0], c->p[1], c->st);
+  c->launches += 1;
+  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_from_fp64(c);
+  return check_launch("pf_set_state");
+}
+
+int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1, int ld2) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  int rc = check_ld(c, ld1, ld2);
+  if (rc) return rc;
+  const Geo& g = c->g;
+  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_to_fp64(c);
+  const size_t hp = (size_t)ld1 * sizeof(double), dp = (size_t)g.X * sizeof(double);
+  const int b = c->cur;
+  double* dst[3] = {u, v, w};
+  const double* src[3] = {c->U[b], c->V[b], c->W[b]};
+  for (int f = 0; f < g.dim; f++) {
+    if (!dst[f]) continue;
+    cudaMemcpy3DParms P = copy_params(c, src[f], dp, g.Y, dst[f], hp, ld2, cudaMemcpyDeviceToHost);
+    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  }
+  if (p) {
+    launch_gather_pk(g, c->p[0], c->p[1], c->stage, c->st);
+    c->launches += 1;
+    cudaMemcpy3DParms P = copy_params(c, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2, p, hp, ld2,
+                                      cudaMemcpyDeviceToHost);
+    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  }
+  rc = check_launch("pf_get_state");
+  if (rc) return rc;
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  return PF_OK;
+}
+
+int pf_get_porosity(pf_case* c, double* poro, int ld1, int ld2) {
+  if (!c || !poro) return fail(PF_E_INVALID, "null argument");
+  int rc = check_ld(c, ld1, ld2);
+  if (rc) return rc;
+  const Geo& g = c->g;
+  cudaMemcpy3DParms P = copy_params(c, c->poro, (size_t)g.X * sizeof(double), g.Y, poro,
+                                    (size_t)ld1 * sizeof(double), ld2, cudaMemcpyDeviceToHost);
+  PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  return PF_OK;
+}
+
+int pf_solve_p(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (c->opt.precision == PF_PREC_MIXED)
+    enqueue_solve_p_mixed(c, false);
+  else
+    enqueue_solve_p(c, false);
+  return check_launch("pf_solve_p");
+}
+
+int pf_projection(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (c->opt.precision == PF_PREC_MIXED)
+    enqueue_projection_mixed(c);
+  else
+    enqueue_projection(c);
+  return check_launch("pf_projection");
+}
+
+int pf_boundary(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (c->opt.precision == PF_PREC_MIXED)
+    enqueue_boundary_mixed(c);
+  else
+    enqueue_boundary(c);
+  return check_launch("pf_boundary");
+}
+
+int pf_step(pf_case* c, int nsteps) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (nsteps < 0) return fail(PF_E_INVALID, "nsteps < 0");
+  for (int s = 0; s < nsteps; s++) {
+    if (c->profiling) {
+      int rc = ensure_events(c, (size_t)(c->prof_steps + 1) * 4);
+      if (rc) return rc;
+      cudaEvent_t* ev = &c->events[(size_t)c->prof_steps * 4];
+      c->ev_cur = ev;
+      cudaEventRecord(ev[0], c->st);
+      enqueue_step(c, true);
+      cudaEventRecord(ev[3], c->st);
+      c->prof_steps++;
+    } else if (c->opt.use_graph) {
+      int rc = step_graph(c);
+      if (rc) return rc;
+    } else {
+      enqueue_step(c, false);
+    }
+  }
+  return check_launch("pf_step");
+}
+
+int pf_synchronize(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  return PF_OK;
+}
+
+int pf_norms(pf_case* c, double* max_div, double* sor_error) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  const Geo& g = c->g;
+  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_to_fp64(c);
+  PF_CUDA(cudaMemsetAsync(&c->red[1], 0, sizeof(unsigned long long), c->st));
+  const int b = c->cur;
+  launch_div_diag<double>(g, c->s, c->U[b], c->V[b], c->W[b], c->poro, c->gx, c->gy, c->gz, &c->red[1], c->st);
+  c->launches += 1;
+  int rc = check_launch("pf_norms");
+  if (rc) return rc;
+  PF_CUDA(cudaMemcpyAsync(c->hred, c->red, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  double e, d;
+  unsigned long long be = c->hred[0], bd = c->hred[1];
+  std::memcpy(&e, &be, sizeof(double));
+  std::memcpy(&d, &bd, sizeof(double));
+  if (sor_error) *sor_error = e;
+  if (max_div) *max_div = d;
+  if (!std::isfinite(d)) return fail(PF_E_NONFINITE, "max|div u| is not finite");
+  return PF_OK;
+}
+
+int pf_host_register(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return fail(PF_E_INVALID, "null argument");
+  PF_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return PF_OK;
+}
+
+int pf_host_unregister(void* ptr) {
+  if (!ptr) return fail(PF_E_INVALID, "null argument");
+  PF_CUDA(cudaHostUnregister(ptr));
+  return PF_OK;
+}
+
+int pf_profile_begin(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  c->profiling = true;
+  c->prof_steps = 0;
+  return PF_OK;
+}
+
+int pf_profile_end(pf_case* c, double* sor_ms, int64_t* sor_launches, double* step_ms, int64_t* steps) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (!c->profiling) return fail(PF_E_STATE, "profiling not started");
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  double sor = 0, step = 0;
+  c->step_times.clear();
+  for (int64_t s = 0; s < c->prof_steps; s++) {
+    float a = 0, b = 0;
+    cudaEvent_t* ev = &c->events[(size_t)s * 4];
+    PF_CUDA(cudaEventElapsedTime(&a, ev[1], ev[2]));
+    PF_CUDA(cudaEventElapsedTime(&b, ev[0], ev[3]));
+    sor += a;
+    step += b;
+    c->step_times.push_back(b);
+  }
+  if (sor_ms) *sor_ms = sor;
+  if (step_ms) *step_ms = step;
+  if (steps) *steps = c->prof_steps;
+  if (sor_launches) *sor_launches = c->prof_steps * c->sor_launches_per_step();
+  c->profiling = false;
+  return PF_OK;
+}
+
+int pf_profile_step_times(pf_case* c, double* ms, int64_t max_steps, int64_t* n) {
+  if (!c || !ms || !n) return fail(PF_E_INVALID, "null argument");
+  int64_t k = 0;
+  for (; k < max_steps && k < (int64_t)c->step_times.size(); k++) ms[k] = c->step_times[(size_t)k];
+  *n = k;
+  return PF_OK;
+}
+
+int pf_kernel_launches(pf_case* c, int64_t* count) {
+  if (!c || !count) return fail(PF_E_INVALID, "null argument");
+  *count = c->launches;
+  return PF_OK;
+}
+
+int pf_memory_bytes(pf_case* c, size_t* bytes) {
+  if (!c || !bytes) return fail(PF_E_INVALID, "null argument");
+  *bytes = c->bytes + c->mixed_bytes;
+  return PF_OK;
+}
+
+}  // extern "C"

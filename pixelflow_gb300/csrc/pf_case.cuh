@@ -1,0 +1,62 @@
+// pf_case.cuh -- the case handle behind the opaque pf_case of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "pf_internal.cuh"
+
+struct pf_case {
+  pf_params prm{};
+  pf_options opt{};
+  pf::Geo g{};
+  pf::Scal s{};
+  cudaStream_t st = nullptr;
+  char* base = nullptr;  // one device allocation for the FP64 arrays
+  size_t bytes = 0;
+  // natural layout, FP64
+  double *poro = nullptr, *gx = nullptr, *gy = nullptr, *gz = nullptr, *rinv = nullptr, *damp = nullptr;
+  double* div = nullptr;
+  double *U[2] = {nullptr, nullptr}, *V[2] = {nullptr, nullptr}, *W[2] = {nullptr, nullptr};
+  int cur = 0;  // buffer holding the current velocities
+  // packed red-black, FP64
+  double* p[2] = {nullptr, nullptr};
+  pf::Coef<double> C[2]{};
+  double* stage = nullptr;          // dense (m+2)(n+2)[(l+2)] staging
+  unsigned long long* red = nullptr;   // [0] SOR error bits, [1] max|div| bits, [2] max|r| bits, [3] flag
+  unsigned long long* hred = nullptr;  // pinned host mirror
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  // profiling
+  bool profiling = false;
+  int64_t prof_steps = 0;
+  std::vector<cudaEvent_t> events;
+  cudaEvent_t* ev_cur = nullptr;
+  std::vector<double> step_times;  // ms, last profiling session
+  int64_t launches = 0;            // kernels launched so far
+  int64_t graph_kernels[2] = {0, 0};
+
+  // ---- mixed precision form (pf_mixed.cu) ----
+  char* mbase = nullptr;
+  size_t mixed_bytes = 0;
+  float *Uf[2] = {nullptr, nullptr}, *Vf[2] = {nullptr, nullptr}, *Wf[2] = {nullptr, nullptr};
+  float* divf = nullptr;
+  float* e[2] = {nullptr, nullptr};  // packed FP32 correction
+  pf::Coef<float> Cf[2]{};           // FP32 operator; bbn holds the normalised residual
+  int* skip = nullptr;               // device flag: defect correction converged
+
+  int64_t sor_launches_per_step() const {
+    if (opt.precision == PF_PREC_MIXED) return 2LL * opt.outer_max * opt.inner_sweeps;
+    return 2LL * prm.iter_max;
+  }
+};
+
+namespace pf {
+int mixed_alloc(pf_case* c);
+void mixed_free(pf_case* c);
+void mixed_setup(pf_case* c);
+void mixed_sync_from_fp64(pf_case* c);
+void mixed_sync_to_fp64(pf_case* c);
+void enqueue_solve_p_mixed(pf_case* c, bool prof);
+void enqueue_projection_mixed(pf_case* c);
+void enqueue_boundary_mixed(pf_case* c);
+}  // namespace pf

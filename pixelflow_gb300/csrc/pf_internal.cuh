@@ -1,0 +1,132 @@
+// pf_internal.cuh -- device layout, kernel declarations and host helpers
+// shared by the translation units of libpixelflow_gb300.so.
+//
+// Device data layout (one case):
+//  * "natural" arrays (u, v, w, div, porosity and time-invariant predictor
+//    factors): i fastest with the ghost layer, element (i,j,k) at
+//    i + X*(j + Y*k), X = m+2 rounded up to 32 elements (256 B rows for
+//    FP64), Y = n+2, and Z = l+2 planes (one plane, k = 0, in 2D).
+//  * "packed" red-black arrays (p, SOR coefficients, RHS): cell (i,j,k) has
+//    colour c = (i + j + kk) & 1, kk = k in 3D and 1 in 2D, so colour 0 is
+//    the reference's first half-sweep ((i+j) odd in 2D, (i+j+k) even in 3D).
+//    It lives in the colour-c array at h = i >> 1, element h + H*(j + Y*k),
+//    H = (m+2)/2 rounded up to 32.  A cell's x-neighbours are the
+//    other-colour elements h-1+s and h+s (s = i & 1); its y/z neighbours are
+//    element h of the neighbouring rows.  Each half-sweep therefore streams
+//    one colour contiguously and reads the other colour contiguously.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/pixelflow_gpu.h"
+
+namespace pf {
+
+struct Geo {
+  int dim, m, n, l;   // l == 1 in 2D
+  int X, Y, Z;        // natural pitch, rows, planes
+  int H;              // packed pitch
+  long long nat;      // X*Y*Z elements per natural array
+  long long pk;       // H*Y*Z elements per packed colour array
+  // neighbour rows of the periodic edges used by the SOR: a wrap to the
+  // opposite interior row when it has the other colour (even n / l), else
+  // the ghost row, refreshed before every half-sweep like the reference.
+  int jn_n, js_1, kt_l, kb_1;
+};
+
+__host__ __device__ inline long long nat_idx(const Geo& g, int i, int j, int k) {
+  return (long long)i + (long long)g.X * ((long long)j + (long long)g.Y * k);
+}
+__host__ __device__ inline long long pk_idx(const Geo& g, int h, int j, int k) {
+  return (long long)h + (long long)g.H * ((long long)j + (long long)g.Y * k);
+}
+__host__ __device__ inline int colour_of(const Geo& g, int i, int j, int k) {
+  return (i + j + (g.dim == 3 ? k : 1)) & 1;
+}
+
+// Scalars of one case, derived once on the host in double.
+struct Scal {
+  double dx, dy, dz, dt;
+  double xnue, xlambda, density, thickness, threshold;
+  double inlet_u, inlet_v, inlet_w;  // boundary() inflow values
+  double init_u, init_v;             // initial_conditions() values
+  double outlet_pressure, omega;
+  int nonslip;
+};
+
+// Time-invariant SOR operator of one colour, normalised by omega/ap:
+//   p_new = (1-omega) p + bbn - sum_nb a_nb p_nb
+template <typename T>
+struct Coef {
+  T* a[6];   // e, w, n, s, t, b
+  T* bbn;    // RHS * omega/ap (rewritten every step)
+  T* wap;    // omega/ap
+  T* oadd;   // ae*p(m+1) kept for the outlet row (boundrary_matrix), else 0
+};
+
+// ---- kernels (pf_kernels.cu) ----------------------------------------
+// TV: velocity type, TP / TC: pressure and operator type.  The plain step
+// uses double throughout; the mixed form uses float velocities with the
+// FP64 pressure and operator, and float for the correction sweeps.
+void launch_porosity_factors(const Geo& g, const Scal& s, const double* poro, double* gx, double* gy,
+                             double* gz, double* rinv, double* damp, cudaStream_t st);
+void launch_setup_coef(const Geo& g, const Scal& s, const double* poro, Coef<double> c0, Coef<double> c1,
+                       cudaStream_t st);
+template <typename TV>
+void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, TV* div,
+                       cudaStream_t st);
+template <typename TV>
+void launch_predictor(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, const TV* div,
+                      const double* gx, const double* gy, const double* gz, const double* rinv,
+                      const double* damp, TV* u, TV* v, TV* w, cudaStream_t st);
+template <typename TV>
+void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
+                const double* gx, const double* gy, const double* gz, Coef<double> c0, Coef<double> c1,
+                cudaStream_t st);
+template <typename T>
+void launch_sor_half(const Geo& g, const Coef<T>& cc, T* pc, const T* po, T one_minus_omega, int colour,
+                     unsigned long long* err, const int* skip, cudaStream_t st);
+template <typename T>
+void launch_p_halo(const Geo& g, T* p0, T* p1, const int* skip, cudaStream_t st);
+template <typename TV>
+void launch_projection(const Geo& g, const Scal& s, const double* p0, const double* p1, TV* u, TV* v, TV* w,
+                       cudaStream_t st);
+template <typename TV>
+void launch_boundary(const Geo& g, const Scal& s, TV* u, TV* v, TV* w, double* p0, double* p1,
+                     cudaStream_t st);
+template <typename TV>
+void launch_initial(const Geo& g, const Scal& s, TV* u, TV* v, TV* w, double* p0, double* p1,
+                    cudaStream_t st);
+template <typename TV>
+void launch_div_diag(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
+                     const double* gx, const double* gy, const double* gz, unsigned long long* out,
+                     cudaStream_t st);
+// mixed precision form
+void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, const double* po, double omega,
+                     int colour, float* rf, float* ec, unsigned long long* rmax, const int* skip,
+                     cudaStream_t st);
+void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, const float* e1, const int* skip,
+                       cudaStream_t st);
+void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
+void launch_coef_to_float(const Geo& g, const Coef<double>& c, Coef<float> cf, cudaStream_t st);
+void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
+void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
+// staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts
+void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st);
+void launch_scatter_pk(const Geo& g, const double* stage, double* p0, double* p1, cudaStream_t st);
+void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* stage, cudaStream_t st);
+
+// ---- host error plumbing (pf_api.cu) ----------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+}  // namespace pf
+
+#define PF_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t _e = (call);                            \
+    if (_e != cudaSuccess) return pf::cuda_fail(_e, #call); \
+  } while (0)

@@ -1,0 +1,141 @@
+// pf_mixed.cu -- the precision form of the step: FP32 velocity stencils and
+// FP32 red-black sweeps inside an FP64 defect-correction loop.
+//
+// FP64 stays in: the pressure p and its accumulation p += e, the Poisson
+// residual r (normalised by omega/ap), the RHS bb, and every norm.  FP32:
+// the velocities and their stencils (divergence, predictor, projection,
+// boundary), the operator copy used by the sweeps, and the correction e.
+// Per step: outer_max passes of { r = bbn - w p - sum a p_nb (FP64);
+// inner_sweeps FP32 SOR iterations on e from e = 0; p += e (FP64) }.
+// With outer_max * inner_sweeps == iter_max the pass structure reproduces
+// the plain SOR's iterates up to the FP32 rounding of e; dc_tol > 0 ends
+// the passes of a step early once max|r|/omega <= dc_tol (a device flag, so
+// the step stays one graph).
+#include <cuda_runtime.h>
+
+#include "pf_case.cuh"
+#include "pf_internal.cuh"
+
+namespace pf {
+
+int mixed_alloc(pf_case* c) {
+  const Geo& g = c->g;
+  const size_t nat = (size_t)g.nat * sizeof(float), pk = (size_t)g.pk * sizeof(float);
+  const bool three = g.dim == 3;
+  struct Req {
+    float** dst;
+    size_t bytes;
+  };
+  Req req[32];
+  int nr = 0;
+  for (int b = 0; b < 2; b++) {
+    req[nr++] = {&c->Uf[b], nat};
+    req[nr++] = {&c->Vf[b], nat};
+    req[nr++] = {&c->Wf[b], three ? nat : 0};
+  }
+  req[nr++] = {&c->divf, nat};
+  req[nr++] = {&c->e[0], pk};
+  req[nr++] = {&c->e[1], pk};
+  for (int col = 0; col < 2; col++) {
+    for (int d = 0; d < 6; d++) req[nr++] = {&c->Cf[col].a[d], d < 2 * g.dim ? pk : 0};
+    req[nr++] = {&c->Cf[col].bbn, pk};
+    c->Cf[col].wap = nullptr;
+    c->Cf[col].oadd = nullptr;
+  }
+  size_t total = 256;  // flag
+  for (int r = 0; r < nr; r++) total += (req[r].bytes + 255) / 256 * 256;
+  char* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, total);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(mixed)");
+  c->mbase = base;
+  c->mixed_bytes = total;
+  size_t off = 0;
+  for (int r = 0; r < nr; r++) {
+    *req[r].dst = req[r].bytes ? reinterpret_cast<float*>(base + off) : nullptr;
+    off += (req[r].bytes + 255) / 256 * 256;
+  }
+  c->skip = reinterpret_cast<int*>(base + off);
+  PF_CUDA(cudaMemsetAsync(base, 0, total, c->st));
+  return PF_OK;
+}
+
+void mixed_free(pf_case* c) {
+  if (c->mbase) cudaFree(c->mbase);
+  c->mbase = nullptr;
+}
+
+void mixed_setup(pf_case* c) {
+  for (int col = 0; col < 2; col++) launch_coef_to_float(c->g, c->C[col], c->Cf[col], c->st);
+}
+
+void mixed_sync_from_fp64(pf_case* c) {
+  const int b = c->cur;
+  c->launches += c->g.dim;
+  const long long n = c->g.nat;
+  launch_to_float(c->U[b], c->Uf[b], n, c->st);
+  launch_to_float(c->V[b], c->Vf[b], n, c->st);
+  if (c->g.dim == 3) launch_to_float(c->W[b], c->Wf[b], n, c->st);
+}
+
+void mixed_sync_to_fp64(pf_case* c) {
+  const int b = c->cur;
+  c->launches += c->g.dim;
+  const long long n = c->g.nat;
+  launch_to_double(c->Uf[b], c->U[b], n, c->st);
+  launch_to_double(c->Vf[b], c->V[b], n, c->st);
+  if (c->g.dim == 3) launch_to_double(c->Wf[b], c->W[b], n, c->st);
+}
+
+void enqueue_solve_p_mixed(pf_case* c, bool prof) {
+  const Geo& g = c->g;
+  const Scal& s = c->s;
+  cudaStream_t st = c->st;
+  const int o = c->cur, nw = 1 - c->cur;
+  const bool track = c->opt.track_sor_error != 0;
+  const bool early = c->opt.dc_tol > 0.0;
+  const int* skip = early ? c->skip : nullptr;
+  if (track) cudaMemsetAsync(&c->red[0], 0, sizeof(unsigned long long), st);
+  if (early) cudaMemsetAsync(c->skip, 0, sizeof(int), st);
+  launch_divergence<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, st);
+  launch_predictor<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, c->gx, c->gy, c->gz, c->rinv, c->damp,
+                          c->Uf[nw], c->Vf[nw], c->Wf[nw], st);
+  launch_rhs<float>(g, s, c->Uf[nw], c->Vf[nw], c->Wf[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
+  if (prof) cudaEventRecord(c->ev_cur[1], st);
+  const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
+  const float omw = (float)(1.0 - s.omega);
+  for (int pass = 0; pass < c->opt.outer_max; pass++) {
+    cudaMemsetAsync(&c->red[2], 0, sizeof(unsigned long long), st);
+    for (int col = 0; col < 2; col++)
+      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->Cf[col].bbn, c->e[col], &c->red[2],
+                      skip, st);
+    if (early) launch_dc_check(&c->red[2], c->opt.dc_tol * s.omega, c->skip, st);
+    for (int it = 0; it < c->opt.inner_sweeps; it++) {
+      for (int col = 0; col < 2; col++) {
+        if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
+        unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[0] : nullptr;
+        launch_sor_half<float>(g, c->Cf[col], c->e[col], c->e[1 - col], omw, col, err, skip, st);
+      }
+    }
+    launch_accumulate(g, c->p[0], c->p[1], c->e[0], c->e[1], skip, st);
+    if (halo) launch_p_halo<double>(g, c->p[0], c->p[1], skip, st);
+  }
+  if (prof) cudaEventRecord(c->ev_cur[2], st);
+  launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
+  c->launches += 4 + (int64_t)c->opt.outer_max *
+                         (3 + (early ? 1 : 0) + (halo ? 1 : 0) + (int64_t)c->opt.inner_sweeps * 2 * (halo ? 2 : 1));
+  c->cur = nw;
+}
+
+void enqueue_projection_mixed(pf_case* c) {
+  const int b = c->cur;
+  c->launches += 1;
+  launch_projection<float>(c->g, c->s, c->p[0], c->p[1], c->Uf[b], c->Vf[b], c->Wf[b], c->st);
+}
+
+void enqueue_boundary_mixed(pf_case* c) {
+  const int b = c->cur;
+  c->launches += c->g.dim == 3 ? 3 : 2;
+  launch_boundary<float>(c->g, c->s, c->Uf[b], c->Vf[b], c->Wf[b], c->p[0], c->p[1], c->st);
+}
+
+}  // namespace pf

@@ -1,0 +1,179 @@
+"""Synthetic porosity fields for the benchmark and test geometries.
+
+Porosity follows the reference's preprocessing tools: a tanh profile of the
+signed distance to the solid, ``0.5*tanh(sdf/thickness) + 0.5`` with sdf in
+cells and positive in the fluid (tools/cylinder/make_porosity_2d_cylinder.py:
+119-122, tools/channel/channel.py:27).  Here sdf is computed in physical units
+and divided by ``edge*dx``.  ``edge`` is the half-width of the transition in
+cells: the profile rises from 0.12 to 0.88 over |sdf| <= edge, so the
+benchmark's "tanh transition of width 2 cells" is edge = 1.  (With a wider
+tail the solid core of a small obstacle is not clamped to the threshold and
+the reference scheme itself diverges within ~100 steps of the 2D cylinder
+case; edge = 1 keeps the core at the threshold as the reference's own
+cylinder fixture does.)  Nodes sit at x_i = (i-1)*dx with
+dx = width/(m-1) (lib/grid.f90:50,82).  Several obstacles combine by the
+minimum of their signed distances.  The clamp ``max(value, threshold)`` is
+applied later at ingest, as grid.f90:43 does.
+
+All random draws use ``numpy.random.default_rng(seed)``.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from .config import Settings
+
+
+def tanh_porosity(sdf: np.ndarray, edge: float, dx: float) -> np.ndarray:
+    return 0.5 * np.tanh(sdf / (edge * dx)) + 0.5
+
+
+def node_coords(count: int, length: float) -> np.ndarray:
+    d = length / (count - 1)
+    return np.arange(count, dtype=np.float64) * d
+
+
+def cylinder_2d(m: int = 512, n: int = 256, width: float = 2.0, height: float = 1.0,
+                cx: float = 0.5, cy: float = 0.5, radius: float = 0.05,
+                edge: float = 1.0) -> np.ndarray:
+    """Circle of `radius` at (cx, cy): porosity values, shape (n, m)."""
+    x = node_coords(m, width)
+    y = node_coords(n, height)
+    dx = width / (m - 1)
+    sdf = np.sqrt((x[None, :] - cx) ** 2 + (y[:, None] - cy) ** 2) - radius
+    return tanh_porosity(sdf, edge, dx)
+
+
+def _ellipse_sdf(X: np.ndarray, Y: np.ndarray, cx: float, cy: float, a: float, b: float,
+                 angle: float) -> np.ndarray:
+    """First-order signed distance to a rotated ellipse, (q-1)/|grad q|."""
+    c, s = np.cos(angle), np.sin(angle)
+    xr = (X - cx) * c + (Y - cy) * s
+    yr = -(X - cx) * s + (Y - cy) * c
+    q = np.sqrt((xr / a) ** 2 + (yr / b) ** 2)
+    g = np.sqrt((xr / (a * a)) ** 2 + (yr / (b * b)) ** 2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        d = np.where(g > 0, (q - 1.0) * q / np.where(g > 0, g, 1.0), -min(a, b))
+    return d
+
+
+def obstacles_2d(m: int, n: int, width: float, height: float,
+                 shapes: Sequence[Tuple[float, float, float, float, float]],
+                 edge: float = 1.0) -> np.ndarray:
+    """Union of ellipses (cx, cy, a, b, angle); circles have a == b."""
+    x = node_coords(m, width)
+    y = node_coords(n, height)
+    X, Y = np.meshgrid(x, y)
+    sdf = np.full((n, m), np.inf)
+    for (cx, cy, a, b, ang) in shapes:
+        if a == b:
+            d = np.sqrt((X - cx) ** 2 + (Y - cy) ** 2) - a
+        else:
+            d = _ellipse_sdf(X, Y, cx, cy, a, b, ang)
+        sdf = np.minimum(sdf, d)
+    return tanh_porosity(sdf, edge, width / (m - 1))
+
+
+def random_spheres(count: int, seed: int = 0, cmin: float = 0.15, cmax: float = 0.85,
+                   rmin: float = 0.03, rmax: float = 0.08) -> np.ndarray:
+    """(count, 4) array of sphere centres and radii in the unit cube."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(cmin, cmax, size=(count, 3))
+    radii = rng.uniform(rmin, rmax, size=(count, 1))
+    return np.concatenate([centres, radii], axis=1)
+
+
+def spheres_3d(m: int = 256, n: int = 256, l: int = 256, width: float = 1.0, height: float = 1.0,
+               depth: float = 1.0, spheres: np.ndarray | None = None, count: int = 32,
+               seed: int = 0, edge: float = 1.0) -> np.ndarray:
+    """Union of spheres: porosity values, shape (l, n, m), built plane by plane."""
+    if spheres is None:
+        spheres = random_spheres(count, seed)
+    x = node_coords(m, width)
+    y = node_coords(n, height)
+    z = node_coords(l, depth)
+    dx = width / (m - 1)
+    out = np.empty((l, n, m), dtype=np.float64)
+    dxy = [(x[None, :] - s[0]) ** 2 + (y[:, None] - s[1]) ** 2 for s in spheres]
+    for k in range(l):
+        sdf = np.full((n, m), np.inf)
+        for s, d2 in zip(spheres, dxy):
+            sdf = np.minimum(sdf, np.sqrt(d2 + (z[k] - s[2]) ** 2) - s[3])
+        out[k] = tanh_porosity(sdf, edge, dx)
+    return out
+
+
+# --------------------------------------------------------------------------
+# Benchmark configurations.
+# --------------------------------------------------------------------------
+
+def settings_cylinder_2d(**kw) -> Settings:
+    """2D flow past a cylinder, 512x256, Re=100, dt=2e-4, 1000 steps."""
+    s = Settings(xnue=1e-3, xlambda=0.0, density=1.0, width=2.0, height=1.0, depth=0.0,
+                 time=0.2, inlet_velocity=1.0, outlet_pressure=0.0, aoa=0.0,
+                 istep_max=1000, istep_out=100000, thickness=2.0, threshold=1e-6,
+                 radius=0.05, center_x=0.25, center_y=0.5, nonslip=True,
+                 iter_max=100, relux_factor=1.7)
+    return s.replace(**kw)
+
+
+def settings_spheres_3d(**kw) -> Settings:
+    """3D unit cube with seeded spheres, nu=1e-3, dt=1e-4, 200 steps."""
+    s = Settings(xnue=1e-3, xlambda=0.0, density=1.0, width=1.0, height=1.0, depth=1.0,
+                 time=0.02, inlet_velocity=1.0, outlet_pressure=0.0, aoa=0.0,
+                 istep_max=200, istep_out=100000, thickness=2.0, threshold=1e-6,
+                 radius=0.05, nonslip=True, iter_max=100, relux_factor=1.7)
+    return s.replace(**kw)
+
+
+@dataclasses.dataclass
+class BatchCase2D:
+    m: int
+    n: int
+    settings: Settings
+    shapes: List[Tuple[float, float, float, float, float]]
+
+    def porosity(self) -> np.ndarray:
+        return obstacles_2d(self.m, self.n, self.settings.width, self.settings.height, self.shapes)
+
+
+def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
+                   sizes: Sequence[int] = tuple(range(64, 513, 32)),
+                   iter_max: int = 100) -> List[BatchCase2D]:
+    """Independent 2D cases of uneven size: nx, ny from `sizes`, 1-4 circles or
+    ellipses with semi-axes 0.02-0.1 of the height at random angles, Re uniform
+    in [50, 400] (nu = U*D/Re with D twice the first obstacle's larger
+    semi-axis), unit inflow, dt from CFL 0.2 (dt = 0.2*dx/U), square cells."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(count):
+        m = int(rng.choice(sizes))
+        n = int(rng.choice(sizes))
+        height = 1.0
+        h = height / (n - 1)
+        width = h * (m - 1)
+        nobs = int(rng.integers(1, 5))
+        shapes = []
+        for _o in range(nobs):
+            a = float(rng.uniform(0.02, 0.1)) * height
+            circle = bool(rng.integers(0, 2))
+            b = a if circle else float(rng.uniform(0.02, 0.1)) * height
+            ang = float(rng.uniform(0.0, np.pi))
+            cx = float(rng.uniform(0.2, 0.8)) * width
+            cy = float(rng.uniform(0.2, 0.8)) * height
+            shapes.append((cx, cy, a, b, ang))
+        re = float(rng.uniform(50.0, 400.0))
+        d_ref = 2.0 * max(shapes[0][2], shapes[0][3])
+        u_in = 1.0
+        nu = u_in * d_ref / re
+        dt = 0.2 * h / u_in
+        s = Settings(xnue=nu, xlambda=0.0, density=1.0, width=width, height=height, depth=0.0,
+                     time=dt * steps, inlet_velocity=u_in, outlet_pressure=0.0, aoa=0.0,
+                     istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6,
+                     radius=d_ref / 2, nonslip=True, iter_max=iter_max, relux_factor=1.7,
+                     precision="mixed")
+        cases.append(BatchCase2D(m, n, s, shapes))
+    return cases

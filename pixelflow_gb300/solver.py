@@ -1,0 +1,196 @@
+"""Host-side mirror of PixelFlow's step routines, running on the GB300 library.
+
+`Case` exposes the reference's own routine names with the same meaning:
+`initial_conditions` (+ `boundary`), `solve_p`, `projection`, `boundary` and
+the whole step loop body `step` (ibm_2d_uniform_omp_cpu.f90:80-125,
+ibm_3d_uniform_omp_cpu.f90:81-132).  Fields cross the boundary in the
+reference's Fortran layout: numpy arrays of shape (ld2, ld1) in 2D and
+(l+2, ld2, ld1) in 3D, C-ordered, so ``a[k, j, i]`` is Fortran ``a(i, j, k)``
+with the ghost layer at index 0 and m+1 (n+1, l+1).
+
+Every call goes to libpixelflow_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from .config import Settings, read_porosity_csv, read_settings
+from ._lib import PfOptions, PfParams, check
+
+PRECISIONS = {"fp64": _lib.PF_PREC_FP64, "plain": _lib.PF_PREC_FP64, "mixed": _lib.PF_PREC_MIXED}
+
+
+def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
+    dim = len(shape)
+    m, n = int(shape[0]), int(shape[1])
+    l = int(shape[2]) if dim == 3 else 1
+    return PfParams(dim, m, n, l, s.xnue, s.xlambda, s.density, s.width, s.height, s.depth, s.time,
+                    s.inlet_velocity, s.outlet_pressure, s.aoa, int(s.istep_max), int(s.iter_max),
+                    s.thickness, s.threshold, s.relux_factor, 1 if s.nonslip else 0, 0)
+
+
+def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
+    L = _lib.load()
+    o = PfOptions()
+    L.pf_default_options(ctypes.byref(o))
+    prec = str(s.precision).lower()
+    if prec not in PRECISIONS:
+        raise ValueError(f"unknown precision {s.precision!r}")
+    o.precision = PRECISIONS[prec]
+    o.outer_max = int(s.outer_max)
+    o.inner_sweeps = int(s.inner_sweeps)
+    o.dc_tol = float(s.dc_tol)
+    o.track_sor_error = 1 if s.track_sor_error else 0
+    o.use_graph = 1 if use_graph else 0
+    return o
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Case:
+    """One case resident on the GPU."""
+
+    def __init__(self, settings: Settings, shape: Sequence[int], porosity_values: np.ndarray,
+                 use_graph: bool = True):
+        self.L = _lib.load()
+        self.settings = settings
+        self.shape = tuple(int(x) for x in shape)
+        self.dim = len(self.shape)
+        if self.dim not in (2, 3):
+            raise ValueError("shape must be (m, n) or (m, n, l)")
+        self.m, self.n = self.shape[0], self.shape[1]
+        self.l = self.shape[2] if self.dim == 3 else 1
+        vals = np.ascontiguousarray(porosity_values, dtype=np.float64)
+        expect = (self.n, self.m) if self.dim == 2 else (self.l, self.n, self.m)
+        if vals.shape != expect:
+            raise ValueError(f"porosity values must have shape {expect}, got {vals.shape}")
+        self.params = make_params(settings, self.shape)
+        self.options = make_options(settings, use_graph)
+        h = ctypes.c_void_p()
+        check(self.L.pf_create(ctypes.byref(self.params), ctypes.byref(self.options), _ptr(vals), ctypes.byref(h)))
+        self.h = h
+        self.field_shape = (self.n + 2, self.m + 2) if self.dim == 2 else (self.l + 2, self.n + 2, self.m + 2)
+
+    @classmethod
+    def from_project(cls, project_dir: str, **kw) -> "Case":
+        """Open a reference project directory: config/controlDict.txt + its porosity CSV."""
+        s = read_settings(os.path.join(project_dir, "config", "controlDict.txt"))
+        shape, vals = read_porosity_csv(os.path.join(project_dir, s.csv_file))
+        return cls(s, shape, vals, **kw)
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            check(self.L.pf_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference routines ------------------------------------------------
+    def initial_conditions(self):
+        """initial_conditions + boundary, as the main programs call them."""
+        check(self.L.pf_initial_conditions(self.h))
+
+    def solve_p(self):
+        check(self.L.pf_solve_p(self.h))
+
+    def projection(self):
+        check(self.L.pf_projection(self.h))
+
+    def boundary(self):
+        check(self.L.pf_boundary(self.h))
+
+    def step(self, nsteps: int = 1):
+        check(self.L.pf_step(self.h, int(nsteps)))
+
+    def synchronize(self):
+        check(self.L.pf_synchronize(self.h))
+
+    def norms(self) -> Tuple[float, float]:
+        """(max|div u| of the porosity-weighted divergence, SOR error of the last solve_p)."""
+        md, se = ctypes.c_double(), ctypes.c_double()
+        rc = self.L.pf_norms(self.h, ctypes.byref(md), ctypes.byref(se))
+        if rc not in (_lib.PF_OK, -4):
+            check(rc)
+        return md.value, se.value
+
+    # -- fields ------------------------------------------------------------
+    def _check_field(self, a: np.ndarray) -> Tuple[int, int]:
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("fields must be C-contiguous float64 arrays")
+        if a.ndim != self.dim:
+            raise ValueError(f"fields must have {self.dim} axes")
+        if self.dim == 3 and a.shape[0] != self.l + 2:
+            raise ValueError("3D fields need l+2 planes")
+        return a.shape[-1], a.shape[-2]
+
+    def set_state(self, u: np.ndarray, v: np.ndarray, p: np.ndarray, w: Optional[np.ndarray] = None):
+        ld1, ld2 = self._check_field(u)
+        for a in (v, p) + ((w,) if self.dim == 3 else ()):
+            if self._check_field(a) != (ld1, ld2):
+                raise ValueError("all fields must share leading dimensions")
+        check(self.L.pf_set_state(self.h, _ptr(u), _ptr(v), _ptr(w), _ptr(p), ld1, ld2))
+
+    def get_state(self, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        if out is None:
+            out = {k: np.empty(self.field_shape) for k in (("u", "v", "p") + (("w",) if self.dim == 3 else ()))}
+        ld1, ld2 = self._check_field(out["u"])
+        check(self.L.pf_get_state(self.h, _ptr(out["u"]), _ptr(out["v"]), _ptr(out.get("w")), _ptr(out["p"]),
+                                  ld1, ld2))
+        return out
+
+    def porosity(self) -> np.ndarray:
+        a = np.empty(self.field_shape)
+        check(self.L.pf_get_porosity(self.h, _ptr(a), a.shape[-1], a.shape[-2]))
+        return a
+
+    def kernel_launches(self) -> int:
+        n = ctypes.c_int64()
+        check(self.L.pf_kernel_launches(self.h, ctypes.byref(n)))
+        return n.value
+
+    def profile_step_times(self, max_steps: int = 1 << 20) -> np.ndarray:
+        n = ctypes.c_int64()
+        buf = np.zeros(max_steps)
+        check(self.L.pf_profile_step_times(self.h, _ptr(buf), max_steps, ctypes.byref(n)))
+        return buf[: n.value].copy()
+
+    def memory_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        check(self.L.pf_memory_bytes(self.h, ctypes.byref(b)))
+        return b.value
+
+    # -- profiling -----------------------------------------------------------
+    def profile_begin(self):
+        check(self.L.pf_profile_begin(self.h))
+
+    def profile_end(self) -> Dict[str, float]:
+        sor, st = ctypes.c_double(), ctypes.c_double()
+        nl, ns = ctypes.c_int64(), ctypes.c_int64()
+        check(self.L.pf_profile_end(self.h, ctypes.byref(sor), ctypes.byref(nl), ctypes.byref(st), ctypes.byref(ns)))
+        return dict(sor_ms=sor.value, sor_launches=nl.value, step_ms=st.value, steps=ns.value)
+
+
+def host_register(a: np.ndarray):
+    check(_lib.load().pf_host_register(_ptr(a), a.nbytes))
+
+
+def host_unregister(a: np.ndarray):
+    check(_lib.load().pf_host_unregister(_ptr(a)))

@@ -1,0 +1,219 @@
+"""GPU parity: the CUDA step through the C ABI against the oracle (the C
+restatement of the reference's OpenMP step) and the golden vectors.
+
+Tolerances (relative L2 over the whole field incl. ghosts):
+  * a few steps / single stages: 1e-12 -- the GPU reorders the floating point
+    operations of each expression (reciprocal multiplies, FMAs), so it is not
+    bit-identical, but every stage agrees to a few ulp;
+  * long runs: 1e-10 after 1000 steps (the parity bar for the plain FP64 step).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from pixelflow_gb300 import geometry as G
+from pixelflow_gb300.solver import Case
+from oracle.oracle import OracleCase
+from tests.conftest import rel_l2
+from tests.golden.make_golden import CASES, case_inputs
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FIELDS2, FIELDS3 = ("u", "v", "p"), ("u", "v", "w", "p")
+
+
+def fields(dim):
+    return FIELDS2 if dim == 2 else FIELDS3
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_golden(name):
+    spec = CASES[name]
+    s, vals = case_inputs(spec)
+    ref = np.load(os.path.join(GOLDEN, name + ".npz"))
+    with Case(s, spec["shape"], vals) as c:
+        assert np.array_equal(c.porosity(), ref["poro"])
+        c.initial_conditions()
+        c.step(spec["steps"])
+        got = c.get_state()
+        max_div, sor_err = c.norms()
+    for f in fields(spec["dim"]):
+        assert rel_l2(got[f], ref[f]) < 1e-12, f
+    assert abs(sor_err - float(ref["sor_error"])) <= 1e-9 * abs(float(ref["sor_error"]))
+    assert abs(max_div - float(ref["max_div"])) <= 1e-9 * abs(float(ref["max_div"]))
+
+
+def _pair(s, shape, vals, **kw):
+    ref = OracleCase(s, shape, vals)
+    ref.initialize()
+    return ref, Case(s, shape, vals, **kw)
+
+
+@pytest.mark.parametrize("shape", [(40, 20), (41, 21), (33, 18)])
+def test_predictor_and_rhs_stage(shape):
+    """solve_p with iter_max=0 leaves p alone and returns u*, v* of the predictor."""
+    s = G.settings_cylinder_2d(iter_max=0)
+    vals = G.cylinder_2d(*shape, radius=0.2, cx=0.7, cy=0.45)
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        ref.step(2)
+        c.step(2)  # non-trivial state with pressure still 0
+        ref.copy_old()
+        ref.solve_p()
+        c.solve_p()
+        got = c.get_state()
+    for f in ("u", "v"):
+        assert rel_l2(got[f], getattr(ref, f)) < 1e-13, f
+
+
+@pytest.mark.parametrize("shape", [(24, 16), (25, 15), (16, 11, 9), (15, 12, 10)])
+def test_solve_p_projection_boundary_stages(shape):
+    dim = len(shape)
+    if dim == 2:
+        s = G.settings_cylinder_2d(iter_max=3)
+        vals = G.cylinder_2d(*shape, radius=0.2, cx=0.7, cy=0.45)
+    else:
+        s = G.settings_spheres_3d(iter_max=3)
+        vals = G.spheres_3d(*shape, spheres=np.array([[0.5, 0.45, 0.5, 0.25]]))
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        ref.step(2)
+        st = ref.state()
+        c.set_state(st["u"], st["v"], st["p"], st.get("w"))
+        ref.copy_old()
+        ref.solve_p()
+        c.solve_p()
+        got = c.get_state()
+        for f in fields(dim):
+            assert rel_l2(got[f], getattr(ref, f)) < 1e-12, ("solve_p", f)
+        ref.projection()
+        c.projection()
+        ref.boundary()
+        c.boundary()
+        got = c.get_state()
+        for f in fields(dim):
+            assert rel_l2(got[f], getattr(ref, f)) < 1e-12, ("projection+boundary", f)
+
+
+def test_state_roundtrip_fortran_leading_dims():
+    """pf_set_state / pf_get_state with the caller's static (0:md,0:nd) arrays."""
+    s = G.settings_spheres_3d(iter_max=2)
+    m, n, l = 13, 9, 6
+    vals = G.spheres_3d(m, n, l, count=2, seed=1)
+    with Case(s, (m, n, l), vals) as c:
+        md1, nd1 = m + 7, n + 4
+        rng = np.random.default_rng(0)
+        src = {f: rng.standard_normal((l + 2, nd1, md1)) for f in FIELDS3}
+        c.set_state(src["u"], src["v"], src["p"], src["w"])
+        out = {f: np.zeros((l + 2, nd1, md1)) for f in FIELDS3}
+        c.get_state(out)
+        for f in FIELDS3:
+            assert np.array_equal(out[f][:, : n + 2, : m + 2], src[f][:, : n + 2, : m + 2]), f
+            assert not out[f][:, n + 2:, :].any() and not out[f][:, :, m + 2:].any()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_graph_replay_matches_eager_launches(dim):
+    if dim == 2:
+        s, shape = G.settings_cylinder_2d(iter_max=15), (48, 30)
+        vals = G.cylinder_2d(*shape, radius=0.2, cx=0.6, cy=0.5)
+    else:
+        s, shape = G.settings_spheres_3d(iter_max=8), (20, 16, 14)
+        vals = G.spheres_3d(*shape, count=3, seed=2)
+    outs = []
+    for graph in (True, False):
+        with Case(s, shape, vals, use_graph=graph) as c:
+            c.initial_conditions()
+            c.step(7)
+            outs.append((c.get_state(), c.norms()))
+    for f in fields(dim):
+        assert np.array_equal(outs[0][0][f], outs[1][0][f]), f
+    assert outs[0][1] == outs[1][1]
+
+
+@pytest.mark.parametrize("shape,steps", [((64, 32), 40), ((63, 33), 30), ((30, 24, 20), 12),
+                                         ((29, 23, 21), 10), ((24, 25, 18), 10)])
+def test_multi_step_parity(shape, steps):
+    dim = len(shape)
+    if dim == 2:
+        s = G.settings_cylinder_2d(iter_max=30)
+        vals = G.cylinder_2d(*shape, radius=0.15, cx=0.6, cy=0.5)
+    else:
+        s = G.settings_spheres_3d(iter_max=20)
+        vals = G.spheres_3d(*shape, count=4, seed=5)
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        c.step(steps)
+        got = c.get_state()
+        max_div, sor_err = c.norms()
+    e_ref = ref.step(steps)
+    for f in fields(dim):
+        assert rel_l2(got[f], getattr(ref, f)) < 1e-11, f
+    assert abs(sor_err - e_ref) <= 1e-8 * abs(e_ref)
+    assert abs(max_div - ref.divergence_diag()) <= 1e-8 * ref.divergence_diag()
+
+
+def test_uniform_flow_stays_exact():
+    s = G.settings_spheres_3d(iter_max=10)
+    with Case(s, (16, 12, 10), np.ones((10, 12, 16))) as c:
+        c.initial_conditions()
+        c.step(5)
+        st = c.get_state()
+    assert np.all(st["u"] == 1.0) and not st["v"].any() and not st["w"].any() and not st["p"].any()
+
+
+def test_nonfinite_fields_are_reported():
+    """A run that diverges (wide porosity tail, see geometry.py) is reported by
+    pf_norms as PF_E_NONFINITE instead of returning garbage silently."""
+    s = G.settings_cylinder_2d(iter_max=100)
+    vals = G.cylinder_2d(512, 256, edge=2.0)
+    with Case(s, (512, 256), vals) as c:
+        c.initial_conditions()
+        c.step(120)
+        md = ctypes.c_double()
+        se = ctypes.c_double()
+        rc = c.L.pf_norms(c.h, ctypes.byref(md), ctypes.byref(se))
+    assert rc == -4 and not np.isfinite(md.value)
+
+
+@pytest.mark.slow
+def test_cylinder_512x256_1000_steps_parity():
+    """The 2D benchmark case for its full 1000 steps against the oracle:
+    u, v, p within 1e-10 relative L2."""
+    s = G.settings_cylinder_2d()
+    vals = G.cylinder_2d()
+    ref, c = _pair(s, (512, 256), vals)
+    with c:
+        c.initial_conditions()
+        c.step(1000)
+        got = c.get_state()
+        max_div, _ = c.norms()
+    ref.step(1000)
+    errs = {f: rel_l2(got[f], getattr(ref, f)) for f in FIELDS2}
+    print("1000-step relative L2 vs oracle:", errs, "max|div|", max_div, ref.divergence_diag())
+    for f in FIELDS2:
+        assert errs[f] < 1e-10, (f, errs)
+
+
+@pytest.mark.slow
+def test_spheres_3d_reduced_parity():
+    """The 3D benchmark geometry (32 seeded spheres) on a 64x64x64 grid for
+    60 steps with iter_max=100."""
+    s = G.settings_spheres_3d()
+    shape = (64, 64, 64)
+    vals = G.spheres_3d(*shape)
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        c.step(60)
+        got = c.get_state()
+    ref.step(60)
+    errs = {f: rel_l2(got[f], getattr(ref, f)) for f in FIELDS3}
+    print("3D 64^3 60-step relative L2 vs oracle:", errs)
+    for f in FIELDS3:
+        assert errs[f] < 1e-10, (f, errs)

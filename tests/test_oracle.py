@@ -1,0 +1,175 @@
+"""The oracle (C restatement of the reference step) against an independent
+numpy restatement, the reference's colour mapping, physical invariants and
+the committed golden vectors.  CPU only."""
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+from pixelflow_gb300 import geometry as G
+from oracle.np_oracle import NpCase
+from oracle.oracle import OracleCase
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _case2d(shape, iters=7, dtype=np.float64):
+    m, n = shape
+    s = G.settings_cylinder_2d(iter_max=iters)
+    return s, G.cylinder_2d(m, n, radius=0.2, cx=0.6, cy=0.45)
+
+
+def _case3d(shape, iters=5):
+    m, n, l = shape
+    s = G.settings_spheres_3d(iter_max=iters)
+    sph = np.array([[0.4, 0.5, 0.5, 0.2], [0.7, 0.3, 0.6, 0.15]])
+    return s, G.spheres_3d(m, n, l, spheres=sph)
+
+
+@pytest.mark.parametrize("shape", [(8, 6), (9, 6), (8, 7), (9, 7), (16, 12)])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_c_oracle_matches_numpy_restatement_2d(shape, dtype):
+    s, vals = _case2d(shape)
+    a, b = OracleCase(s, shape, vals, dtype), NpCase(s, shape, vals, dtype)
+    a.initialize()
+    b.initialize()
+    assert np.array_equal(a.poro, b.poro)
+    for _ in range(3):
+        assert a.step(1) == b.step(1)
+        for f in ("u", "v", "p"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    assert a.divergence_diag() == b.divergence_diag()[0]
+
+
+@pytest.mark.parametrize("shape", [(6, 6, 6), (7, 6, 6), (6, 7, 6), (7, 7, 5), (6, 5, 7), (8, 6, 4)])
+def test_c_oracle_matches_numpy_restatement_3d(shape):
+    s, vals = _case3d(shape)
+    a, b = OracleCase(s, shape, vals), NpCase(s, shape, vals)
+    a.initialize()
+    b.initialize()
+    for _ in range(2):
+        assert a.step(1) == b.step(1)
+        for f in ("u", "v", "w", "p"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+
+
+def _ref_colours_2d(m, n):
+    """The reference's linear-index mapping (ibm_2d_uniform_omp_cpu.f90:339-344, 373-378)."""
+    first, second = [], []
+    for k in range(2, m * n + 1, 2):
+        j = (k - 1) // m + 1
+        i = k - (j - 1) * m
+        if m % 2 == 0 and j % 2 == 0:
+            i -= 1
+        first.append((i, j))
+    for k in range(1, m * n + 1, 2):
+        j = (k - 1) // m + 1
+        i = k - (j - 1) * m
+        if m % 2 == 0 and j % 2 == 0:
+            i += 1
+        second.append((i, j))
+    return first, second
+
+
+def _ref_colours_3d(m, n, l):
+    """ibm_3d_uniform_omp_cpu.f90:493-508, 550-565."""
+    out = []
+    for start, sign in ((2, -1), (1, +1)):
+        cells = []
+        for ii in range(start, m * n * l + 1, 2):
+            k = (ii - 1) // (m * n) + 1
+            j = ((ii - 1) // m + 1) - (k - 1) * n
+            i = (ii - (j - 1) * m) - (k - 1) * m * n
+            if m % 2 != 0 and n % 2 == 0 and k % 2 == 0:
+                j = j + sign if i % 2 != 0 else j - sign
+            elif m % 2 == 0 and (j % 2 + k % 2 == 1):
+                i = i + sign
+            cells.append((i, j, k))
+        out.append(cells)
+    return out
+
+
+@pytest.mark.parametrize("m,n", list(itertools.product(range(2, 9), range(2, 9))))
+def test_colour_order_2d(m, n):
+    first, second = _ref_colours_2d(m, n)
+    allc = {(i, j) for i in range(1, m + 1) for j in range(1, n + 1)}
+    assert len(set(first)) == len(first) and len(set(second)) == len(second)
+    assert set(first) | set(second) == allc and not set(first) & set(second)
+    assert set(first) == {(i, j) for (i, j) in allc if (i + j) % 2 == 1}
+    # the GPU colour function: colour 0 sweeps first, colour = (i + j + 1) & 1
+    assert all(((i + j + 1) & 1) == 0 for (i, j) in first)
+
+
+@pytest.mark.parametrize("m,n,l", list(itertools.product(range(2, 7), range(2, 7), range(2, 6))))
+def test_colour_order_3d(m, n, l):
+    first, second = _ref_colours_3d(m, n, l)
+    allc = {(i, j, k) for i in range(1, m + 1) for j in range(1, n + 1) for k in range(1, l + 1)}
+    assert set(first) | set(second) == allc and not set(first) & set(second)
+    assert len(first) == len(set(first))
+    assert all(((i + j + k) & 1) == 0 for (i, j, k) in first)
+
+
+def test_uniform_flow_is_steady():
+    """Porosity 1 everywhere, AoA 0: u = U, v = 0, p = p_out stay exact."""
+    s = G.settings_cylinder_2d(iter_max=10)
+    shape = (16, 10)
+    c = OracleCase(s, shape, np.ones((10, 16)))
+    c.initialize()
+    c.step(5)
+    assert np.all(c.u == 1.0) and np.all(c.v == 0.0) and np.all(c.p == 0.0)
+    s3 = G.settings_spheres_3d(iter_max=4)
+    c3 = OracleCase(s3, (8, 6, 6), np.ones((6, 6, 8)))
+    c3.initialize()
+    c3.step(3)
+    assert np.all(c3.u == 1.0) and np.all(c3.v == 0.0) and np.all(c3.w == 0.0) and np.all(c3.p == 0.0)
+
+
+def test_periodic_shift_and_lagged_ghost_quirk():
+    """Without pressure (iter_max=0) a shift of the geometry by an even number
+    of rows shifts the solution bit for bit.  With the SOR running it does
+    not: bb at the rows next to the periodic boundary reads the ghost
+    velocities left by the previous step's boundary call instead of the new
+    predictor values (ibm_2d_uniform_omp_cpu.f90:271-274), so the first
+    difference appears in bb on the periodic rows of the second step."""
+    m, n, shift = 20, 12, 4
+    vals = G.cylinder_2d(m, n, radius=0.25, cx=0.8, cy=0.4)
+    R = lambda x: np.roll(x[1:-1], shift, axis=0)
+    s0 = G.settings_cylinder_2d(iter_max=0)
+    a, b = OracleCase(s0, (m, n), vals), OracleCase(s0, (m, n), np.roll(vals, shift, axis=0))
+    a.initialize(); b.initialize()
+    a.step(3); b.step(3)
+    for f in ("u", "v", "p"):
+        assert np.array_equal(R(getattr(a, f)), getattr(b, f)[1:-1]), f
+    s1 = G.settings_cylinder_2d(iter_max=1)
+    a, b = OracleCase(s1, (m, n), vals), OracleCase(s1, (m, n), np.roll(vals, shift, axis=0))
+    a.initialize(); b.initialize()
+    a.step(1); b.step(1)
+    assert np.array_equal(R(a.p), b.p[1:-1])
+    for c in (a, b):
+        c.copy_old(); c.divergence(); c.predictor(); c.coefficients()
+    assert np.array_equal(R(a.u), b.u[1:-1])
+    d = np.abs(R(a.work("bb")) - b.work("bb")[1:-1])
+    rows = set(np.nonzero(d)[0].tolist())
+    # b's periodic rows (0, n-1) and a's, which the shift moves to (shift, shift-1)
+    assert rows and rows <= {0, n - 1, shift - 1, shift}
+
+
+def test_sor_error_semantics():
+    """2D error is the running max over both half-sweeps, 3D over the
+    second half-sweep only; both are non-negative and finite."""
+    s, vals = _case2d((10, 8), iters=3)
+    a = OracleCase(s, (10, 8), vals)
+    a.initialize()
+    e = a.step(1)
+    assert np.isfinite(e) and e > 0
+
+
+@pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
+def test_oracle_reproduces_golden(name):
+    from tests.golden.make_golden import CASES, run_oracle
+    spec = CASES[name[:-4]]
+    out = run_oracle(spec)
+    ref = np.load(os.path.join(GOLDEN, name))
+    for k in ref.files:
+        assert np.array_equal(out[k], ref[k]), k
