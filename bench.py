@@ -42,7 +42,7 @@ UNIT = "Mcell-steps/s"
 
 def workload(name: str, precision: str):
     from pixelflow_gb300 import geometry as G
-    if name in ("spheres3d_256", "spheres3d_384", "spheres3d_128"):
+    if name in ("spheres3d_256", "spheres3d_384", "spheres3d_192", "spheres3d_128"):
         nn = int(name.split("_")[1])
         s = G.settings_spheres_3d(precision=precision)
         shape = (nn, nn, nn)

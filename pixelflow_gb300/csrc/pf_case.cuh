@@ -40,9 +40,11 @@ struct pf_case {
   size_t mixed_bytes = 0;
   float *Uf[2] = {nullptr, nullptr}, *Vf[2] = {nullptr, nullptr}, *Wf[2] = {nullptr, nullptr};
   float* divf = nullptr;
-  float* e[2] = {nullptr, nullptr};  // packed FP32 correction
-  pf::Coef<float> Cf[2]{};           // FP32 operator; bbn holds the normalised residual
-  int* skip = nullptr;               // device flag: defect correction converged
+  float *gxf = nullptr, *gyf = nullptr, *gzf = nullptr, *rinvf = nullptr, *dampf = nullptr;
+  float* e[2] = {nullptr, nullptr};     // packed FP32 correction
+  float* rf[2] = {nullptr, nullptr};    // packed FP32 normalised residual (RHS of the sweeps)
+  float* epsf[2] = {nullptr, nullptr};  // packed FP32 porosity (operator rebuilt on the fly)
+  int* skip = nullptr;                  // device flag: defect correction converged
 
   int64_t sor_launches_per_step() const {
     if (opt.precision == PF_PREC_MIXED) return 2LL * opt.outer_max * opt.inner_sweeps;

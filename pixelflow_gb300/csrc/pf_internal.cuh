@@ -79,8 +79,8 @@ void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, 
                        cudaStream_t st);
 template <typename TV>
 void launch_predictor(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, const TV* div,
-                      const double* gx, const double* gy, const double* gz, const double* rinv,
-                      const double* damp, TV* u, TV* v, TV* w, cudaStream_t st);
+                      const TV* gx, const TV* gy, const TV* gz, const TV* rinv, const TV* damp, TV* u, TV* v,
+                      TV* w, cudaStream_t st);
 template <typename TV>
 void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
                 const double* gx, const double* gy, const double* gz, Coef<double> c0, Coef<double> c1,
@@ -110,6 +110,9 @@ void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, cons
 void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, const float* e1, const int* skip,
                        cudaStream_t st);
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
+void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
+                   const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);
+void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st);
 void launch_coef_to_float(const Geo& g, const Coef<double>& c, Coef<float> cf, cudaStream_t st);
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);

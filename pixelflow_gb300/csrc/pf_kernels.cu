@@ -164,12 +164,10 @@ __global__ void k_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* _
 template <typename T, int DIM>
 __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __restrict__ uo,
                                                       const T* __restrict__ vo, const T* __restrict__ wo,
-                                                      const T* __restrict__ div, const double* __restrict__ gxa,
-                                                      const double* __restrict__ gya,
-                                                      const double* __restrict__ gza,
-                                                      const double* __restrict__ rinva,
-                                                      const double* __restrict__ dampa, T* __restrict__ u,
-                                                      T* __restrict__ v, T* __restrict__ w) {
+                                                      const T* __restrict__ div, const T* __restrict__ gxa,
+                                                      const T* __restrict__ gya, const T* __restrict__ gza,
+                                                      const T* __restrict__ rinva, const T* __restrict__ dampa,
+                                                      T* __restrict__ u, T* __restrict__ v, T* __restrict__ w) {
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
@@ -185,7 +183,7 @@ __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __
   const long long jn = (j == g.n) ? q - (long long)(g.n - 1) * X : q + X;
   const long long js = (j == 1) ? q + (long long)(g.n - 1) * X : q - X;
   const T dc = div[q], dE = div[q + 1], dW = div[q - 1], dN = div[jn], dS = div[js];
-  const T gx = (T)gxa[q], gy = (T)gya[q], rv = (T)rinva[q], dp = (T)dampa[q];
+  const T gx = gxa[q], gy = gya[q], rv = rinva[q], dp = dampa[q];
 
   const T uc = uo[q], ue = uo[q + 1], uw = uo[q - 1], un = uo[q + X], us = uo[q - X];
   const T vc = vo[q], ve = vo[q + 1], vw = vo[q - 1], vn = vo[q + X], vs = vo[q - X];
@@ -219,7 +217,7 @@ __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __
     const long long kt = (k == g.l) ? q - (long long)(g.l - 1) * XY : q + XY;
     const long long kb = (k == 1) ? q + (long long)(g.l - 1) * XY : q - XY;
     const T dT = div[kt], dB = div[kb];
-    const T gz = (T)gza[q];
+    const T gz = gza[q];
     const T ut = uo[q + XY], ub = uo[q - XY], vt = vo[q + XY], vb = vo[q - XY];
     const T wc = wo[q], we = wo[q + 1], ww = wo[q - 1], wn = wo[q + X], ws = wo[q - X];
     const T wt = wo[q + XY], wb = wo[q - XY];
@@ -593,6 +591,83 @@ __global__ void __launch_bounds__(BX* BY) k_residual(Geo g, Coef<double> C, cons
   block_max_atomic(e, rmax);
 }
 
+// FP32 correction sweep with the operator rebuilt on the fly from the FP32
+// porosity (packed by colour, ghosts included), so a half-sweep streams only
+// porosity, r and e (24 bytes per update) instead of six stored
+// coefficients.  Same operator as k_setup_coef up to FP32 rounding:
+//   a_f = dt/h^2 * max(small, (eps_a+eps_b)/2), ap = -sum a_f (before the
+//   inlet/outlet edits), inlet: a_e += a_w, a_w = 0; outlet: all a_f = 0,
+//   e = (1-w) e + r - (w/ap) sum a_f e_f.
+struct DCConst {
+  float kx, ky, kz;  // dt/dx^2 etc.
+  float small, omega, omw;
+};
+
+template <int DIM, bool TRACK>
+__global__ void __launch_bounds__(BX* BY) k_sor_dc(Geo g, DCConst K, const float* __restrict__ epsc,
+                                                   const float* __restrict__ epso, const float* __restrict__ r,
+                                                   float* __restrict__ ec, const float* __restrict__ eo, int colour,
+                                                   unsigned long long* __restrict__ err, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int h = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y + 1;
+  const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const int i = 2 * h + s;
+  unsigned long long e = 0;
+  if (j <= g.n && i >= 1 && i <= g.m) {
+    const long long H = g.H, HY = (long long)g.H * g.Y;
+    const long long q = pk_idx(g, h, j, k);
+    const long long qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
+    const long long qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
+    const float pc = epsc[q];
+    float ae = K.kx * fmaxf(K.small, (epso[q + s] + pc) * 0.5f);
+    float aw = K.kx * fmaxf(K.small, (pc + epso[q - 1 + s]) * 0.5f);
+    const float an = K.ky * fmaxf(K.small, (epso[q + H] + pc) * 0.5f);
+    const float as = K.ky * fmaxf(K.small, (pc + epso[q - H]) * 0.5f);
+    float at = 0.f, ab = 0.f;
+    if (DIM == 3) {
+      at = K.kz * fmaxf(K.small, (epso[q + HY] + pc) * 0.5f);
+      ab = K.kz * fmaxf(K.small, (pc + epso[q - HY]) * 0.5f);
+    }
+    const float ap = -ae - aw - an - as - at - ab;
+    const float wap = K.omega / ap;
+    const float eold = ec[q];
+    float enew = fmaf(K.omw, eold, r[q]);
+    if (i != g.m) {
+      if (i == 1) {
+        ae += aw;
+        aw = 0.f;
+      }
+      float t = ae * eo[q + s];
+      t = fmaf(aw, eo[q - 1 + s], t);
+      t = fmaf(an, eo[qn], t);
+      t = fmaf(as, eo[qs], t);
+      if (DIM == 3) {
+        const long long qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
+        const long long qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
+        t = fmaf(at, eo[qt], t);
+        t = fmaf(ab, eo[qb], t);
+      }
+      enew = fmaf(-wap, t, enew);
+    }
+    ec[q] = enew;
+    if (TRACK) e = abs_bits(enew - eold);
+  }
+  if (TRACK) block_max_atomic(e, err);
+}
+
+// FP32 porosity packed by colour (all positions, ghosts included).
+__global__ void k_pack_eps(Geo g, const double* __restrict__ po, float* e0, float* e1) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.m + 1 || j > g.n + 1) return;
+  int c;
+  const long long r = pk_of(g, i, j, k, c);
+  (c ? e1 : e0)[r] = (float)po[nat_idx(g, i, j, k)];
+}
+
 // p += e over the interior cells of both colours (FP64 accumulation).
 template <int DIM>
 __global__ void k_accumulate(Geo g, double* __restrict__ p0, double* __restrict__ p1, const float* __restrict__ e0,
@@ -654,8 +729,8 @@ void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, 
 
 template <typename TV>
 void launch_predictor(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, const TV* div,
-                      const double* gx, const double* gy, const double* gz, const double* rinv,
-                      const double* damp, TV* u, TV* v, TV* w, cudaStream_t st) {
+                      const TV* gx, const TV* gy, const TV* gz, const TV* rinv, const TV* damp, TV* u, TV* v,
+                      TV* w, cudaStream_t st) {
   if (g.dim == 3)
     k_predictor<TV, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
                                                                   damp, u, v, w);
@@ -741,6 +816,33 @@ void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, cons
     k_residual<2><<<grid_packed(g), dim3(BX, BY), 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
 }
 
+void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
+                   const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st) {
+  DCConst K;
+  K.kx = (float)(sc.dt / sc.dx / sc.dx);
+  K.ky = (float)(sc.dt / sc.dy / sc.dy);
+  K.kz = g.dim == 3 ? (float)(sc.dt / sc.dz / sc.dz) : 0.f;
+  K.small = 1.e-6f;
+  K.omega = (float)sc.omega;
+  K.omw = (float)(1.0 - sc.omega);
+  const dim3 grid = grid_packed(g);
+  if (g.dim == 3) {
+    if (err)
+      k_sor_dc<3, true><<<grid, dim3(BX, BY), 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, err, skip);
+    else
+      k_sor_dc<3, false><<<grid, dim3(BX, BY), 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, err, skip);
+  } else {
+    if (err)
+      k_sor_dc<2, true><<<grid, dim3(BX, BY), 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, err, skip);
+    else
+      k_sor_dc<2, false><<<grid, dim3(BX, BY), 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, err, skip);
+  }
+}
+
+void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st) {
+  k_pack_eps<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, poro, e0, e1);
+}
+
 void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, const float* e1, const int* skip,
                        cudaStream_t st) {
   dim3 grid = grid_packed(g);
@@ -782,8 +884,8 @@ void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* 
   template void launch_divergence<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, TV*,         \
                                       cudaStream_t);                                                         \
   template void launch_predictor<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, const TV*,    \
-                                     const double*, const double*, const double*, const double*,            \
-                                     const double*, TV*, TV*, TV*, cudaStream_t);                           \
+                                     const TV*, const TV*, const TV*, const TV*, const TV*, TV*, TV*, TV*,  \
+                                     cudaStream_t);                                                         \
   template void launch_rhs<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, const double*,      \
                                const double*, const double*, const double*, Coef<double>, Coef<double>,     \
                                cudaStream_t);                                                                \

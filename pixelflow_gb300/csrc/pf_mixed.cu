@@ -7,6 +7,8 @@
 // boundary), the operator copy used by the sweeps, and the correction e.
 // Per step: outer_max passes of { r = bbn - w p - sum a p_nb (FP64);
 // inner_sweeps FP32 SOR iterations on e from e = 0; p += e (FP64) }.
+// The FP32 sweeps rebuild their operator on the fly from FP32 porosity
+// (k_sor_dc), so they stream 24 bytes per cell update.
 // With outer_max * inner_sweeps == iter_max the pass structure reproduces
 // the plain SOR's iterates up to the FP32 rounding of e; dc_tol > 0 ends
 // the passes of a step early once max|r|/omega <= dc_tol (a device flag, so
@@ -34,13 +36,15 @@ int mixed_alloc(pf_case* c) {
     req[nr++] = {&c->Wf[b], three ? nat : 0};
   }
   req[nr++] = {&c->divf, nat};
-  req[nr++] = {&c->e[0], pk};
-  req[nr++] = {&c->e[1], pk};
+  req[nr++] = {&c->gxf, nat};
+  req[nr++] = {&c->gyf, nat};
+  req[nr++] = {&c->gzf, three ? nat : 0};
+  req[nr++] = {&c->rinvf, nat};
+  req[nr++] = {&c->dampf, nat};
   for (int col = 0; col < 2; col++) {
-    for (int d = 0; d < 6; d++) req[nr++] = {&c->Cf[col].a[d], d < 2 * g.dim ? pk : 0};
-    req[nr++] = {&c->Cf[col].bbn, pk};
-    c->Cf[col].wap = nullptr;
-    c->Cf[col].oadd = nullptr;
+    req[nr++] = {&c->e[col], pk};
+    req[nr++] = {&c->rf[col], pk};
+    req[nr++] = {&c->epsf[col], pk};
   }
   size_t total = 256;  // flag
   for (int r = 0; r < nr; r++) total += (req[r].bytes + 255) / 256 * 256;
@@ -65,7 +69,13 @@ void mixed_free(pf_case* c) {
 }
 
 void mixed_setup(pf_case* c) {
-  for (int col = 0; col < 2; col++) launch_coef_to_float(c->g, c->C[col], c->Cf[col], c->st);
+  const long long n = c->g.nat;
+  launch_to_float(c->gx, c->gxf, n, c->st);
+  launch_to_float(c->gy, c->gyf, n, c->st);
+  if (c->g.dim == 3) launch_to_float(c->gz, c->gzf, n, c->st);
+  launch_to_float(c->rinv, c->rinvf, n, c->st);
+  launch_to_float(c->damp, c->dampf, n, c->st);
+  launch_pack_eps(c->g, c->poro, c->epsf[0], c->epsf[1], c->st);
 }
 
 void mixed_sync_from_fp64(pf_case* c) {
@@ -97,23 +107,23 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   if (track) cudaMemsetAsync(&c->red[0], 0, sizeof(unsigned long long), st);
   if (early) cudaMemsetAsync(c->skip, 0, sizeof(int), st);
   launch_divergence<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, st);
-  launch_predictor<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, c->gx, c->gy, c->gz, c->rinv, c->damp,
-                          c->Uf[nw], c->Vf[nw], c->Wf[nw], st);
+  launch_predictor<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, c->gxf, c->gyf, c->gzf, c->rinvf,
+                          c->dampf, c->Uf[nw], c->Vf[nw], c->Wf[nw], st);
   launch_rhs<float>(g, s, c->Uf[nw], c->Vf[nw], c->Wf[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
-  const float omw = (float)(1.0 - s.omega);
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
     cudaMemsetAsync(&c->red[2], 0, sizeof(unsigned long long), st);
     for (int col = 0; col < 2; col++)
-      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->Cf[col].bbn, c->e[col], &c->red[2],
+      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col], &c->red[2],
                       skip, st);
     if (early) launch_dc_check(&c->red[2], c->opt.dc_tol * s.omega, c->skip, st);
     for (int it = 0; it < c->opt.inner_sweeps; it++) {
       for (int col = 0; col < 2; col++) {
         if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
         unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[0] : nullptr;
-        launch_sor_half<float>(g, c->Cf[col], c->e[col], c->e[1 - col], omw, col, err, skip, st);
+        launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err, skip,
+                      st);
       }
     }
     launch_accumulate(g, c->p[0], c->p[1], c->e[0], c->e[1], skip, st);

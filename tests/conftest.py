@@ -18,6 +18,15 @@ def rel_l2(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300))
 
 
+def rel_vel(got, ref, dim):
+    """Relative L2 error of the velocity vector field (u, v[, w]) together."""
+    import numpy as np
+    keys = ("u", "v", "w")[:dim]
+    num = sum(float(np.sum((np.asarray(got[k]) - np.asarray(ref[k])) ** 2)) for k in keys)
+    den = sum(float(np.sum(np.asarray(ref[k]) ** 2)) for k in keys)
+    return (num / max(den, 1e-300)) ** 0.5
+
+
 @pytest.fixture
 def rel():
     return rel_l2
