@@ -146,6 +146,26 @@ int pf_kernel_launches(pf_case *c, int64_t *count);
 /* Device memory held by the case, in bytes. */
 int pf_memory_bytes(pf_case *c, size_t *bytes);
 
+/* max|div u| without allocating device memory.  No counterpart in the
+ * reference: it exists for callers that must not call cudaMalloc at this
+ * point -- cudaMalloc/cudaFree synchronise the whole device, which stalls a
+ * loop that keeps other work running on other streams, and some programs run
+ * under a memory budget owned by another allocator.  u, v, w (NULL in 2D)
+ * and porosity are the caller's DEVICE arrays in the Fortran layout of
+ * pf_get_state / pf_get_porosity (leading dimensions ld1 >= m+2,
+ * ld2 >= n+2); *max_div is a DEVICE double written on `stream` (a
+ * cudaStream_t, NULL for the legacy default stream).  Same value as
+ * pf_norms' max_div.  The reduction uses a fixed scratch array compiled into
+ * the library (PF_NOALLOC_MAX_ROWS partials, 2 MiB, held by every GPU that
+ * loads the library until exit); cases with n*l > PF_NOALLOC_MAX_ROWS are
+ * rejected with PF_E_INVALID.  All calls share that array, so calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress); make
+ * it before any stream capture begins. */
+#define PF_NOALLOC_MAX_ROWS 262144
+int pf_max_div_noalloc(const pf_params *prm, const double *u, const double *v, const double *w,
+                       const double *porosity, int ld1, int ld2, double *max_div, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

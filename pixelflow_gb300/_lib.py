@@ -78,6 +78,7 @@ _PROTOS = {
     "pf_profile_step_times": (_I, [_VP, _VP, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
+    "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
 }
 
 
