@@ -42,7 +42,7 @@ UNIT = "Mcell-steps/s"
 
 def workload(name: str, precision: str):
     from pixelflow_gb300 import geometry as G
-    if name in ("spheres3d_256", "spheres3d_384", "spheres3d_192", "spheres3d_128"):
+    if name in ("spheres3d_256", "spheres3d_384", "spheres3d_192", "spheres3d_128", "spheres3d_64"):
         nn = int(name.split("_")[1])
         s = G.settings_spheres_3d(precision=precision)
         shape = (nn, nn, nn)
@@ -186,6 +186,97 @@ def cpu_baseline(settings, shape, vals, budget_s: float = 20.0, max_steps: int =
                       f"({sum(times):.1f} s, oracle = C restatement of the reference OpenMP step, FP64)"}
 
 
+def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
+                baseline_sample: int = 6, baseline_steps: int = 3):
+    """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
+    {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400, dt from CFL 0.2),
+    precision form (FP32 sweeps in FP64 defect correction, 4 x 25), advanced by
+    the persistent batch kernel.  Reports device-timed aggregate Mcell-steps/s
+    and, as the comparison, the plain FP64 single-case step run sequentially
+    on a sample of the same cases."""
+    from pixelflow_gb300 import geometry as G
+    from pixelflow_gb300.autotune import tune_batch
+    from pixelflow_gb300.batch import Batch
+    from pixelflow_gb300.solver import Case
+    cases = G.batch_cases_2d(ncases, seed=seed)
+    t0 = time.perf_counter()
+    b = Batch(max_cases=ncases)
+    slots = [b.add(c.settings, (c.m, c.n), c.porosity()) for c in cases]
+    setup_s = time.perf_counter() - t0
+    cells = sum(c.m * c.n for c in cases)
+    best, trials = tune_batch(b, slots, steps=warmup_steps, use_cache=False)
+    l0 = b.kernel_launches()
+    b.step_slots(slots, [steps] * len(slots))
+    ms = b.last_ms()
+    launches = b.kernel_launches() - l0
+    value = cells * steps / (ms / 1e3) / 1e6
+    mem = b.memory()[0]
+    b.close()
+    # plain FP64 single-case step, one case after another, on a sample
+    rng = np.random.default_rng(seed + 1)
+    sample = rng.choice(len(cases), size=min(baseline_sample, len(cases)), replace=False)
+    tot_cells, tot_ms = 0, 0.0
+    for k in sample:
+        c = cases[int(k)]
+        with Case(c.settings.replace(precision="fp64"), (c.m, c.n), c.porosity()) as sc:
+            sc.initial_conditions()
+            sc.step(1)
+            sc.synchronize()
+            sc.profile_begin()
+            sc.step(baseline_steps)
+            prof = sc.profile_end()
+        tot_cells += c.m * c.n * baseline_steps
+        tot_ms += prof["step_ms"]
+    plain = tot_cells / (tot_ms / 1e3) / 1e6
+    return {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25",
+            "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
+            "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
+            "autotune": {"best": list(best), "trials": trials},
+            "plain_fp64_sequential": {"value": plain, "unit": UNIT, "sample_cases": len(sample),
+                                      "steps_each": baseline_steps},
+            "speedup_vs_plain_fp64_sequential": value / plain}
+
+
+def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
+                  baseline_sample: int = 4, baseline_steps: int = 3):
+    """The serving form: `count` requests with Poisson arrivals (mean `rate`
+    per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
+    100-1000 steps each, admitted by a 150 GB HBM budget into one resident
+    batch and advanced `chunk` steps per persistent launch.  Latency is
+    wall-clock from arrival to the result (fields and norms) on the host."""
+    from pixelflow_gb300 import geometry as G
+    from pixelflow_gb300.serve import Server, summarize
+    from pixelflow_gb300.solver import Case
+    reqs = G.serving_requests(count=count, rate=rate, seed=seed)
+    t0 = time.perf_counter()
+    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True) as srv:
+        res = srv.run(reqs, realtime=True)
+        wall = time.perf_counter() - t0
+        summ = summarize(res, wall)
+        summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes)
+    # the plain FP64 single-case step on a sample of the same requests, one after another
+    rng = np.random.default_rng(seed + 2)
+    tot_cells, tot_ms = 0, 0.0
+    for k in rng.choice(len(reqs), size=min(baseline_sample, len(reqs)), replace=False):
+        r = reqs[int(k)]
+        with Case.from_shapes(r.settings.replace(precision="fp64"), r.shape, r.shapes) as c:
+            c.initial_conditions()
+            c.step(1)
+            c.synchronize()
+            c.profile_begin()
+            c.step(baseline_steps)
+            prof = c.profile_end()
+        tot_cells += r.cells * baseline_steps
+        tot_ms += prof["step_ms"]
+    plain = tot_cells / (tot_ms / 1e3) / 1e6
+    summ["workload"] = (f"{count} requests, Poisson {rate:g}/s, 70% 2D 128^2-1024^2 / 30% 3D 64^3-192^3, "
+                        f"100-1000 steps, 150 GB budget, chunk {chunk}")
+    summ["plain_fp64_sequential"] = {"value": plain, "unit": UNIT, "sample_requests": int(min(baseline_sample, len(reqs))),
+                                     "steps_each": baseline_steps}
+    summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain
+    return summ
+
+
 def run_reference(args):
     rank, world, _ = dist_setup()
     if rank != 0:
@@ -219,7 +310,24 @@ def run_reference(args):
     barrier(world)
 
 
+def run_batch_line(args):
+    rank, world, local = dist_setup()
+    from pixelflow_gb300 import _lib
+    _lib.check(_lib.load().pf_set_device(local))
+    r = bench_batch(steps=args.steps, warmup_steps=max(1, args.warmup // 2))
+    line = {"metric": METRIC, "value": r["value"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": r["workload"], "precision": "mixed", "form": "batched persistent kernel"},
+            "batch": r, "gpu_launches": r["launches_in_timed_region"]}
+    barrier(world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
+    if args.workload == "batch2d":
+        return run_batch_line(args)
     rank, world, local = dist_setup()
     from pixelflow_gb300 import _lib
     from pixelflow_gb300.solver import Case, host_register, host_unregister
@@ -299,6 +407,24 @@ def run_ours(args):
     line["gpu_launches"] = launches
     line["clocks"] = clocks
     case.close()
+    if args.forms and args.precision == "fp64" and args.workload.startswith("spheres3d"):
+        # the precision form on the same case, and the batched form (2D batch)
+        mc = Case(s.replace(precision="mixed"), shape, vals)
+        mc.initial_conditions()
+        mc.step(args.warmup)
+        mc.synchronize()
+        mc.profile_begin()
+        mc.step(args.steps)
+        mp = mc.profile_end()
+        mdiv, _ = mc.norms()
+        mc.close()
+        mval = world * cells * args.steps / (reduce_max(mp["step_ms"], world) / 1e3) / 1e6
+        line["forms"] = {"mixed_same_case": {"value": mval, "unit": UNIT, "max_div": mdiv,
+                                             "speedup_vs_plain_fp64": mval / value,
+                                             "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation"}}
+        if not args.no_batch:
+            line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
+            line["forms"]["serving"] = bench_serving()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)
     barrier(world)
@@ -315,6 +441,8 @@ def main():
     ap.add_argument("--workload", default="spheres3d_256")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", type=int, default=1, help="also measure the precision and batched forms")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         raise SystemExit("--warmup must be >= 3")

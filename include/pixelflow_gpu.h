@@ -90,6 +90,25 @@ int pf_create(const pf_params *prm, const pf_options *opt, const double *porosit
               pf_case **out);
 int pf_destroy(pf_case *c);
 
+/* Create a case whose porosity is generated on the GPU from analytic shapes,
+ * with the profile of the reference's preprocessing tools
+ * (tools/cylinder/make_porosity_2d_cylinder.py:119-122):
+ *   porosity = max(threshold, 0.5*tanh(sdf/(edge*dx)) + 0.5),
+ * sdf = min over the shapes of the signed distance (positive in the fluid),
+ * node (i,j,k) at ((i-1)dx, (j-1)dy, (k-1)dz).  Circles and ellipses (2D,
+ * ellipse distance to first order) and spheres (3D); at most PF_MAX_SHAPES.
+ * Same set-up as pf_create otherwise. */
+enum { PF_SHAPE_CIRCLE = 0, PF_SHAPE_ELLIPSE = 1, PF_SHAPE_SPHERE = 2 };
+#define PF_MAX_SHAPES 32
+typedef struct pf_shape {
+  int32_t kind, reserved;
+  double cx, cy, cz; /* centre (cz ignored in 2D) */
+  double a, b;       /* radius / semi-axes */
+  double angle;      /* ellipse rotation (radians) */
+} pf_shape;
+int pf_create_shapes(const pf_params *prm, const pf_options *opt, const pf_shape *shapes, int nshapes,
+                     double edge, pf_case **out);
+
 /* initial_conditions followed by boundary
  * (ibm_2d_uniform_omp_cpu.f90:67-70 / ibm_3d_uniform_omp_cpu.f90:68-71). */
 int pf_initial_conditions(pf_case *c);
@@ -145,6 +164,50 @@ int pf_kernel_launches(pf_case *c, int64_t *count);
 
 /* Device memory held by the case, in bytes. */
 int pf_memory_bytes(pf_case *c, size_t *bytes);
+
+/* ---- Batched form -------------------------------------------------------
+ * Many independent cases (2D and 3D, uneven sizes) resident on one GPU,
+ * advanced by one persistent kernel per dimension: each thread-block cluster
+ * claims a case from a device queue (largest work first) and runs all stages
+ * of its steps itself, separated by hardware cluster barriers.  Cases run the
+ * precision form (PF_PREC_MIXED) with the per-case options given at add time.
+ * No counterpart in the reference, which runs one case per process; the
+ * per-case step is the same routine sequence as pf_step. */
+typedef struct pf_batch pf_batch;
+typedef struct pf_batch_options {
+  int32_t cluster;           /* CTAs per cluster: 1, 2, 4 or 8 */
+  int32_t threads;           /* threads per CTA: 256, 512 or 1024 */
+  int32_t max_cases;         /* slots */
+  int32_t reserved0;
+  uint64_t hbm_budget_bytes; /* admission limit for the cases' device memory */
+  int32_t reserved[8];
+} pf_batch_options;
+void pf_batch_default_options(pf_batch_options *opt); /* cluster 4, 512 threads, 1024 slots, 150 GiB */
+int pf_batch_create(const pf_batch_options *opt, pf_batch **out);
+int pf_batch_destroy(pf_batch *b);
+/* Device bytes a case needs (same accounting as the admission check). */
+int pf_case_bytes(const pf_params *prm, const pf_options *opt, size_t *bytes);
+/* Add a case (initial conditions applied).  PF_E_NOMEM when it does not fit
+ * the budget now, PF_E_BUSY when no slot is free. */
+int pf_batch_add(pf_batch *b, const pf_params *prm, const pf_options *opt, const double *porosity_values,
+                 int *slot);
+int pf_batch_add_shapes(pf_batch *b, const pf_params *prm, const pf_options *opt, const pf_shape *shapes,
+                        int nshapes, double edge, int *slot);
+int pf_batch_remove(pf_batch *b, int slot);
+/* Advance slots[q] by nsteps[q] steps, all in one persistent launch per
+ * dimension; returns when the launch has finished. */
+int pf_batch_step_slots(pf_batch *b, const int *slots, const int *nsteps, int n);
+int pf_batch_step(pf_batch *b, int nsteps); /* every occupied slot */
+int pf_batch_synchronize(pf_batch *b);
+int pf_batch_get_state(pf_batch *b, int slot, double *u, double *v, double *w, double *p, int ld1, int ld2);
+int pf_batch_norms(pf_batch *b, int slot, double *max_div, double *sor_error);
+int pf_batch_memory(pf_batch *b, size_t *in_use, size_t *budget);
+int pf_batch_kernel_launches(pf_batch *b, int64_t *n);
+/* Change the launch shape (CTAs per cluster, threads per CTA) used by later
+ * steps; the autotuner calls this between timed trials. */
+int pf_batch_configure(pf_batch *b, int cluster, int threads);
+/* Device time (CUDA events on the batch stream) of the last step call. */
+int pf_batch_last_ms(pf_batch *b, double *ms);
 
 /* max|div u| without allocating device memory.  No counterpart in the
  * reference: it exists for callers that must not call cudaMalloc at this

@@ -41,6 +41,23 @@ class PfOptions(ctypes.Structure):
     ]
 
 
+class PfShape(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32), ("cx", ctypes.c_double),
+                ("cy", ctypes.c_double), ("cz", ctypes.c_double), ("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("angle", ctypes.c_double)]
+
+
+PF_SHAPE_CIRCLE, PF_SHAPE_ELLIPSE, PF_SHAPE_SPHERE = 0, 1, 2
+PF_MAX_SHAPES = 32
+
+
+class PfBatchOptions(ctypes.Structure):
+    _fields_ = [
+        ("cluster", ctypes.c_int32), ("threads", ctypes.c_int32), ("max_cases", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("reserved", ctypes.c_int32 * 8),
+    ]
+
+
 class PfError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
@@ -60,6 +77,8 @@ _PROTOS = {
     "pf_default_options": (None, [ctypes.POINTER(PfOptions)]),
     "pf_create": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), _VP, ctypes.POINTER(_VP)]),
     "pf_destroy": (_I, [_VP]),
+    "pf_create_shapes": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), _VP, _I, _D,
+                              ctypes.POINTER(_VP)]),
     "pf_initial_conditions": (_I, [_VP]),
     "pf_set_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
     "pf_get_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
@@ -79,6 +98,23 @@ _PROTOS = {
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
+    "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),
+    "pf_batch_create": (_I, [ctypes.POINTER(PfBatchOptions), ctypes.POINTER(_VP)]),
+    "pf_batch_destroy": (_I, [_VP]),
+    "pf_case_bytes": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), ctypes.POINTER(ctypes.c_size_t)]),
+    "pf_batch_add": (_I, [_VP, ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), _VP, ctypes.POINTER(_I)]),
+    "pf_batch_add_shapes": (_I, [_VP, ctypes.POINTER(PfParams), ctypes.POINTER(PfOptions), _VP, _I, _D,
+                                 ctypes.POINTER(_I)]),
+    "pf_batch_remove": (_I, [_VP, _I]),
+    "pf_batch_step_slots": (_I, [_VP, _VP, _VP, _I]),
+    "pf_batch_step": (_I, [_VP, _I]),
+    "pf_batch_synchronize": (_I, [_VP]),
+    "pf_batch_get_state": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _I, _I]),
+    "pf_batch_norms": (_I, [_VP, _I, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "pf_batch_memory": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+    "pf_batch_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
+    "pf_batch_configure": (_I, [_VP, _I, _I]),
+    "pf_batch_last_ms": (_I, [_VP, ctypes.POINTER(_D)]),
 }
 
 

@@ -6,6 +6,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,6 +46,9 @@ int make_geo(const pf_params& p, Geo& g) {
   g.H = round_up((g.m + 1) / 2 + 1, 32);
   g.nat = (long long)g.X * g.Y * g.Z;
   g.pk = (long long)g.H * g.Y * g.Z;
+  const long long dense = (long long)(g.m + 2) * (g.n + 2) * g.Z;
+  if (g.nat >= (1LL << 31) || g.pk >= (1LL << 31) || dense >= (1LL << 31))
+    return fail(PF_E_INVALID, "grid too large: arrays are limited to 2^31 elements");
   g.jn_n = (g.n % 2 == 0) ? 1 : g.n + 1;
   g.js_1 = (g.n % 2 == 0) ? g.n : 0;
   g.kt_l = (g.l % 2 == 0) ? 1 : g.l + 1;
@@ -167,7 +171,7 @@ static int case_alloc(pf_case* c) {
   req.push_back({&c->stage, stage});
   size_t total = 0;
   for (auto& r : req) total += (r.bytes + 255) / 256 * 256;
-  total += 256;  // reductions
+  total += RED_TOTAL * sizeof(unsigned long long);  // reductions
   char* base = nullptr;
   cudaError_t e = cudaMalloc(&base, total);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(case)");
@@ -203,10 +207,10 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
   cudaStream_t st = c->st;
   const int o = c->cur, nw = 1 - c->cur;
   const bool track = c->opt.track_sor_error != 0;
-  if (track) cudaMemsetAsync(&c->red[0], 0, sizeof(unsigned long long), st);
+  if (track) cudaMemsetAsync(&c->red[RED_ERR], 0, RED_SLOTS * sizeof(unsigned long long), st);
   launch_divergence<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, st);
-  launch_predictor<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv, c->damp,
-                           c->U[nw], c->V[nw], c->W[nw], st);
+  launch_predictor<double, double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv,
+                                   c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
@@ -215,7 +219,7 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
     for (int col = 0; col < 2; col++) {
       if (halo) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
       // 2D tracks both half-sweeps (ibm_2d:351,385); 3D only the second (ibm_3d:575-583)
-      unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[0] : nullptr;
+      unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERR] : nullptr;
       launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, st);
     }
   }
@@ -328,8 +332,10 @@ void pf_default_options(pf_options* opt) {
   opt->use_graph = 1;
 }
 
-int pf_create(const pf_params* prm, const pf_options* opt, const double* porosity_values, pf_case** out) {
-  if (!prm || !porosity_values || !out) return fail(PF_E_INVALID, "pf_create: null argument");
+}  // extern "C"
+
+// Allocation and scalars of a new case; the porosity comes next.
+static int create_case(const pf_params* prm, const pf_options* opt, pf_case** out) {
   *out = nullptr;
   pf_case* c = new pf_case();
   c->prm = *prm;
@@ -341,6 +347,8 @@ int pf_create(const pf_params* prm, const pf_options* opt, const double* porosit
   if (rc == PF_OK) rc = make_scal(c->prm, c->s);
   if (rc == PF_OK && c->opt.precision != PF_PREC_FP64 && c->opt.precision != PF_PREC_MIXED)
     rc = fail(PF_E_INVALID, "unknown precision");
+  if (rc == PF_OK && c->opt.precision == PF_PREC_MIXED && (c->opt.outer_max < 0 || c->opt.inner_sweeps < 0))
+    rc = fail(PF_E_INVALID, "outer_max and inner_sweeps must be >= 0");
   if (rc != PF_OK) {
     delete c;
     return rc;
@@ -352,7 +360,7 @@ int pf_create(const pf_params* prm, const pf_options* opt, const double* porosit
   }
   rc = case_alloc(c);
   if (rc == PF_OK) {
-    e = cudaHostAlloc(&c->hred, 4 * sizeof(unsigned long long), cudaHostAllocDefault);
+    e = cudaHostAlloc(&c->hred, RED_TOTAL * sizeof(unsigned long long), cudaHostAllocDefault);
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaHostAlloc");
   }
   if (rc == PF_OK && c->opt.precision == PF_PREC_MIXED) rc = mixed_alloc(c);
@@ -360,25 +368,54 @@ int pf_create(const pf_params* prm, const pf_options* opt, const double* porosit
     case_free(c);
     return rc;
   }
-  // porosity with ghosts (host, once), then the time-invariant factors
-  std::vector<double> por;
-  build_porosity(c->g, c->prm.threshold, porosity_values, por);
+  *out = c;
+  return PF_OK;
+}
+
+// Porosity in c->stage (dense, ghosts filled) -> device layouts and the
+// time-invariant factors and operator.
+static int finish_setup(pf_case* c) {
   const Geo& g = c->g;
-  e = cudaMemcpyAsync(c->stage, por.data(), por.size() * sizeof(double), cudaMemcpyHostToDevice, c->st);
-  if (e != cudaSuccess) {
-    case_free(c);
-    return cuda_fail(e, "cudaMemcpyAsync(porosity)");
-  }
   launch_scatter_nat(g, c->stage, c->poro, c->st);
   launch_porosity_factors(g, c->s, c->poro, c->gx, c->gy, c->gz, c->rinv, c->damp, c->st);
   launch_setup_coef(g, c->s, c->poro, c->C[0], c->C[1], c->st);
   if (c->opt.precision == PF_PREC_MIXED) mixed_setup(c);
-  rc = check_launch("pf_create kernels");
-  if (rc == PF_OK) {
-    e = cudaStreamSynchronize(c->st);  // `por` goes out of scope
-    if (e != cudaSuccess) rc = cuda_fail(e, "pf_create sync");
+  int rc = check_launch("case set-up kernels");
+  if (rc) return rc;
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  return PF_OK;
+}
+
+extern "C" {
+
+int pf_create(const pf_params* prm, const pf_options* opt, const double* porosity_values, pf_case** out) {
+  if (!prm || !porosity_values || !out) return fail(PF_E_INVALID, "pf_create: null argument");
+  pf_case* c = nullptr;
+  int rc = create_case(prm, opt, &c);
+  if (rc) return rc;
+  // porosity with ghosts (host, once), then the time-invariant factors
+  std::vector<double> por;
+  build_porosity(c->g, c->prm.threshold, porosity_values, por);
+  cudaError_t e =
+      cudaMemcpyAsync(c->stage, por.data(), por.size() * sizeof(double), cudaMemcpyHostToDevice, c->st);
+  rc = e != cudaSuccess ? cuda_fail(e, "cudaMemcpyAsync(porosity)") : finish_setup(c);
+  if (rc) {
+    case_free(c);
+    return rc;
   }
-  if (rc != PF_OK) {
+  *out = c;
+  return PF_OK;
+}
+
+int pf_create_shapes(const pf_params* prm, const pf_options* opt, const pf_shape* shapes, int nshapes,
+                     double edge, pf_case** out) {
+  if (!prm || !out) return fail(PF_E_INVALID, "pf_create_shapes: null argument");
+  pf_case* c = nullptr;
+  int rc = create_case(prm, opt, &c);
+  if (rc) return rc;
+  rc = geometry_to_stage(c, shapes, nshapes, edge);
+  if (rc == PF_OK) rc = finish_setup(c);
+  if (rc) {
     case_free(c);
     return rc;
   }
@@ -455,7 +492,6 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   int rc = check_ld(c, ld1, ld2);
   if (rc) return rc;
   const Geo& g = c->g;
-  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_to_fp64(c);
   const size_t hp = (size_t)ld1 * sizeof(double), dp = (size_t)g.X * sizeof(double);
   const int b = c->cur;
   double* dst[3] = {u, v, w};
@@ -549,19 +585,28 @@ int pf_synchronize(pf_case* c) {
 int pf_norms(pf_case* c, double* max_div, double* sor_error) {
   if (!c) return fail(PF_E_INVALID, "null handle");
   const Geo& g = c->g;
-  if (c->opt.precision == PF_PREC_MIXED) mixed_sync_to_fp64(c);
-  PF_CUDA(cudaMemsetAsync(&c->red[1], 0, sizeof(unsigned long long), c->st));
+  PF_CUDA(cudaMemsetAsync(&c->red[RED_DIV], 0, RED_SLOTS * sizeof(unsigned long long), c->st));
   const int b = c->cur;
-  launch_div_diag<double>(g, c->s, c->U[b], c->V[b], c->W[b], c->poro, c->gx, c->gy, c->gz, &c->red[1], c->st);
+  launch_div_diag<double>(g, c->s, c->U[b], c->V[b], c->W[b], c->poro, c->gx, c->gy, c->gz, &c->red[RED_DIV], c->st);
   c->launches += 1;
   int rc = check_launch("pf_norms");
   if (rc) return rc;
-  PF_CUDA(cudaMemcpyAsync(c->hred, c->red, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+  PF_CUDA(cudaMemcpyAsync(c->hred, c->red, RED_TOTAL * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
   PF_CUDA(cudaStreamSynchronize(c->st));
+  unsigned long long be = 0, bd = 0;
+  unsigned bf = 0;
+  for (int q = 0; q < RED_SLOTS; q++) {
+    be = std::max(be, c->hred[RED_ERR + q]);
+    bd = std::max(bd, c->hred[RED_DIV + q]);
+    // FP32 sweeps of the mixed form track their max change in the low halves
+    bf = std::max(bf, (unsigned)(c->hred[RED_ERRF + q] & 0xffffffffULL));
+  }
   double e, d;
-  unsigned long long be = c->hred[0], bd = c->hred[1];
   std::memcpy(&e, &be, sizeof(double));
   std::memcpy(&d, &bd, sizeof(double));
+  float ef;
+  std::memcpy(&ef, &bf, sizeof(float));
+  if (std::isnan(ef) || (double)ef > e) e = (double)ef;  // NaN propagates
   if (sor_error) *sor_error = e;
   if (max_div) *max_div = d;
   if (!std::isfinite(d)) return fail(PF_E_NONFINITE, "max|div u| is not finite");

@@ -61,4 +61,5 @@ void mixed_sync_to_fp64(pf_case* c);
 void enqueue_solve_p_mixed(pf_case* c, bool prof);
 void enqueue_projection_mixed(pf_case* c);
 void enqueue_boundary_mixed(pf_case* c);
+int geometry_to_stage(pf_case* c, const pf_shape* shapes, int nshapes, double edge);
 }  // namespace pf

@@ -1,0 +1,500 @@
+// pf_cells.cuh -- per-cell bodies of the step's stages, shared by the
+// single-case kernels (pf_kernels.cu) and the persistent batch kernel
+// (pf_batch.cu), so every form computes a cell with the same arithmetic.
+//
+// Arithmetic: the algebra of each reference expression is kept, but the
+// operations are reordered for the GPU: divisions by dx, ap and porosity
+// become multiplications by factors computed once per case, and products
+// fuse into FMAs.  Results therefore differ from the reference in the last
+// bits of each operation; the parity tests bound the drift over whole runs.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pf_internal.cuh"
+
+namespace pf {
+
+constexpr int BX = 32, BY = 8;
+
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned abs_bits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+
+// Block-wide max of non-negative IEEE bit patterns (integer order == value
+// order for non-negative numbers; NaN patterns sort above +Inf), then one
+// atomicMax per block.  Order independent, hence deterministic.  The 64-bit
+// patterns are compared as (hi, lo) 32-bit pairs so the reduction stays on
+// the integer pipe (the FP64 pipe is the scarce one on GB300).
+__device__ __forceinline__ void max_pair(unsigned& hi, unsigned& lo, unsigned h2, unsigned l2) {
+  const bool gt = (h2 > hi) || (h2 == hi && l2 > lo);
+  hi = gt ? h2 : hi;
+  lo = gt ? l2 : lo;
+}
+
+__device__ __forceinline__ int red_slot() {
+  return (int)((blockIdx.x + 37u * blockIdx.y + 101u * blockIdx.z) & (RED_SLOTS - 1));
+}
+
+__device__ __forceinline__ unsigned long long max_of_slots(const unsigned long long* s) {
+  unsigned long long r = 0;
+  for (int i = 0; i < RED_SLOTS; i++) r = s[i] > r ? s[i] : r;
+  return r;
+}
+
+__device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned long long* out) {
+  __shared__ unsigned long long red[32];
+  unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
+  for (int o = 16; o > 0; o >>= 1) max_pair(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, warp = tid >> 5;
+  if (lane == 0) red[warp] = ((unsigned long long)hi << 32) | lo;
+  __syncthreads();
+  if (warp == 0) {
+    const unsigned long long w = (lane < (nthr + 31) / 32) ? red[lane] : 0ULL;
+    hi = (unsigned)(w >> 32);
+    lo = (unsigned)w;
+    for (int o = 16; o > 0; o >>= 1)
+      max_pair(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+    const unsigned long long r = ((unsigned long long)hi << 32) | lo;
+    if (lane == 0 && r) atomicMax(out + red_slot(), r);
+  }
+}
+
+// FP32 magnitudes: 32-bit patterns, max into the low 32 bits of *slot.
+__device__ __forceinline__ void block_max_atomic(unsigned v, unsigned long long* slot) {
+  __shared__ unsigned red[32];
+  v = __reduce_max_sync(0xffffffffu, v);
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, warp = tid >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = (lane < (nthr + 31) / 32) ? red[lane] : 0u;
+    v = __reduce_max_sync(0xffffffffu, v);
+    if (lane == 0 && v) atomicMax(reinterpret_cast<unsigned*>(slot + red_slot()), v);
+  }
+}
+
+
+__device__ __forceinline__ idx_t pk_of(const Geo& g, int i, int j, int k, int& c) {
+  c = colour_of(g, i, j, k);
+  return pk_idx(g, i >> 1, j, k);
+}
+
+
+template <typename T>
+__device__ __forceinline__ T& pref(const Geo& g, T* p0, T* p1, int i, int j, int k) {
+  int c;
+  idx_t r = pk_of(g, i, j, k, c);
+  return c ? p1[r] : p0[r];
+}
+
+
+// The ghost cells of the old fields carry over into the new buffer (the
+// reference's u keeps its ghosts through solve_p): every interior cell next to
+// the ghost layer copies the ghost cells it touches -- faces, edges and
+// corners, each ghost copied by exactly one interior cell.
+template <typename T, int DIM>
+__device__ __forceinline__ void keep_ghosts(const Geo& g, int i, int j, int k, idx_t q, const T* uo,
+                                            const T* vo, const T* wo, T* u, T* v, T* w) {
+  const int i0 = i == 1 ? -1 : 0, i1 = i == g.m ? 1 : 0;
+  const int j0 = j == 1 ? -1 : 0, j1 = j == g.n ? 1 : 0;
+  const int k0 = (DIM == 3 && k == 1) ? -1 : 0, k1 = (DIM == 3 && k == g.l) ? 1 : 0;
+  if (!(i0 | i1 | j0 | j1 | k0 | k1)) return;
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
+  for (int dk = k0; dk <= k1; dk++)
+    for (int dj = j0; dj <= j1; dj++)
+      for (int di = i0; di <= i1; di++) {
+        if (!(di | dj | dk)) continue;
+        const idx_t r = q + di + X * dj + XY * dk;
+        u[r] = uo[r];
+        v[r] = vo[r];
+        if (DIM == 3) w[r] = wo[r];
+      }
+}
+
+
+template <typename T>
+__device__ __forceinline__ void c_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* __restrict__ vo,
+                             const T* __restrict__ wo, T* __restrict__ div, int i, int j, int k) {
+  const idx_t q = nat_idx(g, i, j, k);
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
+  const T hx = (T)(0.5 / s.dx);
+  if (g.dim == 3) {
+    const T hy = (T)(0.5 / s.dy), hz = (T)(0.5 / s.dz);
+    T d = (uo[q + 1] - uo[q - 1]) * hx;
+    d = fma(vo[q + X] - vo[q - X], hy, d);
+    d = fma(wo[q + XY] - wo[q - XY], hz, d);
+    div[q] = d;
+  } else {
+    div[q] = fma(vo[q + X] - vo[q - X], hx, (uo[q + 1] - uo[q - 1]) * hx);
+  }
+}
+
+template <typename T, typename TS, int DIM>
+__device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__ uo,
+                                                      const T* __restrict__ vo, const T* __restrict__ wo,
+                                                      const T* __restrict__ div, const T* __restrict__ gxa,
+                                                      const T* __restrict__ gya, const T* __restrict__ gza,
+                                                      const T* __restrict__ rinva, const T* __restrict__ dampa,
+                                                      const TS* __restrict__ su, const TS* __restrict__ sv,
+                                                      const TS* __restrict__ sw, TS* __restrict__ u,
+                                                      TS* __restrict__ v, TS* __restrict__ w, int i, int j, int k) {
+  const idx_t q = nat_idx(g, i, j, k);
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
+  const T hx = (T)(0.5 / s.dx), hy = (T)(0.5 / s.dy);
+  const T ix2 = (T)(1.0 / (s.dx * s.dx)), iy2 = (T)(1.0 / (s.dy * s.dy));
+  const T dt = (T)s.dt, nu = (T)s.xnue, lam = (T)s.xlambda;
+  const T dtnu = (T)(s.dt * s.xnue), dtnl = (T)(s.dt * (s.xnue + s.xlambda));
+  const T two = (T)2;
+  // div neighbours with the periodic wrap of the y (and z) ghost rows
+  const idx_t jn = (j == g.n) ? q - (idx_t)(g.n - 1) * X : q + X;
+  const idx_t js = (j == 1) ? q + (idx_t)(g.n - 1) * X : q - X;
+  const T dc = div[q], dE = div[q + 1], dW = div[q - 1], dN = div[jn], dS = div[js];
+  const T gx = gxa[q], gy = gya[q], rv = rinva[q], dp = dampa[q];
+
+  const T uc = uo[q], ue = uo[q + 1], uw = uo[q - 1], un = uo[q + X], us = uo[q - X];
+  const T vc = vo[q], ve = vo[q + 1], vw = vo[q - 1], vn = vo[q + X], vs = vo[q - X];
+  const T dux = (ue - uw) * hx, duy = (un - us) * hy;
+  const T dvx = (ve - vw) * hx, dvy = (vn - vs) * hy;
+  const T lux = fma(-two, uc, ue + uw), luy = fma(-two, uc, un + us);
+  const T lvx = fma(-two, vc, ve + vw), lvy = fma(-two, vc, vn + vs);
+  if (DIM == 2) {
+    // u
+    T conv = fma(vc, duy, uc * dux);
+    T lap = fma(luy, iy2, lux * ix2);
+    T por = fma(duy + dvx, gy, (dux + dux) * gx) * nu;
+    por = fma(lam * dc, gx, por);
+    T t = -dt * conv;
+    t = fma(dtnu, lap, t);
+    t = fma(dtnl, (dE - dW) * hx, t);
+    t = fma(rv, por, t);
+    u[q] = su[q] + (TS)fma(-uc, dp * ix2, t);
+    // v (the reference damps v with (thickness*dx)^2 as well, ibm_2d:254)
+    conv = fma(vc, dvy, uc * dvx);
+    lap = fma(lvy, iy2, lvx * ix2);
+    por = fma(dvy + dvy, gy, (dvx + duy) * gx) * nu;
+    por = fma(lam * dc, gy, por);
+    t = -dt * conv;
+    t = fma(dtnu, lap, t);
+    t = fma(dtnl, (dN - dS) * hy, t);
+    t = fma(rv, por, t);
+    v[q] = sv[q] + (TS)fma(-vc, dp * ix2, t);
+  } else {
+    const T hz = (T)(0.5 / s.dz), iz2 = (T)(1.0 / (s.dz * s.dz));
+    const idx_t kt = (k == g.l) ? q - (idx_t)(g.l - 1) * XY : q + XY;
+    const idx_t kb = (k == 1) ? q + (idx_t)(g.l - 1) * XY : q - XY;
+    const T dT = div[kt], dB = div[kb];
+    const T gz = gza[q];
+    const T ut = uo[q + XY], ub = uo[q - XY], vt = vo[q + XY], vb = vo[q - XY];
+    const T wc = wo[q], we = wo[q + 1], ww = wo[q - 1], wn = wo[q + X], ws = wo[q - X];
+    const T wt = wo[q + XY], wb = wo[q - XY];
+    const T duz = (ut - ub) * hz, dvz = (vt - vb) * hz;
+    const T dwx = (we - ww) * hx, dwy = (wn - ws) * hy, dwz = (wt - wb) * hz;
+    const T luz = fma(-two, uc, ut + ub), lvz = fma(-two, vc, vt + vb);
+    const T lwx = fma(-two, wc, we + ww), lwy = fma(-two, wc, wn + ws), lwz = fma(-two, wc, wt + wb);
+    // u
+    T conv = fma(wc, duz, fma(vc, duy, uc * dux));
+    T lap = fma(luz, iz2, fma(luy, iy2, lux * ix2));
+    T por = fma(duz + dwx, gz, fma(duy + dvx, gy, (dux + dux) * gx)) * nu;
+    por = fma(lam * dc, gx, por);
+    T t = -dt * conv;
+    t = fma(dtnu, lap, t);
+    t = fma(dtnl, (dE - dW) * hx, t);
+    t = fma(rv, por, t);
+    u[q] = su[q] + (TS)fma(-uc, dp * ix2, t);
+    // v
+    conv = fma(wc, dvz, fma(vc, dvy, uc * dvx));
+    lap = fma(lvz, iz2, fma(lvy, iy2, lvx * ix2));
+    por = fma(dvz + dwy, gz, fma(dvy + dvy, gy, (dvx + duy) * gx)) * nu;
+    por = fma(lam * dc, gy, por);
+    t = -dt * conv;
+    t = fma(dtnu, lap, t);
+    t = fma(dtnl, (dN - dS) * hy, t);
+    t = fma(rv, por, t);
+    v[q] = sv[q] + (TS)fma(-vc, dp * iy2, t);
+    // w
+    conv = fma(wc, dwz, fma(vc, dwy, uc * dwx));
+    lap = fma(lwz, iz2, fma(lwy, iy2, lwx * ix2));
+    por = fma(dwz + dwz, gz, fma(dwy + dvz, gy, (dwx + duz) * gx)) * nu;
+    por = fma(lam * dc, gz, por);
+    t = -dt * conv;
+    t = fma(dtnu, lap, t);
+    t = fma(dtnl, (dT - dB) * hz, t);
+    t = fma(rv, por, t);
+    w[q] = sw[q] + (TS)fma(-wc, dp * iz2, t);
+  }
+  keep_ghosts<TS, DIM>(g, i, j, k, q, su, sv, sw, u, v, w);
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void c_rhs(Geo g, Scal s, const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ w,
+                      const double* __restrict__ po, const double* __restrict__ gxa,
+                      const double* __restrict__ gya, const double* __restrict__ gza, Coef<double> c0,
+                      Coef<double> c1, int i, int j, int k) {
+  const idx_t q = nat_idx(g, i, j, k);
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
+  const double hx = 0.5 / s.dx, hy = 0.5 / s.dy;
+  double sd = ((double)u[q + 1] - (double)u[q - 1]) * hx;
+  sd = fma((double)v[q + X] - (double)v[q - X], hy, sd);
+  double sg = gxa[q] * (double)u[q];
+  sg = fma(gya[q], (double)v[q], sg);
+  if (DIM == 3) {
+    sd = fma((double)w[q + XY] - (double)w[q - XY], 0.5 / s.dz, sd);
+    sg = fma(gza[q], (double)w[q], sg);
+  }
+  const double bb = s.density * fma(po[q], sd, sg);
+  const int c = colour_of(g, i, j, k);
+  const Coef<double> C = c ? c1 : c0;
+  const idx_t r = pk_idx(g, i >> 1, j, k);
+  C.bbn[r] = (bb + C.oadd[r]) * C.wap[r];
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void c_projection(Geo g, Scal s, const double* __restrict__ p0, const double* __restrict__ p1, T* u,
+                             T* v, T* w, int i, int j, int k) {
+  const idx_t q = nat_idx(g, i, j, k);
+  const int c = colour_of(g, i, j, k);
+  const double* P = c ? p0 : p1;  // every neighbour has the other colour
+  const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+  const idx_t r = pk_idx(g, i >> 1, j, k);
+  const int sx = i & 1;
+  const double cdt = s.dt / s.density;
+  u[q] = fma(-(T)(cdt * 0.5 / s.dx), (T)(P[r + sx] - P[r - 1 + sx]), u[q]);
+  v[q] = fma(-(T)(cdt * 0.5 / s.dy), (T)(P[r + H] - P[r - H]), v[q]);
+  if (DIM == 3) w[q] = fma(-(T)(cdt * 0.5 / s.dz), (T)(P[r + HY] - P[r - HY]), w[q]);
+}
+
+template <typename T>
+__device__ __forceinline__ void c_initial(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1, int i, int j, int k) {
+  const idx_t q = nat_idx(g, i, j, k);
+  u[q] = (T)s.init_u;
+  v[q] = (T)s.init_v;
+  if (g.dim == 3) w[q] = (T)0;
+  pref(g, p0, p1, i, j, k) = s.outlet_pressure;
+}
+
+// One red-black half-sweep update of cell (2h+s, j, k) of colour `colour`,
+// in place:  p = (1-omega) p + bbn - sum_nb a_nb p_nb  (all neighbours have
+// the other colour), which is the reference's
+//   p = (bb - sum a_nb p_old_nb)/ap*omega + p_old*(1-omega)
+// because no neighbour of a cell changes during its own colour's sweep.
+// Returns |p_new - p_old| as bits when TRACK (0 for cells outside the grid).
+template <typename T, int DIM, bool TRACK>
+__device__ __forceinline__ decltype(abs_bits(T(0))) c_sor_half(const Geo& g, const Coef<T>& C, T* __restrict__ pc,
+                                                              const T* __restrict__ po, T omw, int colour, int h,
+                                                              int j, int k) {
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const int i = 2 * h + s;
+  decltype(abs_bits(T(0))) e = 0;
+  if (j <= g.n && i >= 1 && i <= g.m) {
+    const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+    const idx_t q = pk_idx(g, h, j, k);
+    const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
+    const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
+    const T pold = pc[q];
+    T t = C.bbn[q];
+    t = fma(-C.a[0][q], po[q + s], t);
+    t = fma(-C.a[1][q], po[q - 1 + s], t);
+    t = fma(-C.a[2][q], po[qn], t);
+    t = fma(-C.a[3][q], po[qs], t);
+    if (DIM == 3) {
+      const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
+      const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
+      t = fma(-C.a[4][q], po[qt], t);
+      t = fma(-C.a[5][q], po[qb], t);
+    }
+    const T pnew = fma(omw, pold, t);
+    pc[q] = pnew;
+    if (TRACK) e = abs_bits(pnew - pold);
+  }
+  return e;
+}
+
+// FP64 residual of one cell, stored as the FP32 right-hand side of the
+// correction sweeps; zeroes e of that cell; returns |r| as bits.
+template <int DIM>
+__device__ __forceinline__ unsigned long long c_residual(const Geo& g, const Coef<double>& C,
+                                                         const double* __restrict__ pc, const double* __restrict__ po,
+                                                         double omega, int colour, float* __restrict__ rf,
+                                                         float* __restrict__ ec, int h, int j, int k) {
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const int i = 2 * h + s;
+  if (!(j <= g.n && i >= 1 && i <= g.m)) return 0ULL;
+  const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+  const idx_t q = pk_idx(g, h, j, k);
+  const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
+  const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
+  double t = C.bbn[q];
+  t = fma(-C.a[0][q], po[q + s], t);
+  t = fma(-C.a[1][q], po[q - 1 + s], t);
+  t = fma(-C.a[2][q], po[qn], t);
+  t = fma(-C.a[3][q], po[qs], t);
+  if (DIM == 3) {
+    const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
+    const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
+    t = fma(-C.a[4][q], po[qt], t);
+    t = fma(-C.a[5][q], po[qb], t);
+  }
+  t = fma(-omega, pc[q], t);
+  rf[q] = (float)t;
+  ec[q] = 0.0f;
+  return abs_bits(t);
+}
+
+// p += e for one interior cell of the given colour.
+template <int DIM>
+__device__ __forceinline__ void c_accumulate(const Geo& g, double* __restrict__ pcol, const float* __restrict__ ecol,
+                                             int colour, int h, int j, int k) {
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const int i = 2 * h + s;
+  if (j > g.n || i < 1 || i > g.m) return;
+  const idx_t q = pk_idx(g, h, j, k);
+  pcol[q] += (double)ecol[q];
+}
+
+// Periodic ghost rows of a packed pair for interior i: y rows of plane k
+// (ysel) or z planes of row j (3D), as the reference refreshes them before
+// each half-sweep (ibm_2d:322-327; ibm_3d:463-480).
+template <typename T>
+__device__ __forceinline__ void c_p_halo_y(const Geo& g, T* p0, T* p1, int i, int k) {
+  T* P[2] = {p0, p1};
+  int cs, cd;
+  idx_t s0 = pk_of(g, i, g.n, k, cs), d0 = pk_of(g, i, 0, k, cd);
+  P[cd][d0] = P[cs][s0];
+  s0 = pk_of(g, i, 1, k, cs);
+  d0 = pk_of(g, i, g.n + 1, k, cd);
+  P[cd][d0] = P[cs][s0];
+}
+template <typename T>
+__device__ __forceinline__ void c_p_halo_z(const Geo& g, T* p0, T* p1, int i, int j) {
+  T* P[2] = {p0, p1};
+  int cs, cd;
+  idx_t s0 = pk_of(g, i, j, g.l, cs), d0 = pk_of(g, i, j, 0, cd);
+  P[cd][d0] = P[cs][s0];
+  s0 = pk_of(g, i, j, 1, cs);
+  d0 = pk_of(g, i, j, g.l + 1, cd);
+  P[cd][d0] = P[cs][s0];
+}
+
+// boundary, x faces of row (j, k): inflow at i=1 and its ghost, outflow copy at m+1.
+template <typename T>
+__device__ __forceinline__ void c_bnd_x(const Geo& g, const Scal& s, T* u, T* v, T* w, double* p0, double* p1,
+                                        int j, int k) {
+  const idx_t q1 = nat_idx(g, 1, j, k), q0 = q1 - 1;
+  u[q1] = (T)s.inlet_u;
+  v[q1] = (T)s.inlet_v;
+  u[q0] = u[q1];
+  v[q0] = v[q1];
+  if (g.dim == 3) {
+    w[q1] = (T)0;
+    w[q0] = w[q1];
+  }
+  pref(g, p0, p1, 0, j, k) = pref(g, p0, p1, 2, j, k);
+  const idx_t qm = nat_idx(g, g.m + 1, j, k);
+  u[qm] = u[qm - 2];
+  v[qm] = v[qm - 2];
+  if (g.dim == 3) w[qm] = w[qm - 2];
+  pref(g, p0, p1, g.m + 1, j, k) = s.outlet_pressure;
+}
+
+// boundary, y faces: periodic ghost rows at column i of plane k.
+template <typename T>
+__device__ __forceinline__ void c_bnd_y(const Geo& g, T* u, T* v, T* w, double* p0, double* p1, int i, int k) {
+  const idx_t a = nat_idx(g, i, 0, k), b = nat_idx(g, i, g.n, k);
+  const idx_t c = nat_idx(g, i, g.n + 1, k), d = nat_idx(g, i, 1, k);
+  u[a] = u[b];
+  v[a] = v[b];
+  u[c] = u[d];
+  v[c] = v[d];
+  if (g.dim == 3) {
+    w[a] = w[b];
+    w[c] = w[d];
+  }
+  pref(g, p0, p1, i, 0, k) = pref(g, p0, p1, i, g.n, k);
+  pref(g, p0, p1, i, g.n + 1, k) = pref(g, p0, p1, i, 1, k);
+}
+
+// boundary, z faces (3D): periodic ghost planes at column i of row j.
+template <typename T>
+__device__ __forceinline__ void c_bnd_z(const Geo& g, T* u, T* v, T* w, double* p0, double* p1, int i, int j) {
+  const idx_t a = nat_idx(g, i, j, 0), b = nat_idx(g, i, j, g.l);
+  const idx_t c = nat_idx(g, i, j, g.l + 1), d = nat_idx(g, i, j, 1);
+  u[a] = u[b];
+  v[a] = v[b];
+  w[a] = w[b];
+  u[c] = u[d];
+  v[c] = v[d];
+  w[c] = w[d];
+  pref(g, p0, p1, i, j, 0) = pref(g, p0, p1, i, j, g.l);
+  pref(g, p0, p1, i, j, g.l + 1) = pref(g, p0, p1, i, j, 1);
+}
+
+// FP32 correction sweep with the operator rebuilt on the fly from the FP32
+// porosity (packed by colour, ghosts included), so a half-sweep streams only
+// porosity, r and e (24 bytes per update) instead of six stored
+// coefficients.  Same operator as k_setup_coef up to FP32 rounding:
+//   a_f = dt/h^2 * max(small, (eps_a+eps_b)/2), ap = -sum a_f (before the
+//   inlet/outlet edits), inlet: a_e += a_w, a_w = 0; outlet: all a_f = 0,
+//   e = (1-w) e + r - (w/ap) sum a_f e_f.
+struct DCConst {
+  float kx, ky, kz;  // dt/dx^2 etc.
+  float small, omega, omw;
+};
+
+template <int DIM>
+__device__ __forceinline__ void dc_update(const Geo& g, const DCConst& K, const float* __restrict__ epsc,
+                                          const float* __restrict__ epso, const float* __restrict__ r,
+                                          float* __restrict__ ec, const float* __restrict__ eo, int h, int j,
+                                          int k, int s, int i, float& eold, float& enew) {
+  const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+  const idx_t q = pk_idx(g, h, j, k);
+  const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
+  const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
+  // all loads first: this kernel is latency bound, not ALU bound
+  const float pc = epsc[q], pe = epso[q + s], pw = epso[q - 1 + s], pn = epso[q + H], ps = epso[q - H];
+  const float xe = eo[q + s], xw = eo[q - 1 + s], xn = eo[qn], xs = eo[qs];
+  const float rr = r[q];
+  eold = ec[q];
+  float pt = 0.f, pb = 0.f, xt = 0.f, xb = 0.f;
+  if (DIM == 3) {
+    const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
+    const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
+    pt = epso[q + HY];
+    pb = epso[q - HY];
+    xt = eo[qt];
+    xb = eo[qb];
+  }
+  float ae = K.kx * fmaxf(K.small, (pe + pc) * 0.5f);
+  float aw = K.kx * fmaxf(K.small, (pc + pw) * 0.5f);
+  const float an = K.ky * fmaxf(K.small, (pn + pc) * 0.5f);
+  const float as = K.ky * fmaxf(K.small, (pc + ps) * 0.5f);
+  float at = 0.f, ab = 0.f;
+  if (DIM == 3) {
+    at = K.kz * fmaxf(K.small, (pt + pc) * 0.5f);
+    ab = K.kz * fmaxf(K.small, (pc + pb) * 0.5f);
+  }
+  const float ap = -ae - aw - an - as - at - ab;
+  enew = fmaf(K.omw, eold, rr);
+  if (i != g.m) {
+    if (i == 1) {
+      ae += aw;
+      aw = 0.f;
+    }
+    float t = ae * xe;
+    t = fmaf(aw, xw, t);
+    t = fmaf(an, xn, t);
+    t = fmaf(as, xs, t);
+    if (DIM == 3) {
+      t = fmaf(at, xt, t);
+      t = fmaf(ab, xb, t);
+    }
+    enew = fmaf(-__fdividef(K.omega, ap), t, enew);
+  }
+}
+
+
+}  // namespace pf

@@ -36,15 +36,21 @@ struct Geo {
   int jn_n, js_1, kt_l, kb_1;
 };
 
-__host__ __device__ inline long long nat_idx(const Geo& g, int i, int j, int k) {
-  return (long long)i + (long long)g.X * ((long long)j + (long long)g.Y * k);
-}
-__host__ __device__ inline long long pk_idx(const Geo& g, int h, int j, int k) {
-  return (long long)h + (long long)g.H * ((long long)j + (long long)g.Y * k);
-}
+// Element indices are 32-bit (make_geo rejects grids whose arrays exceed
+// 2^31 elements): 64-bit index arithmetic was a large share of the
+// instructions of the latency-bound sweeps.
+using idx_t = int;
+__host__ __device__ inline idx_t nat_idx(const Geo& g, int i, int j, int k) { return i + g.X * (j + g.Y * k); }
+__host__ __device__ inline idx_t pk_idx(const Geo& g, int h, int j, int k) { return h + g.H * (j + g.Y * k); }
 __host__ __device__ inline int colour_of(const Geo& g, int i, int j, int k) {
   return (i + j + (g.dim == 3 ? k : 1)) & 1;
 }
+
+// Reduction slots of a case: each max-reduction spreads its per-block
+// atomics over RED_SLOTS addresses (one address would serialise tens of
+// thousands of atomics per launch in L2); readers take the max of the slots.
+constexpr int RED_SLOTS = 256;
+enum { RED_ERR = 0, RED_ERRF = 256, RED_DIV = 512, RED_RMAX = 768, RED_TOTAL = 1024 };
 
 // Scalars of one case, derived once on the host in double.
 struct Scal {
@@ -77,10 +83,10 @@ void launch_setup_coef(const Geo& g, const Scal& s, const double* poro, Coef<dou
 template <typename TV>
 void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, TV* div,
                        cudaStream_t st);
-template <typename TV>
-void launch_predictor(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, const TV* div,
-                      const TV* gx, const TV* gy, const TV* gz, const TV* rinv, const TV* damp, TV* u, TV* v,
-                      TV* w, cudaStream_t st);
+template <typename T, typename TS>
+void launch_predictor(const Geo& g, const Scal& s, const T* uo, const T* vo, const T* wo, const T* div,
+                      const T* gx, const T* gy, const T* gz, const T* rinv, const T* damp, const TS* us,
+                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st);
 template <typename TV>
 void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
                 const double* gx, const double* gy, const double* gz, Coef<double> c0, Coef<double> c1,
@@ -113,13 +119,16 @@ void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cuda
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);
 void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st);
-void launch_coef_to_float(const Geo& g, const Coef<double>& c, Coef<float> cf, cudaStream_t st);
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
 // staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts
 void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st);
 void launch_scatter_pk(const Geo& g, const double* stage, double* p0, double* p1, cudaStream_t st);
 void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* stage, cudaStream_t st);
+
+// ---- host helpers (pf_api.cu) -------------------------------------------
+int make_geo(const pf_params& p, Geo& g);
+int make_scal(const pf_params& p, Scal& s);
 
 // ---- host error plumbing (pf_api.cu) ----------------------------------
 void set_error(const std::string& msg);

@@ -21,51 +21,17 @@
 #include <cuda_runtime.h>
 
 #include "pf_internal.cuh"
+#include "pf_cells.cuh"
 
 namespace pf {
 
 namespace {
-
-constexpr int BX = 32, BY = 8;
 
 inline dim3 grid_interior(const Geo& g) {
   return dim3((g.m + BX - 1) / BX, (g.n + BY - 1) / BY, g.dim == 3 ? g.l : 1);
 }
 inline dim3 grid_all(const Geo& g) {
   return dim3((g.m + 2 + BX - 1) / BX, (g.n + 2 + BY - 1) / BY, g.Z);
-}
-
-__device__ __forceinline__ unsigned long long abs_bits(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
-}
-__device__ __forceinline__ unsigned long long abs_bits(float x) {
-  // widen so one accumulator type serves both precisions; |x| as double
-  // keeps the ordering of the float magnitudes.
-  return abs_bits((double)x);
-}
-
-// Block-wide max of non-negative IEEE bit patterns (integer order == value
-// order for non-negative doubles; NaN patterns sort above +Inf), then one
-// atomicMax per block.  Order independent, hence deterministic.
-__device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned long long* out) {
-  __shared__ unsigned long long red[32];
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = w > v ? w : v;
-  }
-  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  const int nthr = blockDim.x * blockDim.y * blockDim.z;
-  const int lane = tid & 31, warp = tid >> 5;
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    v = (lane < (nthr + 31) / 32) ? red[lane] : 0ULL;
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-      v = w > v ? w : v;
-    }
-    if (lane == 0 && v) atomicMax(out, v);
-  }
 }
 
 // ---------------------------------------------------------------------
@@ -79,8 +45,8 @@ __global__ void k_porosity_factors(Geo g, Scal s, const double* __restrict__ po,
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const long long X = g.X, XY = (long long)g.X * g.Y;
+  const idx_t q = nat_idx(g, i, j, k);
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
   const double e = po[q];
   gx[q] = (po[q + 1] - po[q - 1]) * (0.5 / s.dx);
   gy[q] = (po[q + X] - po[q - X]) * (0.5 / s.dy);
@@ -97,8 +63,8 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const long long X = g.X, XY = (long long)g.X * g.Y;
+  const idx_t q = nat_idx(g, i, j, k);
+  const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
   const double small = 1.e-6, dt = s.dt;
   const double e = po[q];
   double a[6];
@@ -127,7 +93,7 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
   const double wap = s.omega / ap;
   const int c = colour_of(g, i, j, k);
   const Coef<double> C = c ? c1 : c0;
-  const long long r = pk_idx(g, i >> 1, j, k);
+  const idx_t r = pk_idx(g, i >> 1, j, k);
   for (int d = 0; d < 2 * g.dim; d++) C.a[d][r] = a[d] * wap;
   C.wap[r] = wap;
   C.oadd[r] = oadd;
@@ -144,132 +110,30 @@ __global__ void k_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* _
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const long long X = g.X, XY = (long long)g.X * g.Y;
-  const T hx = (T)(0.5 / s.dx);
-  if (g.dim == 3) {
-    const T hy = (T)(0.5 / s.dy), hz = (T)(0.5 / s.dz);
-    T d = (uo[q + 1] - uo[q - 1]) * hx;
-    d = fma(vo[q + X] - vo[q - X], hy, d);
-    d = fma(wo[q + XY] - wo[q - XY], hz, d);
-    div[q] = d;
-  } else {
-    div[q] = fma(vo[q + X] - vo[q - X], hx, (uo[q + 1] - uo[q - 1]) * hx);
-  }
+  c_divergence<T>(g, s, uo, vo, wo, div, i, j, k);
 }
 
 // Predictor: explicit Euler of the porosity-weighted momentum equation.
 // Also copies the face ghosts of the old fields into the new ones, so the
 // RHS sees the previous step's ghosts exactly as the reference does.
-template <typename T, int DIM>
+// T: type of the stencil arithmetic and of the arrays it reads; TS: type of
+// the velocity state.  The predictor computes the increment u* - u_old in T
+// and adds it to the TS state, so with T = float, TS = double the stencils run
+// in FP32 while the state keeps FP64 precision.
+template <typename T, typename TS, int DIM>
 __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __restrict__ uo,
                                                       const T* __restrict__ vo, const T* __restrict__ wo,
                                                       const T* __restrict__ div, const T* __restrict__ gxa,
                                                       const T* __restrict__ gya, const T* __restrict__ gza,
                                                       const T* __restrict__ rinva, const T* __restrict__ dampa,
-                                                      T* __restrict__ u, T* __restrict__ v, T* __restrict__ w) {
+                                                      const TS* __restrict__ su, const TS* __restrict__ sv,
+                                                      const TS* __restrict__ sw, TS* __restrict__ u,
+                                                      TS* __restrict__ v, TS* __restrict__ w) {
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const long long X = g.X, XY = (long long)g.X * g.Y;
-  const T hx = (T)(0.5 / s.dx), hy = (T)(0.5 / s.dy);
-  const T ix2 = (T)(1.0 / (s.dx * s.dx)), iy2 = (T)(1.0 / (s.dy * s.dy));
-  const T dt = (T)s.dt, nu = (T)s.xnue, lam = (T)s.xlambda;
-  const T dtnu = (T)(s.dt * s.xnue), dtnl = (T)(s.dt * (s.xnue + s.xlambda));
-  const T two = (T)2;
-  // div neighbours with the periodic wrap of the y (and z) ghost rows
-  const long long jn = (j == g.n) ? q - (long long)(g.n - 1) * X : q + X;
-  const long long js = (j == 1) ? q + (long long)(g.n - 1) * X : q - X;
-  const T dc = div[q], dE = div[q + 1], dW = div[q - 1], dN = div[jn], dS = div[js];
-  const T gx = gxa[q], gy = gya[q], rv = rinva[q], dp = dampa[q];
-
-  const T uc = uo[q], ue = uo[q + 1], uw = uo[q - 1], un = uo[q + X], us = uo[q - X];
-  const T vc = vo[q], ve = vo[q + 1], vw = vo[q - 1], vn = vo[q + X], vs = vo[q - X];
-  const T dux = (ue - uw) * hx, duy = (un - us) * hy;
-  const T dvx = (ve - vw) * hx, dvy = (vn - vs) * hy;
-  const T lux = fma(-two, uc, ue + uw), luy = fma(-two, uc, un + us);
-  const T lvx = fma(-two, vc, ve + vw), lvy = fma(-two, vc, vn + vs);
-  if (DIM == 2) {
-    // u
-    T conv = fma(vc, duy, uc * dux);
-    T lap = fma(luy, iy2, lux * ix2);
-    T por = fma(duy + dvx, gy, (dux + dux) * gx) * nu;
-    por = fma(lam * dc, gx, por);
-    T t = fma(-dt, conv, uc);
-    t = fma(dtnu, lap, t);
-    t = fma(dtnl, (dE - dW) * hx, t);
-    t = fma(rv, por, t);
-    u[q] = fma(-uc, dp * ix2, t);
-    // v (the reference damps v with (thickness*dx)^2 as well, ibm_2d:254)
-    conv = fma(vc, dvy, uc * dvx);
-    lap = fma(lvy, iy2, lvx * ix2);
-    por = fma(dvy + dvy, gy, (dvx + duy) * gx) * nu;
-    por = fma(lam * dc, gy, por);
-    t = fma(-dt, conv, vc);
-    t = fma(dtnu, lap, t);
-    t = fma(dtnl, (dN - dS) * hy, t);
-    t = fma(rv, por, t);
-    v[q] = fma(-vc, dp * ix2, t);
-  } else {
-    const T hz = (T)(0.5 / s.dz), iz2 = (T)(1.0 / (s.dz * s.dz));
-    const long long kt = (k == g.l) ? q - (long long)(g.l - 1) * XY : q + XY;
-    const long long kb = (k == 1) ? q + (long long)(g.l - 1) * XY : q - XY;
-    const T dT = div[kt], dB = div[kb];
-    const T gz = gza[q];
-    const T ut = uo[q + XY], ub = uo[q - XY], vt = vo[q + XY], vb = vo[q - XY];
-    const T wc = wo[q], we = wo[q + 1], ww = wo[q - 1], wn = wo[q + X], ws = wo[q - X];
-    const T wt = wo[q + XY], wb = wo[q - XY];
-    const T duz = (ut - ub) * hz, dvz = (vt - vb) * hz;
-    const T dwx = (we - ww) * hx, dwy = (wn - ws) * hy, dwz = (wt - wb) * hz;
-    const T luz = fma(-two, uc, ut + ub), lvz = fma(-two, vc, vt + vb);
-    const T lwx = fma(-two, wc, we + ww), lwy = fma(-two, wc, wn + ws), lwz = fma(-two, wc, wt + wb);
-    // u
-    T conv = fma(wc, duz, fma(vc, duy, uc * dux));
-    T lap = fma(luz, iz2, fma(luy, iy2, lux * ix2));
-    T por = fma(duz + dwx, gz, fma(duy + dvx, gy, (dux + dux) * gx)) * nu;
-    por = fma(lam * dc, gx, por);
-    T t = fma(-dt, conv, uc);
-    t = fma(dtnu, lap, t);
-    t = fma(dtnl, (dE - dW) * hx, t);
-    t = fma(rv, por, t);
-    u[q] = fma(-uc, dp * ix2, t);
-    // v
-    conv = fma(wc, dvz, fma(vc, dvy, uc * dvx));
-    lap = fma(lvz, iz2, fma(lvy, iy2, lvx * ix2));
-    por = fma(dvz + dwy, gz, fma(dvy + dvy, gy, (dvx + duy) * gx)) * nu;
-    por = fma(lam * dc, gy, por);
-    t = fma(-dt, conv, vc);
-    t = fma(dtnu, lap, t);
-    t = fma(dtnl, (dN - dS) * hy, t);
-    t = fma(rv, por, t);
-    v[q] = fma(-vc, dp * iy2, t);
-    // w
-    conv = fma(wc, dwz, fma(vc, dwy, uc * dwx));
-    lap = fma(lwz, iz2, fma(lwy, iy2, lwx * ix2));
-    por = fma(dwz + dwz, gz, fma(dwy + dvz, gy, (dwx + duz) * gx)) * nu;
-    por = fma(lam * dc, gz, por);
-    t = fma(-dt, conv, wc);
-    t = fma(dtnu, lap, t);
-    t = fma(dtnl, (dT - dB) * hz, t);
-    t = fma(rv, por, t);
-    w[q] = fma(-wc, dp * iz2, t);
-  }
-  // face ghosts of the old fields carry over (the reference's u keeps them)
-  auto keep = [&](long long r) {
-    u[r] = uo[r];
-    v[r] = vo[r];
-    if (DIM == 3) w[r] = wo[r];
-  };
-  if (i == 1) keep(q - 1);
-  if (i == g.m) keep(q + 1);
-  if (j == 1) keep(q - X);
-  if (j == g.n) keep(q + X);
-  if (DIM == 3) {
-    if (k == 1) keep(q - XY);
-    if (k == g.l) keep(q + XY);
-  }
+  c_predictor<T, TS, DIM>(g, s, uo, vo, wo, div, gxa, gya, gza, rinva, dampa, su, sv, sw, u, v, w, i, j, k);
 }
 
 // RHS: bb = density * porosity-weighted divergence of u*, written per colour
@@ -285,22 +149,7 @@ __global__ void k_rhs(Geo g, Scal s, const T* __restrict__ u, const T* __restric
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const long long X = g.X, XY = (long long)g.X * g.Y;
-  const double hx = 0.5 / s.dx, hy = 0.5 / s.dy;
-  double sd = ((double)u[q + 1] - (double)u[q - 1]) * hx;
-  sd = fma((double)v[q + X] - (double)v[q - X], hy, sd);
-  double sg = gxa[q] * (double)u[q];
-  sg = fma(gya[q], (double)v[q], sg);
-  if (DIM == 3) {
-    sd = fma((double)w[q + XY] - (double)w[q - XY], 0.5 / s.dz, sd);
-    sg = fma(gza[q], (double)w[q], sg);
-  }
-  const double bb = s.density * fma(po[q], sd, sg);
-  const int c = colour_of(g, i, j, k);
-  const Coef<double> C = c ? c1 : c0;
-  const long long r = pk_idx(g, i >> 1, j, k);
-  C.bbn[r] = (bb + C.oadd[r]) * C.wap[r];
+  c_rhs<T, DIM>(g, s, u, v, w, po, gxa, gya, gza, c0, c1, i, j, k);
 }
 
 // One red-black half-sweep of colour `colour`, in place:
@@ -318,36 +167,8 @@ __global__ void __launch_bounds__(BX* BY) k_sor_half(Geo g, Coef<T> C, T* __rest
   const int h = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
-  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  const int i = 2 * h + s;
-  unsigned long long e = 0;
-  if (j <= g.n && i >= 1 && i <= g.m) {
-    const long long H = g.H, HY = (long long)g.H * g.Y;
-    const long long q = pk_idx(g, h, j, k);
-    const long long qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
-    const long long qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-    const T pold = pc[q];
-    T t = C.bbn[q];
-    t = fma(-C.a[0][q], po[q + s], t);
-    t = fma(-C.a[1][q], po[q - 1 + s], t);
-    t = fma(-C.a[2][q], po[qn], t);
-    t = fma(-C.a[3][q], po[qs], t);
-    if (DIM == 3) {
-      const long long qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
-      const long long qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
-      t = fma(-C.a[4][q], po[qt], t);
-      t = fma(-C.a[5][q], po[qb], t);
-    }
-    const T pnew = fma(omw, pold, t);
-    pc[q] = pnew;
-    if (TRACK) e = abs_bits(pnew - pold);
-  }
+  const auto e = c_sor_half<T, DIM, TRACK>(g, C, pc, po, omw, colour, h, j, k);
   if (TRACK) block_max_atomic(e, err);
-}
-
-__device__ __forceinline__ long long pk_of(const Geo& g, int i, int j, int k, int& c) {
-  c = colour_of(g, i, j, k);
-  return pk_idx(g, i >> 1, j, k);
 }
 
 // Periodic ghost rows (and planes) of p for interior i, as the reference
@@ -358,31 +179,12 @@ __global__ void k_p_halo(Geo g, T* p0, T* p1, const int* __restrict__ skip) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int a = blockIdx.y + 1;  // k for the y rows (3D), j for the z planes
   if (i > g.m) return;
-  T* P[2] = {p0, p1};
-  int cs, cd;
   if (g.dim == 2) {
-    if (a != 1) return;
-    long long s0 = pk_of(g, i, g.n, 0, cs), d0 = pk_of(g, i, 0, 0, cd);
-    P[cd][d0] = P[cs][s0];
-    s0 = pk_of(g, i, 1, 0, cs);
-    d0 = pk_of(g, i, g.n + 1, 0, cd);
-    P[cd][d0] = P[cs][s0];
-    return;
-  }
-  if (blockIdx.z == 0) {  // y rows, k = a in 1..l
-    if (a > g.l) return;
-    long long s0 = pk_of(g, i, g.n, a, cs), d0 = pk_of(g, i, 0, a, cd);
-    P[cd][d0] = P[cs][s0];
-    s0 = pk_of(g, i, 1, a, cs);
-    d0 = pk_of(g, i, g.n + 1, a, cd);
-    P[cd][d0] = P[cs][s0];
-  } else {  // z planes, j = a in 1..n
-    if (a > g.n) return;
-    long long s0 = pk_of(g, i, a, g.l, cs), d0 = pk_of(g, i, a, 0, cd);
-    P[cd][d0] = P[cs][s0];
-    s0 = pk_of(g, i, a, 1, cs);
-    d0 = pk_of(g, i, a, g.l + 1, cd);
-    P[cd][d0] = P[cs][s0];
+    if (a == 1) c_p_halo_y(g, p0, p1, i, 0);
+  } else if (blockIdx.z == 0) {
+    if (a <= g.l) c_p_halo_y(g, p0, p1, i, a);
+  } else {
+    if (a <= g.n) c_p_halo_z(g, p0, p1, i, a);
   }
 }
 
@@ -394,23 +196,7 @@ __global__ void k_projection(Geo g, Scal s, const double* __restrict__ p0, const
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  const int c = colour_of(g, i, j, k);
-  const double* P = c ? p0 : p1;  // every neighbour has the other colour
-  const long long H = g.H, HY = (long long)g.H * g.Y;
-  const long long r = pk_idx(g, i >> 1, j, k);
-  const int sx = i & 1;
-  const double cdt = s.dt / s.density;
-  u[q] = fma(-(T)(cdt * 0.5 / s.dx), (T)(P[r + sx] - P[r - 1 + sx]), u[q]);
-  v[q] = fma(-(T)(cdt * 0.5 / s.dy), (T)(P[r + H] - P[r - H]), v[q]);
-  if (DIM == 3) w[q] = fma(-(T)(cdt * 0.5 / s.dz), (T)(P[r + HY] - P[r - HY]), w[q]);
-}
-
-template <typename T>
-__device__ __forceinline__ T& pref(const Geo& g, T* p0, T* p1, int i, int j, int k) {
-  int c;
-  long long r = pk_of(g, i, j, k, c);
-  return c ? p1[r] : p0[r];
+  c_projection<T, DIM>(g, s, p0, p1, u, v, w, i, j, k);
 }
 
 // boundary, x faces: inflow at i=1 and its ghost, outflow copy at m+1.
@@ -418,60 +204,21 @@ template <typename T>
 __global__ void k_bnd_x(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int k = (g.dim == 3) ? blockIdx.y + 1 : 0;
-  if (j > g.n) return;
-  const long long q1 = nat_idx(g, 1, j, k), q0 = q1 - 1;
-  u[q1] = (T)s.inlet_u;
-  v[q1] = (T)s.inlet_v;
-  u[q0] = u[q1];
-  v[q0] = v[q1];
-  if (g.dim == 3) {
-    w[q1] = (T)0;
-    w[q0] = w[q1];
-  }
-  pref(g, p0, p1, 0, j, k) = pref(g, p0, p1, 2, j, k);
-  const long long qm = nat_idx(g, g.m + 1, j, k);
-  u[qm] = u[qm - 2];
-  v[qm] = v[qm - 2];
-  if (g.dim == 3) w[qm] = w[qm - 2];
-  pref(g, p0, p1, g.m + 1, j, k) = s.outlet_pressure;
+  if (j <= g.n) c_bnd_x(g, s, u, v, w, p0, p1, j, k);
 }
 
 // boundary, y faces: periodic ghost rows over i = 0..m+1 (and k = 0..l+1).
 template <typename T>
 __global__ void k_bnd_y(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;  // 0 in 2D, 0..l+1 in 3D
-  if (i > g.m + 1) return;
-  const long long a = nat_idx(g, i, 0, k), b = nat_idx(g, i, g.n, k);
-  const long long c = nat_idx(g, i, g.n + 1, k), d = nat_idx(g, i, 1, k);
-  u[a] = u[b];
-  v[a] = v[b];
-  u[c] = u[d];
-  v[c] = v[d];
-  if (g.dim == 3) {
-    w[a] = w[b];
-    w[c] = w[d];
-  }
-  pref(g, p0, p1, i, 0, k) = pref(g, p0, p1, i, g.n, k);
-  pref(g, p0, p1, i, g.n + 1, k) = pref(g, p0, p1, i, 1, k);
+  if (i <= g.m + 1) c_bnd_y(g, u, v, w, p0, p1, i, blockIdx.y);  // k = 0 in 2D, 0..l+1 in 3D
 }
 
 // boundary, z faces (3D): periodic ghost planes over i = 0..m+1, j = 0..n+1.
 template <typename T>
 __global__ void k_bnd_z(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i > g.m + 1) return;
-  const long long a = nat_idx(g, i, j, 0), b = nat_idx(g, i, j, g.l);
-  const long long c = nat_idx(g, i, j, g.l + 1), d = nat_idx(g, i, j, 1);
-  u[a] = u[b];
-  v[a] = v[b];
-  w[a] = w[b];
-  u[c] = u[d];
-  v[c] = v[d];
-  w[c] = w[d];
-  pref(g, p0, p1, i, j, 0) = pref(g, p0, p1, i, j, g.l);
-  pref(g, p0, p1, i, j, g.l + 1) = pref(g, p0, p1, i, j, 1);
+  if (i <= g.m + 1) c_bnd_z(g, u, v, w, p0, p1, i, blockIdx.y);
 }
 
 template <typename T>
@@ -480,11 +227,7 @@ __global__ void k_initial(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
   if (i > g.m || j > g.n) return;
-  const long long q = nat_idx(g, i, j, k);
-  u[q] = (T)s.init_u;
-  v[q] = (T)s.init_v;
-  if (g.dim == 3) w[q] = (T)0;
-  pref(g, p0, p1, i, j, k) = s.outlet_pressure;
+  c_initial<T>(g, s, u, v, w, p0, p1, i, j, k);
 }
 
 // max |porosity-weighted divergence| of the current fields.
@@ -498,8 +241,8 @@ __global__ void k_div_diag(Geo g, Scal s, const T* __restrict__ u, const T* __re
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
   unsigned long long e = 0;
   if (i <= g.m && j <= g.n) {
-    const long long q = nat_idx(g, i, j, k);
-    const long long X = g.X, XY = (long long)g.X * g.Y;
+    const idx_t q = nat_idx(g, i, j, k);
+    const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
     double sd = ((double)u[q + 1] - (double)u[q - 1]) * (0.5 / s.dx);
     sd = fma((double)v[q + X] - (double)v[q - X], 0.5 / s.dy, sd);
     double sg = gxa[q] * (double)u[q];
@@ -519,7 +262,7 @@ __global__ void k_scatter_nat(Geo g, const double* __restrict__ st, double* __re
   const int j = blockIdx.y * BY + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.m + 1 || j > g.n + 1) return;
-  const long long d = (long long)i + (long long)(g.m + 2) * ((long long)j + (long long)(g.n + 2) * k);
+  const idx_t d = (idx_t)i + (idx_t)(g.m + 2) * ((idx_t)j + (idx_t)(g.n + 2) * k);
   dst[nat_idx(g, i, j, k)] = st[d];
 }
 __global__ void k_scatter_pk(Geo g, const double* __restrict__ st, double* p0, double* p1) {
@@ -527,7 +270,7 @@ __global__ void k_scatter_pk(Geo g, const double* __restrict__ st, double* p0, d
   const int j = blockIdx.y * BY + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.m + 1 || j > g.n + 1) return;
-  const long long d = (long long)i + (long long)(g.m + 2) * ((long long)j + (long long)(g.n + 2) * k);
+  const idx_t d = (idx_t)i + (idx_t)(g.m + 2) * ((idx_t)j + (idx_t)(g.n + 2) * k);
   pref(g, p0, p1, i, j, k) = st[d];
 }
 __global__ void k_gather_pk(Geo g, const double* p0, const double* p1, double* __restrict__ st) {
@@ -535,9 +278,9 @@ __global__ void k_gather_pk(Geo g, const double* p0, const double* p1, double* _
   const int j = blockIdx.y * BY + threadIdx.y;
   const int k = blockIdx.z;
   if (i > g.m + 1 || j > g.n + 1) return;
-  const long long d = (long long)i + (long long)(g.m + 2) * ((long long)j + (long long)(g.n + 2) * k);
+  const idx_t d = (idx_t)i + (idx_t)(g.m + 2) * ((idx_t)j + (idx_t)(g.n + 2) * k);
   int c;
-  const long long r = pk_of(g, i, j, k, c);
+  const idx_t r = pk_of(g, i, j, k, c);
   st[d] = c ? p1[r] : p0[r];
 }
 
@@ -564,45 +307,12 @@ __global__ void __launch_bounds__(BX* BY) k_residual(Geo g, Coef<double> C, cons
   const int h = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
-  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  const int i = 2 * h + s;
-  unsigned long long e = 0;
-  if (j <= g.n && i >= 1 && i <= g.m) {
-    const long long H = g.H, HY = (long long)g.H * g.Y;
-    const long long q = pk_idx(g, h, j, k);
-    const long long qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
-    const long long qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-    double t = C.bbn[q];
-    t = fma(-C.a[0][q], po[q + s], t);
-    t = fma(-C.a[1][q], po[q - 1 + s], t);
-    t = fma(-C.a[2][q], po[qn], t);
-    t = fma(-C.a[3][q], po[qs], t);
-    if (DIM == 3) {
-      const long long qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
-      const long long qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
-      t = fma(-C.a[4][q], po[qt], t);
-      t = fma(-C.a[5][q], po[qb], t);
-    }
-    t = fma(-omega, pc[q], t);
-    rf[q] = (float)t;
-    ec[q] = 0.0f;
-    e = abs_bits(t);
-  }
-  block_max_atomic(e, rmax);
+  block_max_atomic(c_residual<DIM>(g, C, pc, po, omega, colour, rf, ec, h, j, k), rmax);
 }
 
-// FP32 correction sweep with the operator rebuilt on the fly from the FP32
-// porosity (packed by colour, ghosts included), so a half-sweep streams only
-// porosity, r and e (24 bytes per update) instead of six stored
-// coefficients.  Same operator as k_setup_coef up to FP32 rounding:
-//   a_f = dt/h^2 * max(small, (eps_a+eps_b)/2), ap = -sum a_f (before the
-//   inlet/outlet edits), inlet: a_e += a_w, a_w = 0; outlet: all a_f = 0,
-//   e = (1-w) e + r - (w/ap) sum a_f e_f.
-struct DCConst {
-  float kx, ky, kz;  // dt/dx^2 etc.
-  float small, omega, omw;
-};
-
+// FP32 correction sweep, two rows per thread (j and j+BY) so each thread
+// keeps two independent updates' loads in flight (the kernel is latency
+// bound, not ALU bound).
 template <int DIM, bool TRACK>
 __global__ void __launch_bounds__(BX* BY) k_sor_dc(Geo g, DCConst K, const float* __restrict__ epsc,
                                                    const float* __restrict__ epso, const float* __restrict__ r,
@@ -610,49 +320,25 @@ __global__ void __launch_bounds__(BX* BY) k_sor_dc(Geo g, DCConst K, const float
                                                    unsigned long long* __restrict__ err, const int* __restrict__ skip) {
   if (skip && *skip) return;
   const int h = blockIdx.x * BX + threadIdx.x;
-  const int j = blockIdx.y * BY + threadIdx.y + 1;
+  const int jb = blockIdx.y * (2 * BY) + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
-  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  const int i = 2 * h + s;
-  unsigned long long e = 0;
-  if (j <= g.n && i >= 1 && i <= g.m) {
-    const long long H = g.H, HY = (long long)g.H * g.Y;
-    const long long q = pk_idx(g, h, j, k);
-    const long long qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
-    const long long qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-    const float pc = epsc[q];
-    float ae = K.kx * fmaxf(K.small, (epso[q + s] + pc) * 0.5f);
-    float aw = K.kx * fmaxf(K.small, (pc + epso[q - 1 + s]) * 0.5f);
-    const float an = K.ky * fmaxf(K.small, (epso[q + H] + pc) * 0.5f);
-    const float as = K.ky * fmaxf(K.small, (pc + epso[q - H]) * 0.5f);
-    float at = 0.f, ab = 0.f;
-    if (DIM == 3) {
-      at = K.kz * fmaxf(K.small, (epso[q + HY] + pc) * 0.5f);
-      ab = K.kz * fmaxf(K.small, (pc + epso[q - HY]) * 0.5f);
+  unsigned e = 0;
+  float eold[2], enew[2];
+  bool ok[2];
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const int j = jb + u * BY;
+    const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+    const int i = 2 * h + s;
+    ok[u] = (j <= g.n && i >= 1 && i <= g.m);
+    if (ok[u]) dc_update<DIM>(g, K, epsc, epso, r, ec, eo, h, j, k, s, i, eold[u], enew[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    if (ok[u]) {
+      ec[pk_idx(g, h, jb + u * BY, k)] = enew[u];
+      if (TRACK) e = max(e, abs_bits(enew[u] - eold[u]));
     }
-    const float ap = -ae - aw - an - as - at - ab;
-    const float wap = K.omega / ap;
-    const float eold = ec[q];
-    float enew = fmaf(K.omw, eold, r[q]);
-    if (i != g.m) {
-      if (i == 1) {
-        ae += aw;
-        aw = 0.f;
-      }
-      float t = ae * eo[q + s];
-      t = fmaf(aw, eo[q - 1 + s], t);
-      t = fmaf(an, eo[qn], t);
-      t = fmaf(as, eo[qs], t);
-      if (DIM == 3) {
-        const long long qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
-        const long long qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
-        t = fmaf(at, eo[qt], t);
-        t = fmaf(ab, eo[qb], t);
-      }
-      enew = fmaf(-wap, t, enew);
-    }
-    ec[q] = enew;
-    if (TRACK) e = abs_bits(enew - eold);
   }
   if (TRACK) block_max_atomic(e, err);
 }
@@ -664,7 +350,7 @@ __global__ void k_pack_eps(Geo g, const double* __restrict__ po, float* e0, floa
   const int k = blockIdx.z;
   if (i > g.m + 1 || j > g.n + 1) return;
   int c;
-  const long long r = pk_of(g, i, j, k, c);
+  const idx_t r = pk_of(g, i, j, k, c);
   (c ? e1 : e0)[r] = (float)po[nat_idx(g, i, j, k)];
 }
 
@@ -677,26 +363,13 @@ __global__ void k_accumulate(Geo g, double* __restrict__ p0, double* __restrict_
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int colour = blockIdx.z & 1;
   const int k = (DIM == 3) ? (blockIdx.z >> 1) + 1 : 0;
-  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  const int i = 2 * h + s;
-  if (j > g.n || i < 1 || i > g.m) return;
-  const long long q = pk_idx(g, h, j, k);
-  if (colour)
-    p1[q] += (double)e1[q];
-  else
-    p0[q] += (double)e0[q];
+  c_accumulate<DIM>(g, colour ? p1 : p0, colour ? e1 : e0, colour, h, j, k);
 }
 
 // Stop the remaining passes of this step once max|r|/w <= tol.
 __global__ void k_dc_check(const unsigned long long* rmax, double tol_w, int* skip) {
-  const double r = __longlong_as_double((long long)*rmax);
+  const double r = __longlong_as_double((long long)max_of_slots(rmax));
   if (r <= tol_w) *skip = 1;
-}
-
-__global__ void k_coef_to_float(long long n, Coef<double> c, Coef<float> cf, int nd) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  for (int d = 0; d < nd; d++) cf.a[d][q] = (float)c.a[d][q];
 }
 
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long long n) {
@@ -727,17 +400,26 @@ void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, 
   k_divergence<TV><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div);
 }
 
-template <typename TV>
-void launch_predictor(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, const TV* div,
-                      const TV* gx, const TV* gy, const TV* gz, const TV* rinv, const TV* damp, TV* u, TV* v,
-                      TV* w, cudaStream_t st) {
+template <typename T, typename TS>
+void launch_predictor(const Geo& g, const Scal& s, const T* uo, const T* vo, const T* wo, const T* div,
+                      const T* gx, const T* gy, const T* gz, const T* rinv, const T* damp, const TS* us,
+                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st) {
   if (g.dim == 3)
-    k_predictor<TV, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
-                                                                  damp, u, v, w);
+    k_predictor<T, TS, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
+                                                                     damp, us, vs, ws, u, v, w);
   else
-    k_predictor<TV, 2><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
-                                                                  damp, u, v, w);
+    k_predictor<T, TS, 2><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
+                                                                     damp, us, vs, ws, u, v, w);
 }
+template void launch_predictor<double, double>(const Geo&, const Scal&, const double*, const double*,
+                                               const double*, const double*, const double*, const double*,
+                                               const double*, const double*, const double*, const double*,
+                                               const double*, const double*, double*, double*, double*,
+                                               cudaStream_t);
+template void launch_predictor<float, double>(const Geo&, const Scal&, const float*, const float*, const float*,
+                                              const float*, const float*, const float*, const float*,
+                                              const float*, const float*, const double*, const double*,
+                                              const double*, double*, double*, double*, cudaStream_t);
 
 template <typename TV>
 void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
@@ -825,7 +507,8 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
   K.small = 1.e-6f;
   K.omega = (float)sc.omega;
   K.omw = (float)(1.0 - sc.omega);
-  const dim3 grid = grid_packed(g);
+  dim3 grid = grid_packed(g);
+  grid.y = (g.n + 2 * BY - 1) / (2 * BY);
   if (g.dim == 3) {
     if (err)
       k_sor_dc<3, true><<<grid, dim3(BX, BY), 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, err, skip);
@@ -857,11 +540,6 @@ void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cuda
   k_dc_check<<<1, 1, 0, st>>>(rmax, tol, skip);
 }
 
-void launch_coef_to_float(const Geo& g, const Coef<double>& c, Coef<float> cf, cudaStream_t st) {
-  const long long n = g.pk;
-  k_coef_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, c, cf, 2 * g.dim);
-}
-
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st) {
   k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);
 }
@@ -883,9 +561,6 @@ void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* 
 #define PF_INST_V(TV)                                                                                        \
   template void launch_divergence<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, TV*,         \
                                       cudaStream_t);                                                         \
-  template void launch_predictor<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, const TV*,    \
-                                     const TV*, const TV*, const TV*, const TV*, const TV*, TV*, TV*, TV*,  \
-                                     cudaStream_t);                                                         \
   template void launch_rhs<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, const double*,      \
                                const double*, const double*, const double*, Coef<double>, Coef<double>,     \
                                cudaStream_t);                                                                \

@@ -1,18 +1,19 @@
-// pf_mixed.cu -- the precision form of the step: FP32 velocity stencils and
-// FP32 red-black sweeps inside an FP64 defect-correction loop.
+// pf_mixed.cu -- the precision form of the step: FP32 stencils and FP32
+// red-black sweeps inside an FP64 defect-correction loop.
 //
-// FP64 stays in: the pressure p and its accumulation p += e, the Poisson
-// residual r (normalised by omega/ap), the RHS bb, and every norm.  FP32:
-// the velocities and their stencils (divergence, predictor, projection,
-// boundary), the operator copy used by the sweeps, and the correction e.
+// FP64: the velocity and pressure state, the accumulations into it (u_old +
+// predictor increment, p += e, the projection), the RHS bb, the Poisson
+// residual r (normalised by omega/ap) and every norm.
+// FP32: the velocity stencils (divergence, the predictor's increment, read
+// from an FP32 copy of the state), and the correction sweeps on e, whose
+// operator is rebuilt on the fly from FP32 porosity (k_sor_dc, 24 bytes per
+// update).
 // Per step: outer_max passes of { r = bbn - w p - sum a p_nb (FP64);
 // inner_sweeps FP32 SOR iterations on e from e = 0; p += e (FP64) }.
-// The FP32 sweeps rebuild their operator on the fly from FP32 porosity
-// (k_sor_dc), so they stream 24 bytes per cell update.
-// With outer_max * inner_sweeps == iter_max the pass structure reproduces
-// the plain SOR's iterates up to the FP32 rounding of e; dc_tol > 0 ends
-// the passes of a step early once max|r|/omega <= dc_tol (a device flag, so
-// the step stays one graph).
+// With outer_max * inner_sweeps == iter_max the passes reproduce the plain
+// SOR's iterates up to the FP32 rounding of e (stationary iteration on the
+// residual equation); dc_tol > 0 ends the passes of a step early once
+// max|r|/omega <= dc_tol (a device flag, so the step stays one graph).
 #include <cuda_runtime.h>
 
 #include "pf_case.cuh"
@@ -30,11 +31,9 @@ int mixed_alloc(pf_case* c) {
   };
   Req req[32];
   int nr = 0;
-  for (int b = 0; b < 2; b++) {
-    req[nr++] = {&c->Uf[b], nat};
-    req[nr++] = {&c->Vf[b], nat};
-    req[nr++] = {&c->Wf[b], three ? nat : 0};
-  }
+  req[nr++] = {&c->Uf[0], nat};
+  req[nr++] = {&c->Vf[0], nat};
+  req[nr++] = {&c->Wf[0], three ? nat : 0};
   req[nr++] = {&c->divf, nat};
   req[nr++] = {&c->gxf, nat};
   req[nr++] = {&c->gyf, nat};
@@ -78,23 +77,17 @@ void mixed_setup(pf_case* c) {
   launch_pack_eps(c->g, c->poro, c->epsf[0], c->epsf[1], c->st);
 }
 
+// FP32 copy of the current FP64 velocity state, read by the stencils.
 void mixed_sync_from_fp64(pf_case* c) {
   const int b = c->cur;
-  c->launches += c->g.dim;
   const long long n = c->g.nat;
-  launch_to_float(c->U[b], c->Uf[b], n, c->st);
-  launch_to_float(c->V[b], c->Vf[b], n, c->st);
-  if (c->g.dim == 3) launch_to_float(c->W[b], c->Wf[b], n, c->st);
+  launch_to_float(c->U[b], c->Uf[0], n, c->st);
+  launch_to_float(c->V[b], c->Vf[0], n, c->st);
+  if (c->g.dim == 3) launch_to_float(c->W[b], c->Wf[0], n, c->st);
+  c->launches += c->g.dim;
 }
 
-void mixed_sync_to_fp64(pf_case* c) {
-  const int b = c->cur;
-  c->launches += c->g.dim;
-  const long long n = c->g.nat;
-  launch_to_double(c->Uf[b], c->U[b], n, c->st);
-  launch_to_double(c->Vf[b], c->V[b], n, c->st);
-  if (c->g.dim == 3) launch_to_double(c->Wf[b], c->W[b], n, c->st);
-}
+void mixed_sync_to_fp64(pf_case*) {}  // the state is FP64 already
 
 void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   const Geo& g = c->g;
@@ -104,24 +97,24 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   const bool track = c->opt.track_sor_error != 0;
   const bool early = c->opt.dc_tol > 0.0;
   const int* skip = early ? c->skip : nullptr;
-  if (track) cudaMemsetAsync(&c->red[0], 0, sizeof(unsigned long long), st);
+  if (track) cudaMemsetAsync(&c->red[RED_ERRF], 0, RED_SLOTS * sizeof(unsigned long long), st);
   if (early) cudaMemsetAsync(c->skip, 0, sizeof(int), st);
-  launch_divergence<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, st);
-  launch_predictor<float>(g, s, c->Uf[o], c->Vf[o], c->Wf[o], c->divf, c->gxf, c->gyf, c->gzf, c->rinvf,
-                          c->dampf, c->Uf[nw], c->Vf[nw], c->Wf[nw], st);
-  launch_rhs<float>(g, s, c->Uf[nw], c->Vf[nw], c->Wf[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
+  launch_divergence<float>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, st);
+  launch_predictor<float, double>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, c->gxf, c->gyf, c->gzf, c->rinvf,
+                                  c->dampf, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
+  launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
-    cudaMemsetAsync(&c->red[2], 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(&c->red[RED_RMAX], 0, RED_SLOTS * sizeof(unsigned long long), st);
     for (int col = 0; col < 2; col++)
-      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col], &c->red[2],
-                      skip, st);
-    if (early) launch_dc_check(&c->red[2], c->opt.dc_tol * s.omega, c->skip, st);
+      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col],
+                      &c->red[RED_RMAX], skip, st);
+    if (early) launch_dc_check(&c->red[RED_RMAX], c->opt.dc_tol * s.omega, c->skip, st);
     for (int it = 0; it < c->opt.inner_sweeps; it++) {
       for (int col = 0; col < 2; col++) {
         if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
-        unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[0] : nullptr;
+        unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
         launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err, skip,
                       st);
       }
@@ -139,13 +132,14 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
 void enqueue_projection_mixed(pf_case* c) {
   const int b = c->cur;
   c->launches += 1;
-  launch_projection<float>(c->g, c->s, c->p[0], c->p[1], c->Uf[b], c->Vf[b], c->Wf[b], c->st);
+  launch_projection<double>(c->g, c->s, c->p[0], c->p[1], c->U[b], c->V[b], c->W[b], c->st);
 }
 
 void enqueue_boundary_mixed(pf_case* c) {
   const int b = c->cur;
   c->launches += c->g.dim == 3 ? 3 : 2;
-  launch_boundary<float>(c->g, c->s, c->Uf[b], c->Vf[b], c->Wf[b], c->p[0], c->p[1], c->st);
+  launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
+  mixed_sync_from_fp64(c);
 }
 
 }  // namespace pf

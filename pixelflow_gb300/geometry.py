@@ -177,3 +177,87 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
                      precision="mixed")
         cases.append(BatchCase2D(m, n, s, shapes))
     return cases
+
+
+# --------------------------------------------------------------------------
+# Shape lists for the GPU geometry generator (pf_create_shapes).
+# --------------------------------------------------------------------------
+
+def to_pf_shapes(shapes, dim: int):
+    """Shapes as pf_shape structs: 2D (cx, cy, a, b, angle) tuples -> circles
+    or ellipses; 3D (cx, cy, cz, r) rows -> spheres."""
+    from ._lib import PF_SHAPE_CIRCLE, PF_SHAPE_ELLIPSE, PF_SHAPE_SPHERE, PfShape
+    out = []
+    for sh in shapes:
+        if dim == 2:
+            cx, cy, a, b, ang = sh
+            kind = PF_SHAPE_CIRCLE if a == b else PF_SHAPE_ELLIPSE
+            out.append(PfShape(kind, 0, float(cx), float(cy), 0.0, float(a), float(b), float(ang)))
+        else:
+            cx, cy, cz, r = sh
+            out.append(PfShape(PF_SHAPE_SPHERE, 0, float(cx), float(cy), float(cz), float(r), float(r), 0.0))
+    return out
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival_s: float
+    dim: int
+    shape: Tuple[int, ...]
+    settings: Settings
+    shapes: list
+    steps: int
+
+    @property
+    def cells(self) -> int:
+        c = 1
+        for x in self.shape:
+            c *= x
+        return c
+
+
+def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2d: float = 0.7,
+                     sizes_2d: Sequence[int] = tuple(range(128, 1025, 32)),
+                     sizes_3d: Sequence[int] = (64, 96, 128, 160, 192),
+                     steps_range: Tuple[int, int] = (100, 1000)) -> List[Request]:
+    """Poisson arrivals (exponential gaps, mean 1/rate) of mixed cases.
+    2D: n x n grids, 1-4 circles/ellipses (semi-axes 0.02-0.1), Re 50-400,
+    dt = 0.2 dx.  3D: n^3 unit cubes, 4-16 spheres (radii 0.03-0.08, centres
+    in [0.15, 0.85]^3), nu 2e-3..1e-2, dt = min(0.2 dx, 0.1 dx^2/nu).
+    Steps per request uniform in steps_range."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        if rng.random() < frac_2d:
+            n = int(rng.choice(sizes_2d))
+            h = 1.0 / (n - 1)
+            nobs = int(rng.integers(1, 5))
+            shapes = []
+            for _o in range(nobs):
+                a = float(rng.uniform(0.02, 0.1))
+                b = a if bool(rng.integers(0, 2)) else float(rng.uniform(0.02, 0.1))
+                shapes.append((float(rng.uniform(0.2, 0.8)), float(rng.uniform(0.2, 0.8)), a, b,
+                               float(rng.uniform(0.0, np.pi))))
+            re = float(rng.uniform(50.0, 400.0))
+            nu = 2.0 * max(shapes[0][2], shapes[0][3]) / re
+            dt = 0.2 * h
+            s = Settings(xnue=nu, width=1.0, height=1.0, depth=0.0, time=dt * steps, inlet_velocity=1.0,
+                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
+                         iter_max=100, relux_factor=1.7, precision="mixed")
+            out.append(Request(rid, t, 2, (n, n), s, shapes, steps))
+        else:
+            n = int(rng.choice(sizes_3d))
+            h = 1.0 / (n - 1)
+            ns = int(rng.integers(4, 17))
+            sph = random_spheres(ns, seed=int(rng.integers(0, 2 ** 31)))
+            nu = float(rng.uniform(2e-3, 1e-2))
+            dt = min(0.2 * h, 0.1 * h * h / nu)
+            s = Settings(xnue=nu, width=1.0, height=1.0, depth=1.0, time=dt * steps, inlet_velocity=1.0,
+                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
+                         iter_max=100, relux_factor=1.7, precision="mixed")
+            out.append(Request(rid, t, 3, (n, n, n), s, [tuple(r) for r in sph], steps))
+    return out

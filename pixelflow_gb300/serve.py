@@ -1,0 +1,127 @@
+"""The serving form: a request loop with continuous batching on one GPU.
+
+Requests (a geometry, grid, physics and a step count) arrive over time.  The
+loop keeps every admitted case's fields resident in HBM inside one `Batch`;
+a request is admitted as soon as its memory fits the HBM budget (and a slot
+is free), in arrival order.  Each round advances every active case by up to
+`chunk` steps in one persistent launch per dimension, so requests that arrive
+while others are running join at the next round and their work overlaps on
+the device with the cases already there.  A finished case's result (its
+fields and norms) is read back, its slot and memory freed, and its latency
+(completion minus arrival) recorded.
+
+Each case's arithmetic is independent of what else is in the batch, so a
+result is the same alone and in any mix (bit for bit; tests/test_gpu_serve.py).
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+from collections import deque
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from ._lib import PfError
+from .batch import GIB, Batch, case_bytes
+from .geometry import Request, to_pf_shapes
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    arrival_s: float
+    admitted_s: float
+    done_s: float
+    cells: int
+    steps: int
+    max_div: float
+    sor_error: float
+    state: Optional[Dict[str, np.ndarray]] = None
+
+    @property
+    def latency_s(self) -> float:
+        return self.done_s - self.arrival_s
+
+
+class Server:
+    def __init__(self, hbm_budget_bytes: int = 150 * GIB, chunk: int = 25, cluster: int = 4, threads: int = 512,
+                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0):
+        self.batch = Batch(cluster=cluster, threads=threads, max_cases=max_cases,
+                           hbm_budget_bytes=hbm_budget_bytes)
+        self.chunk = chunk
+        self.keep_state = keep_state
+        self.edge = edge
+        self.peak_bytes = 0
+        self.rounds = 0
+        self.device_ms = 0.0
+
+    def close(self):
+        self.batch.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def run(self, requests: List[Request], realtime: bool = True) -> List[Result]:
+        """Serve `requests` (sorted by arrival).  With realtime=True arrivals
+        follow the wall clock from the start of the call; otherwise every
+        request is available at once (a closed batch)."""
+        reqs = sorted(requests, key=lambda r: r.arrival_s)
+        for r in reqs:
+            need = case_bytes(r.settings, r.shape)
+            if need > self.batch.memory()[1]:
+                raise ValueError(f"request {r.rid} needs {need} bytes, more than the whole budget")
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        incoming = deque(reqs)
+        waiting: deque = deque()
+        active: Dict[int, dict] = {}
+        results: List[Result] = []
+        while incoming or waiting or active:
+            t = now()
+            while incoming and (not realtime or incoming[0].arrival_s <= t):
+                waiting.append(incoming.popleft())
+            # admission in arrival order while memory and slots allow
+            while waiting:
+                r = waiting[0]
+                try:
+                    slot = self.batch.add_shapes(r.settings, r.shape, to_pf_shapes(r.shapes, r.dim), self.edge)
+                except PfError as e:
+                    if e.code in (-3, -7):  # over budget / no slot: wait for a case to finish
+                        break
+                    raise
+                waiting.popleft()
+                active[slot] = {"req": r, "left": r.steps, "admitted": now()}
+                self.peak_bytes = max(self.peak_bytes, self.batch.memory()[0])
+            if not active:
+                if incoming and realtime:
+                    time.sleep(max(0.0, min(0.005, incoming[0].arrival_s - now())))
+                continue
+            slots = list(active)
+            steps = [min(self.chunk, active[s]["left"]) for s in slots]
+            self.batch.step_slots(slots, steps)
+            self.rounds += 1
+            self.device_ms += self.batch.last_ms()
+            for s, k in zip(slots, steps):
+                a = active[s]
+                a["left"] -= k
+                if a["left"] == 0:
+                    md, se = self.batch.norms(s)
+                    st = self.batch.get_state(s) if self.keep_state else None
+                    r = a["req"]
+                    results.append(Result(r.rid, r.arrival_s, a["admitted"], now(), r.cells, r.steps, md, se, st))
+                    self.batch.remove(s)
+                    del active[s]
+        return sorted(results, key=lambda x: x.rid)
+
+
+def summarize(results: List[Result], wall_s: float) -> dict:
+    lat = np.array([r.latency_s for r in results])
+    cell_steps = sum(r.cells * r.steps for r in results)
+    return {"requests": len(results), "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+            "wall_s": wall_s, "cell_steps": cell_steps, "mcell_steps_per_s": cell_steps / wall_s / 1e6,
+            "nonfinite_results": int(sum(1 for r in results if not np.isfinite(r.max_div)))}

@@ -79,6 +79,30 @@ class Case:
         self.field_shape = (self.n + 2, self.m + 2) if self.dim == 2 else (self.l + 2, self.n + 2, self.m + 2)
 
     @classmethod
+    def from_shapes(cls, settings: Settings, shape: Sequence[int], shapes, edge: float = 1.0,
+                    use_graph: bool = True) -> "Case":
+        """A case whose porosity is generated on the GPU from analytic shapes."""
+        from ._lib import PfShape
+        from .geometry import to_pf_shapes
+        self = cls.__new__(cls)
+        self.L = _lib.load()
+        self.settings = settings
+        self.shape = tuple(int(x) for x in shape)
+        self.dim = len(self.shape)
+        self.m, self.n = self.shape[0], self.shape[1]
+        self.l = self.shape[2] if self.dim == 3 else 1
+        self.params = make_params(settings, self.shape)
+        self.options = make_options(settings, use_graph)
+        pfs = shapes if (shapes and isinstance(shapes[0], PfShape)) else to_pf_shapes(shapes, self.dim)
+        arr = (PfShape * max(1, len(pfs)))(*pfs)
+        h = ctypes.c_void_p()
+        check(self.L.pf_create_shapes(ctypes.byref(self.params), ctypes.byref(self.options),
+                                      ctypes.cast(arr, ctypes.c_void_p), len(pfs), float(edge), ctypes.byref(h)))
+        self.h = h
+        self.field_shape = (self.n + 2, self.m + 2) if self.dim == 2 else (self.l + 2, self.n + 2, self.m + 2)
+        return self
+
+    @classmethod
     def from_project(cls, project_dir: str, **kw) -> "Case":
         """Open a reference project directory: config/controlDict.txt + its porosity CSV."""
         s = read_settings(os.path.join(project_dir, "config", "controlDict.txt"))

@@ -1,0 +1,95 @@
+"""The batched form: a persistent kernel advancing many cases of uneven size.
+
+Every stage of a batched case uses the same per-cell code as the single-case
+precision form, so a case must give bit-identical fields alone, in a batch,
+in a different mix, order or launch shape."""
+import numpy as np
+import pytest
+
+from pixelflow_gb300 import geometry as G
+from pixelflow_gb300._lib import PfError
+from pixelflow_gb300.batch import Batch, case_bytes
+from pixelflow_gb300.solver import Case
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    out = []
+    s2 = G.settings_cylinder_2d(iter_max=20, inner_sweeps=5, outer_max=4)
+    out.append((s2, (64, 40), G.cylinder_2d(64, 40, radius=0.15, cx=0.6, cy=0.5)))
+    out.append((s2, (48, 32), G.cylinder_2d(48, 32, radius=0.2, cx=0.7, cy=0.4)))
+    out.append((s2, (33, 17), G.cylinder_2d(33, 17, radius=0.2, cx=0.7, cy=0.5)))  # odd sizes: halo path
+    s3 = G.settings_spheres_3d(iter_max=12, inner_sweeps=3, outer_max=4)
+    out.append((s3, (20, 16, 12), G.spheres_3d(20, 16, 12, count=3, seed=4)))
+    out.append((s3, (17, 15, 13), G.spheres_3d(17, 15, 13, count=2, seed=5)))
+    return out
+
+
+def _single(s, shape, vals, steps):
+    with Case(s.replace(precision="mixed"), shape, vals) as c:
+        c.initial_conditions()
+        c.step(steps)
+        return c.get_state(), c.norms()
+
+
+def _same(a, b):
+    return all(np.array_equal(a[k], b[k], equal_nan=True) for k in a)
+
+
+@pytest.mark.parametrize("cluster,threads", [(4, 512), (1, 256), (2, 1024)])
+def test_batch_matches_single_cases_bitwise(cluster, threads):
+    cases = _cases()
+    steps = 4
+    ref = [_single(s, shape, vals, steps) for (s, shape, vals) in cases]
+    with Batch(cluster=cluster, threads=threads) as b:
+        slots = [b.add(s, shape, vals) for (s, shape, vals) in cases]
+        b.step(steps)
+        for k, sl in enumerate(slots):
+            got = b.get_state(sl)
+            assert _same(got, ref[k][0]), (k, cases[k][1])
+            assert np.array_equal(np.array(b.norms(sl)), np.array(ref[k][1]), equal_nan=True)
+
+
+def test_batch_uneven_steps_and_mix_order():
+    """Per-case step counts in one launch, cases added in another order and
+    advanced in two launches: each still equals its single-case run."""
+    cases = _cases()
+    want_steps = [3, 5, 0, 2, 4]
+    ref = [_single(s, shape, vals, n) for (s, shape, vals), n in zip(cases, want_steps)]
+    with Batch(cluster=2, threads=512) as b:
+        order = [4, 2, 0, 3, 1]
+        slots = {k: b.add(*cases[k]) for k in order}
+        first = [min(2, n) for n in want_steps]
+        b.step_slots([slots[k] for k in range(5)], first)
+        b.step_slots([slots[k] for k in range(5)], [n - f for n, f in zip(want_steps, first)])
+        for k in range(5):
+            assert _same(b.get_state(slots[k]), ref[k][0]), k
+
+
+def test_batch_admission_by_budget_and_slot_reuse():
+    s, shape, vals = _cases()[0]
+    need = case_bytes(s, shape)
+    with Batch(hbm_budget_bytes=int(need * 1.5), max_cases=4) as b:
+        a = b.add(s, shape, vals)
+        with pytest.raises(PfError) as ei:
+            b.add(s, shape, vals)
+        assert ei.value.code == -3  # PF_E_NOMEM: admitted only once memory frees up
+        used, budget = b.memory()
+        assert 0 < used <= budget
+        b.remove(a)
+        c = b.add(s, shape, vals)
+        b.step(2)
+        got = b.get_state(c)
+    ref = _single(s, shape, vals, 2)[0]
+    assert _same(got, ref)
+
+
+def test_batch_launch_is_persistent_one_per_dimension():
+    cases = _cases()
+    with Batch() as b:
+        for c in cases:
+            b.add(*c)
+        n0 = b.kernel_launches()
+        b.step(3)
+        assert b.kernel_launches() - n0 == 2  # one 2D launch + one 3D launch for 3 steps of 5 cases

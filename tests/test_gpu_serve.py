@@ -1,0 +1,54 @@
+"""The serving form: requests admitted by HBM budget into one resident batch,
+advanced together, each result identical (bit for bit) to running the case
+alone."""
+import numpy as np
+import pytest
+
+from pixelflow_gb300 import geometry as G
+from pixelflow_gb300.batch import case_bytes
+from pixelflow_gb300.serve import Server, summarize
+from pixelflow_gb300.solver import Case
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_requests():
+    reqs = G.serving_requests(count=8, rate=400.0, seed=3, sizes_2d=(64, 96, 128), sizes_3d=(24, 32),
+                              steps_range=(6, 20))
+    for r in reqs:  # a short inner schedule keeps the test quick
+        r.settings = r.settings.replace(iter_max=20, outer_max=4, inner_sweeps=5)
+    return reqs
+
+
+def test_gpu_shapes_match_host_generator():
+    s = G.settings_cylinder_2d()
+    shapes = [(0.5, 0.5, 0.05, 0.05, 0.0), (1.2, 0.4, 0.08, 0.03, 0.7)]
+    host = G.obstacles_2d(128, 64, 2.0, 1.0, shapes)
+    with Case.from_shapes(s, (128, 64), shapes) as c:
+        dev = c.porosity()
+    ref = Case(s, (128, 64), host)
+    np.testing.assert_allclose(dev, ref.porosity(), rtol=0, atol=1e-12)
+    ref.close()
+
+
+def test_served_results_equal_single_runs():
+    reqs = _small_requests()
+    # budget for ~2 of the requests at a time forces queueing and slot reuse
+    budget = int(2.2 * max(case_bytes(r.settings, r.shape) for r in reqs))
+    with Server(hbm_budget_bytes=budget, chunk=4) as srv:
+        res = srv.run(reqs, realtime=True)
+        assert srv.peak_bytes <= budget
+    assert [r.rid for r in res] == [r.rid for r in reqs]
+    for r, q in zip(res, reqs):
+        assert r.done_s >= r.admitted_s >= 0
+        with Case.from_shapes(q.settings.replace(precision="mixed"), q.shape, q.shapes) as c:
+            c.initial_conditions()
+            c.step(q.steps)
+            alone = c.get_state()
+            # a request may diverge (the reference scheme is not unconditionally
+            # stable); it must then diverge identically alone and in the mix
+            assert np.array_equal(np.array(c.norms()), np.array([r.max_div, r.sor_error]), equal_nan=True)
+        for k in alone:
+            assert np.array_equal(alone[k], r.state[k], equal_nan=True), (q.rid, k)
+    summ = summarize(res, max(r.done_s for r in res))
+    assert summ["requests"] == len(reqs) and summ["p99_latency_s"] >= summ["p50_latency_s"]
