@@ -189,7 +189,8 @@ def cpu_baseline(settings, shape, vals, budget_s: float = 20.0, max_steps: int =
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
                 baseline_sample: int = 6, baseline_steps: int = 3):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
-    {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400, dt from CFL 0.2),
+    {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
+    Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit),
     precision form (FP32 sweeps in FP64 defect correction, 4 x 25), advanced by
     the persistent batch kernel.  Reports device-timed aggregate Mcell-steps/s
     and, as the comparison, the plain FP64 single-case step run sequentially
@@ -211,6 +212,7 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
     launches = b.kernel_launches() - l0
     value = cells * steps / (ms / 1e3) / 1e6
     mem = b.memory()[0]
+    nonfinite = sum(1 for sl in slots if not np.isfinite(b.norms(sl)[0]))
     b.close()
     # plain FP64 single-case step, one case after another, on a sample
     rng = np.random.default_rng(seed + 1)
@@ -231,6 +233,7 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
     return {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25",
             "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
             "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
+            "nonfinite_cases_after_timed_steps": nonfinite,
             "autotune": {"best": list(best), "trials": trials},
             "plain_fp64_sequential": {"value": plain, "unit": UNIT, "sample_cases": len(sample),
                                       "steps_each": baseline_steps},
@@ -238,18 +241,20 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
 
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
-                  baseline_sample: int = 4, baseline_steps: int = 3):
+                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 300000):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
     100-1000 steps each, admitted by a 150 GB HBM budget into one resident
-    batch and advanced `chunk` steps per persistent launch.  Latency is
-    wall-clock from arrival to the result (fields and norms) on the host."""
+    batch and advanced `chunk` steps per round: cases up to `large_cells`
+    cells in the persistent launch, larger ones as full-GPU step graphs on
+    their own streams beside it.  Latency is wall-clock from arrival to the
+    result (fields and norms) on the host."""
     from pixelflow_gb300 import geometry as G
     from pixelflow_gb300.serve import Server, summarize
     from pixelflow_gb300.solver import Case
     reqs = G.serving_requests(count=count, rate=rate, seed=seed)
     t0 = time.perf_counter()
-    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True) as srv:
+    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True, large_cells=large_cells) as srv:
         res = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         summ = summarize(res, wall)
@@ -270,7 +275,8 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
         tot_ms += prof["step_ms"]
     plain = tot_cells / (tot_ms / 1e3) / 1e6
     summ["workload"] = (f"{count} requests, Poisson {rate:g}/s, 70% 2D 128^2-1024^2 / 30% 3D 64^3-192^3, "
-                        f"100-1000 steps, 150 GB budget, chunk {chunk}")
+                        f"100-1000 steps, 150 GB budget, chunk {chunk}, large cases > {large_cells} cells "
+                        f"on own streams")
     summ["plain_fp64_sequential"] = {"value": plain, "unit": UNIT, "sample_requests": int(min(baseline_sample, len(reqs))),
                                      "steps_each": baseline_steps}
     summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain

@@ -169,18 +169,24 @@ int pf_memory_bytes(pf_case *c, size_t *bytes);
  * Many independent cases (2D and 3D, uneven sizes) resident on one GPU,
  * advanced by one persistent kernel per dimension: each thread-block cluster
  * claims a case from a device queue (largest work first) and runs all stages
- * of its steps itself, separated by hardware cluster barriers.  Cases run the
+ * of its steps itself, separated by hardware cluster barriers.  Cases larger
+ * than large_cells run full-GPU steps on their own streams at the same time.  Cases run the
  * precision form (PF_PREC_MIXED) with the per-case options given at add time.
  * No counterpart in the reference, which runs one case per process; the
  * per-case step is the same routine sequence as pf_step. */
 typedef struct pf_batch pf_batch;
 typedef struct pf_batch_options {
-  int32_t cluster;           /* CTAs per cluster: 1, 2, 4 or 8 */
+  int32_t cluster;           /* CTAs per cluster: 1, 2, 4, 8 or 16 */
   int32_t threads;           /* threads per CTA: 256, 512 or 1024 */
   int32_t max_cases;         /* slots */
-  int32_t reserved0;
+  int32_t global_passes;     /* 1: 2D cases never keep their correction in
+                                shared memory (default 0: they do when the
+                                rows of a CTA fit in 226 KB) */
   uint64_t hbm_budget_bytes; /* admission limit for the cases' device memory */
-  int32_t reserved[8];
+  int32_t large_cells;       /* cases with more cells run full-GPU steps on their
+                                own stream, concurrently with the persistent
+                                kernel (default 300000) */
+  int32_t reserved[7];
 } pf_batch_options;
 void pf_batch_default_options(pf_batch_options *opt); /* cluster 4, 512 threads, 1024 slots, 150 GiB */
 int pf_batch_create(const pf_batch_options *opt, pf_batch **out);

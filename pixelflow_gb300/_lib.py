@@ -54,7 +54,8 @@ PF_MAX_SHAPES = 32
 class PfBatchOptions(ctypes.Structure):
     _fields_ = [
         ("cluster", ctypes.c_int32), ("threads", ctypes.c_int32), ("max_cases", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("reserved", ctypes.c_int32 * 8),
+        ("global_passes", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("large_cells", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
     ]
 
 

@@ -13,7 +13,7 @@ import os
 from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 
 CANDIDATES: Tuple[Tuple[int, int], ...] = ((1, 256), (1, 512), (2, 256), (2, 512), (4, 256), (4, 512),
-                                           (8, 256), (8, 512), (2, 1024), (4, 1024))
+                                           (8, 256), (8, 512), (2, 1024), (4, 1024), (16, 256), (16, 512))
 
 
 def cache_path() -> str:

@@ -37,11 +37,13 @@ def case_bytes(settings: Settings, shape: Sequence[int]) -> int:
 
 class Batch:
     def __init__(self, cluster: int = 4, threads: int = 512, max_cases: int = 1024,
-                 hbm_budget_bytes: int = 150 * GIB):
+                 hbm_budget_bytes: int = 150 * GIB, global_passes: bool = False, large_cells: int = 300000):
         self.L = _lib.load()
         o = PfBatchOptions()
         self.L.pf_batch_default_options(ctypes.byref(o))
         o.cluster, o.threads, o.max_cases, o.hbm_budget_bytes = cluster, threads, max_cases, int(hbm_budget_bytes)
+        o.global_passes = 1 if global_passes else 0
+        o.large_cells = int(large_cells)
         h = ctypes.c_void_p()
         check(self.L.pf_batch_create(ctypes.byref(o), ctypes.byref(h)))
         self.h = h

@@ -144,8 +144,9 @@ static int case_alloc(pf_case* c) {
   const size_t stage = (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double);
   const bool three = g.dim == 3;
   struct Req {
-    double** dst;
+    void** dst;
     size_t bytes;
+    Req(double** d, size_t b) : dst(reinterpret_cast<void**>(d)), bytes(b) {}
   };
   std::vector<Req> req;
   req.push_back({&c->poro, nat});
@@ -179,7 +180,7 @@ static int case_alloc(pf_case* c) {
   c->bytes = total;
   size_t off = 0;
   for (auto& r : req) {
-    *r.dst = r.bytes ? reinterpret_cast<double*>(base + off) : nullptr;
+    *r.dst = r.bytes ? static_cast<void*>(base + off) : nullptr;
     off += (r.bytes + 255) / 256 * 256;
   }
   c->red = reinterpret_cast<unsigned long long*>(base + off);

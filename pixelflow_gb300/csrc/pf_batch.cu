@@ -49,6 +49,8 @@ struct CaseDesc {
   int cur;                  // current velocity buffer when the launch starts
   int nsteps;               // steps to advance in this launch
   int outer, inner, track;
+  int smem_rows;            // 2D: rows per CTA held in shared memory (0: global-memory passes)
+  int smem_pitch;           // shared-memory row pitch (floats)
 };
 
 namespace {
@@ -86,6 +88,99 @@ struct Walk3 {
   }
 };
 
+// The defect-correction passes of a 2D case with the FP32 correction e, the
+// FP32 porosity and the FP32 residual of each CTA's block of rows held in
+// shared memory for all inner iterations.  CTA r of the cluster owns rows
+// j0..j1 (R rows per CTA) plus a halo row on each side; after each
+// half-sweep it writes its updated first and last rows straight into the
+// halo rows of the CTAs that own the neighbouring rows (distributed shared
+// memory, periodic in y), then one cluster barrier.  The halo rows therefore
+// hold exactly what the reference's refreshed ghost rows hold (for an odd n
+// the two rows that cross the periodic edge go to the other colour's array,
+// as the ghost-row copy crosses colours there).  Arithmetic per
+// cell is dc_update's, so results equal the global-memory passes bit for bit.
+__device__ __forceinline__ void passes_smem_2d(const CaseDesc& d, cg::cluster_group& cl, int step, unsigned& emax,
+                                               float* sm) {
+  const Geo& g = d.g;
+  const Scal& s = d.s;
+  const int m = g.m, n = g.n, hc = (m + 1) / 2 + 1, P = d.smem_pitch, R = d.smem_rows;
+  const int r = (int)cl.block_rank();
+  const int j0 = 1 + r * R, j1 = min(n, j0 + R - 1), nr = j1 >= j0 ? j1 - j0 + 1 : 0;
+  float* E[2] = {sm, sm + (R + 2) * P};
+  float* EPS[2] = {sm + 2 * (R + 2) * P, sm + 3 * (R + 2) * P};
+  float* RR[2] = {sm + 4 * (R + 2) * P, sm + 4 * (R + 2) * P + R * P};
+  auto owner = [&](int row) { return (row - 1) / R; };
+  auto rows_of = [&](int t) {
+    const int a = 1 + t * R, b = min(n, a + R - 1);
+    return b >= a ? b - a + 1 : 0;
+  };
+  const int tS = owner(j0 == 1 ? n : j0 - 1);  // receives my first row in its north halo
+  const int tN = owner(j1 == n ? 1 : j1 + 1);  // receives my last row in its south halo
+  const int nrS = rows_of(tS);
+  const bool halo_p = n & 1;
+  if (step == 0) {  // porosity rows j0-1 .. j1+1 (ghost rows included), once per claimed case
+    for (int x = threadIdx.x; x < 2 * (nr + 2) * hc; x += blockDim.x) {
+      const int col = x / ((nr + 2) * hc), y = x - col * (nr + 2) * hc, lr = y / hc, h = y - lr * hc;
+      EPS[col][lr * P + h] = d.epsf[col][pk_idx(g, h, j0 - 1 + lr, 0)];
+    }
+  }
+  for (int pass = 0; pass < d.outer; pass++) {
+    // FP64 residual of my rows -> shared FP32 right-hand side; e = 0 incl. halos
+    for (int x = threadIdx.x; x < 2 * (nr + 2) * hc; x += blockDim.x) {
+      const int col = x / ((nr + 2) * hc), y = x - col * (nr + 2) * hc, lr = y / hc, h = y - lr * hc;
+      E[col][lr * P + h] = 0.f;
+      if (lr >= 1 && lr <= nr) {
+        double t = 0.0;
+        const bool ok = residual_value<2>(g, d.C[col], d.p[col], d.p[1 - col], s.omega, col, h, j0 + lr - 1, 0, t);
+        RR[col][(lr - 1) * P + h] = ok ? (float)t : 0.f;
+      }
+    }
+    cl.sync();  // no CTA pushes into a halo before its owner has zeroed it
+    for (int it = 0; it < d.inner; it++) {
+      for (int col = 0; col < 2; col++) {
+        for (int x = threadIdx.x; x < nr * hc; x += blockDim.x) {
+          const int lr = 1 + x / hc, h = x - (lr - 1) * hc, j = j0 + lr - 1;
+          const int sb = (col + j + 1) & 1, i = 2 * h + sb;
+          if (i < 1 || i > m) continue;
+          const float eold = E[col][lr * P + h];
+          const float enew = dc_update_rows_2d(d.K, EPS[col] + lr * P, EPS[1 - col] + lr * P, E[1 - col] + lr * P, P,
+                                               h, sb, i == 1, i == m, RR[col][(lr - 1) * P + h], eold);
+          E[col][lr * P + h] = enew;
+          emax = max(emax, abs_bits(enew - eold));
+        }
+        __syncthreads();
+        if (nr > 0) {
+          // Across the periodic edge of an odd n the neighbour is a ghost row,
+          // which holds the opposite edge row of the other colour: row n
+          // colour c is ghost row 0 colour 1-c (the reference's refresh before
+          // every half-sweep), so those two pushes land in the other array.
+          const int cS = (halo_p && j0 == 1) ? 1 - col : col;
+          const int cN = (halo_p && j1 == n) ? 1 - col : col;
+          float* dS = cl.map_shared_rank(E[cS], tS) + (nrS + 1) * P;
+          float* dN = cl.map_shared_rank(E[cN], tN);
+          for (int h = threadIdx.x; h < hc; h += blockDim.x) {
+            dS[h] = E[col][P + h];
+            dN[h] = E[col][nr * P + h];
+          }
+        }
+        cl.sync();
+      }
+    }
+    // p += e (FP64) for my rows
+    for (int x = threadIdx.x; x < 2 * nr * hc; x += blockDim.x) {
+      const int col = x / (nr * hc), y = x - col * nr * hc, lr = 1 + y / hc, h = y - (lr - 1) * hc;
+      const int j = j0 + lr - 1, i = 2 * h + ((col + j + 1) & 1);
+      if (i >= 1 && i <= m) d.p[col][pk_idx(g, h, j, 0)] += (double)E[col][lr * P + h];
+    }
+    cl.sync();
+    if (halo_p) {
+      for (int i = (int)cl.block_rank() * blockDim.x + threadIdx.x + 1; i <= m; i += cl.num_blocks() * blockDim.x)
+        c_p_halo_y(g, d.p[0], d.p[1], i, 0);
+      cl.sync();
+    }
+  }
+}
+
 template <int DIM, int BT>
 __device__ __forceinline__ void run_case(const CaseDesc& d, cg::cluster_group& cl, int tid, int nth) {
   const Geo& g = d.g;
@@ -117,6 +212,10 @@ __device__ __forceinline__ void run_case(const CaseDesc& d, cg::cluster_group& c
       c_rhs<double, DIM>(g, s, d.U[nw], d.V[nw], d.W[nw], d.poro, d.gx, d.gy, d.gz, d.C[0], d.C[1], i, j, k);
     }
     cl.sync();
+    if (DIM == 2 && d.smem_rows > 0) {
+      extern __shared__ float dyn_smem[];
+      passes_smem_2d(d, cl, step, emax, dyn_smem);
+    } else
     for (int pass = 0; pass < d.outer; pass++) {
       // FP64 residual of both colours -> FP32 right-hand side, e = 0
       for (Walk3 w(tid, nth, hc, n); w.c < 2 * l; w.next()) {
@@ -269,14 +368,23 @@ struct pf_batch {
   int64_t launches = 0;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   double last_ms = 0.0;  // device time of the last pf_batch_step_slots
+  std::vector<cudaEvent_t> case_ev;  // per slot: completion of a large case's steps
 };
 
 static int batch_fail(int code, const std::string& m) { return fail(code, m); }
 
 template <int DIM, int BT>
-static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, const int* order, const int* ncases, int* head) {
+static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, size_t smem, const int* order, const int* ncases,
+                               int* head) {
+  cudaError_t e = cudaFuncSetAttribute(k_batch<DIM, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(smem)");
+  if (cluster > 8) {
+    e = cudaFuncSetAttribute(k_batch<DIM, BT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(cluster size)");
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.blockDim = dim3(BT);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = b->st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -287,7 +395,7 @@ static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, const int* ord
   cfg.numAttrs = 1;
   cfg.gridDim = dim3(cluster);
   int maxc = 0;
-  cudaError_t e = cudaOccupancyMaxActiveClusters(&maxc, (void*)k_batch<DIM, BT>, &cfg);
+  e = cudaOccupancyMaxActiveClusters(&maxc, (void*)k_batch<DIM, BT>, &cfg);
   if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters");
   if (maxc < 1) return batch_fail(PF_E_INVALID, "batch: cluster configuration cannot be scheduled");
   const int nclusters = std::max(1, std::min(maxc, ncl));
@@ -299,12 +407,16 @@ static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, const int* ord
 }
 
 template <int DIM>
-static int launch_dim(pf_batch* b, int ncl, const int* order, const int* ncases, int* head) {
+static int launch_dim(pf_batch* b, int ncl, size_t smem, const int* order, const int* ncases, int* head) {
   const int c = b->opt.cluster;
-  if (b->opt.threads == 256) return launch_batch_kernel<DIM, 256>(b, ncl, c, order, ncases, head);
-  if (b->opt.threads == 512) return launch_batch_kernel<DIM, 512>(b, ncl, c, order, ncases, head);
-  return launch_batch_kernel<DIM, 1024>(b, ncl, c, order, ncases, head);
+  if (b->opt.threads == 256) return launch_batch_kernel<DIM, 256>(b, ncl, c, smem, order, ncases, head);
+  if (b->opt.threads == 512) return launch_batch_kernel<DIM, 512>(b, ncl, c, smem, order, ncases, head);
+  return launch_batch_kernel<DIM, 1024>(b, ncl, c, smem, order, ncases, head);
 }
+
+// Dynamic shared memory a CTA may take for the on-chip passes (the 227 KB
+// per-CTA limit minus the kernel's static shared memory).
+static const size_t kSmemCap = 227 * 1024 - 1024;
 
 extern "C" {
 
@@ -325,10 +437,11 @@ int pf_batch_create(const pf_batch_options* opt, pf_batch** out) {
     b->opt = *opt;
   else
     pf_batch_default_options(&b->opt);
-  if (!(b->opt.cluster == 1 || b->opt.cluster == 2 || b->opt.cluster == 4 || b->opt.cluster == 8) ||
+  if (!(b->opt.cluster == 1 || b->opt.cluster == 2 || b->opt.cluster == 4 || b->opt.cluster == 8 ||
+        b->opt.cluster == 16) ||
       !(b->opt.threads == 256 || b->opt.threads == 512 || b->opt.threads == 1024) || b->opt.max_cases < 1) {
     delete b;
-    return fail(PF_E_INVALID, "pf_batch_create: cluster must be 1,2,4,8; threads 256,512,1024; max_cases >= 1");
+    return fail(PF_E_INVALID, "pf_batch_create: cluster must be 1,2,4,8,16; threads 256,512,1024; max_cases >= 1");
   }
   b->capacity = b->opt.max_cases;
   cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
@@ -346,6 +459,8 @@ int pf_batch_create(const pf_batch_options* opt, pf_batch** out) {
   }
   b->slots.assign(b->capacity, nullptr);
   b->pending.assign(b->capacity, 0);
+  b->case_ev.assign(b->capacity, nullptr);
+  if (b->opt.large_cells <= 0) b->opt.large_cells = 300000;
   *out = b;
   return PF_OK;
 }
@@ -355,6 +470,8 @@ int pf_batch_destroy(pf_batch* b) {
   cudaStreamSynchronize(b->st);
   for (auto* c : b->slots)
     if (c) pf_destroy(c);
+  for (auto e : b->case_ev)
+    if (e) cudaEventDestroy(e);
   cudaFree(b->d_desc);
   cudaFree(b->d_order);
   cudaFree(b->d_misc);
@@ -402,7 +519,10 @@ static int batch_add_impl(pf_batch* b, const pf_params* prm, const pf_options* o
   else
     pf_default_options(&o);
   o.precision = PF_PREC_MIXED;  // the batched form runs the precision form
-  o.use_graph = 0;
+  // cases too large for one cluster run full-GPU steps (graph replays) on
+  // their own stream, concurrently with the persistent kernel
+  const long long cells = (long long)prm->m * prm->n * (prm->dim == 3 ? prm->l : 1);
+  o.use_graph = cells > b->opt.large_cells ? 1 : 0;
   size_t need = 0;
   int rc = pf_case_bytes(prm, &o, &need);
   if (rc) return rc;
@@ -458,10 +578,17 @@ pf_case* pf_batch_case(pf_batch* b, int slot) {
 
 // Advance the listed slots by their step counts in one persistent launch per
 // dimension (2D and 3D cases run in separate launches on the batch stream).
+// Cases with more than large_cells cells instead replay their single-case
+// step graphs on their own streams, overlapping the persistent kernels: one
+// cluster of a few SMs would take far longer over such a case than the whole
+// GPU does, and the persistent kernels leave the SMs their clusters do not
+// hold to those graphs.  Both paths run the same per-cell arithmetic.
 int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n) {
   if (!b || (n > 0 && (!slots || !nsteps))) return fail(PF_E_INVALID, "pf_batch_step_slots: null argument");
   std::vector<CaseDesc> desc;
   std::vector<std::pair<long long, int>> order2, order3;
+  std::vector<std::pair<int, int>> large;  // (slot, steps) run on their own streams
+  size_t smem2 = 0;  // dynamic shared memory of the 2D launch
   desc.reserve(n);
   for (int q = 0; q < n; q++) {
     const int sl = slots[q];
@@ -469,6 +596,10 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
     if (nsteps[q] < 0) return fail(PF_E_INVALID, "pf_batch_step_slots: negative step count");
     if (nsteps[q] == 0) continue;
     pf_case* c = b->slots[sl];
+    if ((long long)c->g.m * c->g.n * c->g.l > b->opt.large_cells) {
+      large.push_back({sl, nsteps[q]});
+      continue;
+    }
     CaseDesc d;
     std::memset(&d, 0, sizeof(d));
     d.g = c->g;
@@ -508,12 +639,35 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
     d.outer = c->opt.outer_max;
     d.inner = c->opt.inner_sweeps;
     d.track = c->opt.track_sor_error;
+    d.smem_rows = 0;
+    d.smem_pitch = 0;
+    if (c->g.dim == 2 && !b->opt.global_passes) {
+      const int R = (c->g.n + b->opt.cluster - 1) / b->opt.cluster;
+      const int P = (c->g.m + 1) / 2 + 1;
+      const size_t need = (size_t)(6 * R + 8) * P * sizeof(float);
+      if (need <= kSmemCap) {
+        d.smem_rows = R;
+        d.smem_pitch = P;
+        smem2 = std::max(smem2, need);
+      }
+    }
     const long long work = (long long)c->g.m * c->g.n * c->g.l * nsteps[q];
     (c->g.dim == 3 ? order3 : order2).push_back({work, (int)desc.size()});
     desc.push_back(d);
     c->cur ^= (nsteps[q] & 1);
   }
-  if (desc.empty()) return PF_OK;
+  if (desc.empty() && large.empty()) return PF_OK;
+  PF_CUDA(cudaEventRecord(b->ev[0], b->st));
+  for (auto& lc : large) {
+    pf_case* c = b->slots[lc.first];
+    if (!b->case_ev[lc.first]) PF_CUDA(cudaEventCreateWithFlags(&b->case_ev[lc.first], cudaEventDisableTiming));
+    PF_CUDA(cudaStreamWaitEvent(c->st, b->ev[0], 0));
+    const int64_t l0 = c->launches;
+    int rc = pf_step(c, lc.second);
+    if (rc) return rc;
+    b->launches += c->launches - l0;
+    PF_CUDA(cudaEventRecord(b->case_ev[lc.first], c->st));
+  }
   // longest work first, 2D list then 3D list
   auto by_work = [](const std::pair<long long, int>& a, const std::pair<long long, int>& c) { return a.first > c.first; };
   std::sort(order2.begin(), order2.end(), by_work);
@@ -523,15 +677,17 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
   for (auto& p : order3) order.push_back(p.second);
   if ((int)desc.size() > b->capacity) return fail(PF_E_INVALID, "too many cases");
   int misc[8] = {(int)order2.size(), 0, (int)order3.size(), 0, 0, 0, 0, 0};
-  PF_CUDA(cudaMemcpyAsync(b->d_desc, desc.data(), sizeof(CaseDesc) * desc.size(), cudaMemcpyHostToDevice, b->st));
-  PF_CUDA(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->st));
-  PF_CUDA(cudaMemcpyAsync(b->d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, b->st));
+  if (!desc.empty()) {
+    PF_CUDA(cudaMemcpyAsync(b->d_desc, desc.data(), sizeof(CaseDesc) * desc.size(), cudaMemcpyHostToDevice, b->st));
+    PF_CUDA(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->st));
+    PF_CUDA(cudaMemcpyAsync(b->d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, b->st));
+  }
   int rc = PF_OK;
-  PF_CUDA(cudaEventRecord(b->ev[0], b->st));
-  if (!order2.empty()) rc = launch_dim<2>(b, (int)order2.size(), b->d_order, b->d_misc + 0, b->d_misc + 1);
+  if (!order2.empty()) rc = launch_dim<2>(b, (int)order2.size(), smem2, b->d_order, b->d_misc + 0, b->d_misc + 1);
   if (rc == PF_OK && !order3.empty())
-    rc = launch_dim<3>(b, (int)order3.size(), b->d_order + order2.size(), b->d_misc + 2, b->d_misc + 3);
+    rc = launch_dim<3>(b, (int)order3.size(), 0, b->d_order + order2.size(), b->d_misc + 2, b->d_misc + 3);
   if (rc) return rc;
+  for (auto& lc : large) PF_CUDA(cudaStreamWaitEvent(b->st, b->case_ev[lc.first], 0));
   PF_CUDA(cudaEventRecord(b->ev[1], b->st));
   // the host arrays above must outlive the async copies
   PF_CUDA(cudaStreamSynchronize(b->st));
@@ -561,12 +717,14 @@ int pf_batch_synchronize(pf_batch* b) {
 int pf_batch_get_state(pf_batch* b, int slot, double* u, double* v, double* w, double* p, int ld1, int ld2) {
   if (!b || slot < 0 || slot >= b->capacity || !b->slots[slot]) return fail(PF_E_INVALID, "bad slot");
   PF_CUDA(cudaStreamSynchronize(b->st));
+  PF_CUDA(cudaStreamSynchronize(b->slots[slot]->st));
   return pf_get_state(b->slots[slot], u, v, w, p, ld1, ld2);
 }
 
 int pf_batch_norms(pf_batch* b, int slot, double* max_div, double* sor_error) {
   if (!b || slot < 0 || slot >= b->capacity || !b->slots[slot]) return fail(PF_E_INVALID, "bad slot");
   PF_CUDA(cudaStreamSynchronize(b->st));
+  PF_CUDA(cudaStreamSynchronize(b->slots[slot]->st));
   return pf_norms(b->slots[slot], max_div, sor_error);
 }
 
@@ -585,9 +743,9 @@ int pf_batch_last_ms(pf_batch* b, double* ms) {
 
 int pf_batch_configure(pf_batch* b, int cluster, int threads) {
   if (!b) return fail(PF_E_INVALID, "null batch");
-  if (!(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8) ||
+  if (!(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8 || cluster == 16) ||
       !(threads == 256 || threads == 512 || threads == 1024))
-    return fail(PF_E_INVALID, "pf_batch_configure: cluster must be 1,2,4,8 and threads 256,512,1024");
+    return fail(PF_E_INVALID, "pf_batch_configure: cluster must be 1,2,4,8,16 and threads 256,512,1024");
   b->opt.cluster = cluster;
   b->opt.threads = threads;
   return PF_OK;

@@ -314,21 +314,20 @@ __device__ __forceinline__ decltype(abs_bits(T(0))) c_sor_half(const Geo& g, con
   return e;
 }
 
-// FP64 residual of one cell, stored as the FP32 right-hand side of the
-// correction sweeps; zeroes e of that cell; returns |r| as bits.
+// FP64 residual of one cell, r = bbn - w p - sum a p_nb (normalised by w/ap).
+// Returns false for positions outside the grid.
 template <int DIM>
-__device__ __forceinline__ unsigned long long c_residual(const Geo& g, const Coef<double>& C,
-                                                         const double* __restrict__ pc, const double* __restrict__ po,
-                                                         double omega, int colour, float* __restrict__ rf,
-                                                         float* __restrict__ ec, int h, int j, int k) {
+__device__ __forceinline__ bool residual_value(const Geo& g, const Coef<double>& C, const double* __restrict__ pc,
+                                               const double* __restrict__ po, double omega, int colour, int h, int j,
+                                               int k, double& t) {
   const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
   const int i = 2 * h + s;
-  if (!(j <= g.n && i >= 1 && i <= g.m)) return 0ULL;
+  if (!(j <= g.n && i >= 1 && i <= g.m)) return false;
   const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
   const idx_t q = pk_idx(g, h, j, k);
   const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
   const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-  double t = C.bbn[q];
+  t = C.bbn[q];
   t = fma(-C.a[0][q], po[q + s], t);
   t = fma(-C.a[1][q], po[q - 1 + s], t);
   t = fma(-C.a[2][q], po[qn], t);
@@ -340,6 +339,19 @@ __device__ __forceinline__ unsigned long long c_residual(const Geo& g, const Coe
     t = fma(-C.a[5][q], po[qb], t);
   }
   t = fma(-omega, pc[q], t);
+  return true;
+}
+
+// The residual stored as the FP32 right-hand side of the correction sweeps;
+// zeroes e of that cell; returns |r| as bits.
+template <int DIM>
+__device__ __forceinline__ unsigned long long c_residual(const Geo& g, const Coef<double>& C,
+                                                         const double* __restrict__ pc, const double* __restrict__ po,
+                                                         double omega, int colour, float* __restrict__ rf,
+                                                         float* __restrict__ ec, int h, int j, int k) {
+  double t;
+  if (!residual_value<DIM>(g, C, pc, po, omega, colour, h, j, k, t)) return 0ULL;
+  const idx_t q = pk_idx(g, h, j, k);
   rf[q] = (float)t;
   ec[q] = 0.0f;
   return abs_bits(t);
@@ -445,6 +457,42 @@ struct DCConst {
   float small, omega, omw;
 };
 
+// One cell of the correction sweep from its loaded operands.  Every form of
+// the sweep (the vectorised single-case kernel, the persistent batch kernel's
+// global and shared-memory passes) calls this, so they agree bit for bit.
+template <int DIM>
+__device__ __forceinline__ float dc_cell(const DCConst& K, float pc, float pe, float pw, float pn, float ps,
+                                         float pt, float pb, float xe, float xw, float xn, float xs, float xt,
+                                         float xb, float rr, float eold, bool inlet, bool outlet) {
+  float ae = K.kx * fmaxf(K.small, (pe + pc) * 0.5f);
+  float aw = K.kx * fmaxf(K.small, (pc + pw) * 0.5f);
+  const float an = K.ky * fmaxf(K.small, (pn + pc) * 0.5f);
+  const float as = K.ky * fmaxf(K.small, (pc + ps) * 0.5f);
+  float at = 0.f, ab = 0.f;
+  if (DIM == 3) {
+    at = K.kz * fmaxf(K.small, (pt + pc) * 0.5f);
+    ab = K.kz * fmaxf(K.small, (pc + pb) * 0.5f);
+  }
+  const float ap = -ae - aw - an - as - at - ab;
+  float enew = fmaf(K.omw, eold, rr);
+  if (!outlet) {
+    if (inlet) {
+      ae += aw;
+      aw = 0.f;
+    }
+    float t = ae * xe;
+    t = fmaf(aw, xw, t);
+    t = fmaf(an, xn, t);
+    t = fmaf(as, xs, t);
+    if (DIM == 3) {
+      t = fmaf(at, xt, t);
+      t = fmaf(ab, xb, t);
+    }
+    enew = fmaf(-__fdividef(K.omega, ap), t, enew);
+  }
+  return enew;
+}
+
 template <int DIM>
 __device__ __forceinline__ void dc_update(const Geo& g, const DCConst& K, const float* __restrict__ epsc,
                                           const float* __restrict__ epso, const float* __restrict__ r,
@@ -468,33 +516,21 @@ __device__ __forceinline__ void dc_update(const Geo& g, const DCConst& K, const 
     xt = eo[qt];
     xb = eo[qb];
   }
-  float ae = K.kx * fmaxf(K.small, (pe + pc) * 0.5f);
-  float aw = K.kx * fmaxf(K.small, (pc + pw) * 0.5f);
-  const float an = K.ky * fmaxf(K.small, (pn + pc) * 0.5f);
-  const float as = K.ky * fmaxf(K.small, (pc + ps) * 0.5f);
-  float at = 0.f, ab = 0.f;
-  if (DIM == 3) {
-    at = K.kz * fmaxf(K.small, (pt + pc) * 0.5f);
-    ab = K.kz * fmaxf(K.small, (pc + pb) * 0.5f);
-  }
-  const float ap = -ae - aw - an - as - at - ab;
-  enew = fmaf(K.omw, eold, rr);
-  if (i != g.m) {
-    if (i == 1) {
-      ae += aw;
-      aw = 0.f;
-    }
-    float t = ae * xe;
-    t = fmaf(aw, xw, t);
-    t = fmaf(an, xn, t);
-    t = fmaf(as, xs, t);
-    if (DIM == 3) {
-      t = fmaf(at, xt, t);
-      t = fmaf(ab, xb, t);
-    }
-    enew = fmaf(-__fdividef(K.omega, ap), t, enew);
-  }
+  enew = dc_cell<DIM>(K, pc, pe, pw, pn, ps, pt, pb, xe, xw, xn, xs, xt, xb, rr, eold, i == 1, i == g.m);
 }
 
+
+// The same update as dc_update for a 2D cell whose correction, porosity and
+// residual rows are held in shared memory: E*/P* point at the cell's local
+// row of the own (c) and other (o) colour arrays, `pitch` is the row pitch.
+__device__ __forceinline__ float dc_update_rows_2d(const DCConst& K, const float* __restrict__ Pc,
+                                                   const float* __restrict__ Po, const float* __restrict__ Eo,
+                                                   int pitch, int h, int s, bool inlet, bool outlet, float rr,
+                                                   float eold) {
+  const float pc = Pc[h];
+  const float pe = Po[h + s], pw = Po[h - 1 + s], pn = Po[h + pitch], ps = Po[h - pitch];
+  const float xe = Eo[h + s], xw = Eo[h - 1 + s], xn = Eo[h + pitch], xs = Eo[h - pitch];
+  return dc_cell<2>(K, pc, pe, pw, pn, ps, 0.f, 0.f, xe, xw, xn, xs, 0.f, 0.f, rr, eold, inlet, outlet);
+}
 
 }  // namespace pf

@@ -129,6 +129,26 @@ def settings_spheres_3d(**kw) -> Settings:
     return s.replace(**kw)
 
 
+def cfl_dt(h: float, nu: float, u: float = 1.0, dim: int = 2, cfl: float = 0.2) -> float:
+    """Time step at Courant number `cfl` of the explicit predictor's full
+    stability limit.  Forward Euler on central advection plus diffusion is
+    stable (von Neumann) only for dt <= h/|u| (advection), dt <= 2 nu/|u|^2
+    (the central advection term needs viscous damping) and
+    dt <= h^2/(2 dim nu) (diffusion); dt = cfl * the smallest of the three.
+    The plain advective CFL dt = cfl*h/u alone leaves dt*u^2/nu between 1.5
+    and 10 for Re 50-400 on these grids."""
+    return cfl * min(h / u, 2.0 * nu / (u * u), h * h / (2.0 * dim * nu))
+
+
+def grid_nu(nu: float, h: float, u: float = 1.0, cell_re: float = 2.0) -> float:
+    """Viscosity raised, where needed, to cell Reynolds number u*h/nu <= cell_re.
+    The reference scheme's growth there is a property of the spatial
+    discretisation, not of dt: in the restated step the 2D cylinder at
+    256x128 (nu = 1e-3, cell Re 7.8) diverges at the same physical time
+    (t ~ 0.0075) for dt = 1e-4 and 5e-5, and stays bounded at nu = 4e-3."""
+    return max(nu, u * h / cell_re)
+
+
 @dataclasses.dataclass
 class BatchCase2D:
     m: int
@@ -146,7 +166,9 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
     """Independent 2D cases of uneven size: nx, ny from `sizes`, 1-4 circles or
     ellipses with semi-axes 0.02-0.1 of the height at random angles, Re uniform
     in [50, 400] (nu = U*D/Re with D twice the first obstacle's larger
-    semi-axis), unit inflow, dt from CFL 0.2 (dt = 0.2*dx/U), square cells."""
+    semi-axis, raised to cell Reynolds number <= 2 by `grid_nu`), unit
+    inflow, dt from CFL 0.2 of the full stability limit (`cfl_dt`), square
+    cells."""
     rng = np.random.default_rng(seed)
     cases = []
     for _ in range(count):
@@ -168,8 +190,8 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
         re = float(rng.uniform(50.0, 400.0))
         d_ref = 2.0 * max(shapes[0][2], shapes[0][3])
         u_in = 1.0
-        nu = u_in * d_ref / re
-        dt = 0.2 * h / u_in
+        nu = grid_nu(u_in * d_ref / re, h, u_in)
+        dt = cfl_dt(h, nu, u_in, 2)
         s = Settings(xnue=nu, xlambda=0.0, density=1.0, width=width, height=height, depth=0.0,
                      time=dt * steps, inlet_velocity=u_in, outlet_pressure=0.0, aoa=0.0,
                      istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6,
@@ -222,9 +244,11 @@ def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2
                      sizes_3d: Sequence[int] = (64, 96, 128, 160, 192),
                      steps_range: Tuple[int, int] = (100, 1000)) -> List[Request]:
     """Poisson arrivals (exponential gaps, mean 1/rate) of mixed cases.
-    2D: n x n grids, 1-4 circles/ellipses (semi-axes 0.02-0.1), Re 50-400,
-    dt = 0.2 dx.  3D: n^3 unit cubes, 4-16 spheres (radii 0.03-0.08, centres
-    in [0.15, 0.85]^3), nu 2e-3..1e-2, dt = min(0.2 dx, 0.1 dx^2/nu).
+    2D: n x n unit squares, 1-4 circles/ellipses (semi-axes 0.02-0.1),
+    Re 50-400 on the first obstacle's diameter.  3D: n^3 unit cubes, 4-16
+    spheres (radii 0.03-0.08, centres in [0.15, 0.85]^3), nu 2e-3..1e-2.
+    Unit inflow; nu raised to cell Reynolds number <= 2 (`grid_nu`); dt at
+    CFL 0.2 of the full stability limit (`cfl_dt`).
     Steps per request uniform in steps_range."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -243,8 +267,8 @@ def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2
                 shapes.append((float(rng.uniform(0.2, 0.8)), float(rng.uniform(0.2, 0.8)), a, b,
                                float(rng.uniform(0.0, np.pi))))
             re = float(rng.uniform(50.0, 400.0))
-            nu = 2.0 * max(shapes[0][2], shapes[0][3]) / re
-            dt = 0.2 * h
+            nu = grid_nu(2.0 * max(shapes[0][2], shapes[0][3]) / re, h)
+            dt = cfl_dt(h, nu, 1.0, 2)
             s = Settings(xnue=nu, width=1.0, height=1.0, depth=0.0, time=dt * steps, inlet_velocity=1.0,
                          istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
                          iter_max=100, relux_factor=1.7, precision="mixed")
@@ -254,8 +278,8 @@ def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2
             h = 1.0 / (n - 1)
             ns = int(rng.integers(4, 17))
             sph = random_spheres(ns, seed=int(rng.integers(0, 2 ** 31)))
-            nu = float(rng.uniform(2e-3, 1e-2))
-            dt = min(0.2 * h, 0.1 * h * h / nu)
+            nu = grid_nu(float(rng.uniform(2e-3, 1e-2)), h)
+            dt = cfl_dt(h, nu, 1.0, 3)
             s = Settings(xnue=nu, width=1.0, height=1.0, depth=1.0, time=dt * steps, inlet_velocity=1.0,
                          istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
                          iter_max=100, relux_factor=1.7, precision="mixed")

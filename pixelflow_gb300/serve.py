@@ -4,9 +4,10 @@ Requests (a geometry, grid, physics and a step count) arrive over time.  The
 loop keeps every admitted case's fields resident in HBM inside one `Batch`;
 a request is admitted as soon as its memory fits the HBM budget (and a slot
 is free), in arrival order.  Each round advances every active case by up to
-`chunk` steps in one persistent launch per dimension, so requests that arrive
-while others are running join at the next round and their work overlaps on
-the device with the cases already there.  A finished case's result (its
+`chunk` steps: cases of up to `large_cells` cells in one persistent launch per
+dimension, larger ones as full-GPU step graphs on their own streams at the
+same time.  Requests that arrive while others are running join at the next
+round and their work overlaps on the device with the cases already there.  A finished case's result (its
 fields and norms) is read back, its slot and memory freed, and its latency
 (completion minus arrival) recorded.
 
@@ -46,9 +47,9 @@ class Result:
 
 class Server:
     def __init__(self, hbm_budget_bytes: int = 150 * GIB, chunk: int = 25, cluster: int = 4, threads: int = 512,
-                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0):
+                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 300000):
         self.batch = Batch(cluster=cluster, threads=threads, max_cases=max_cases,
-                           hbm_budget_bytes=hbm_budget_bytes)
+                           hbm_budget_bytes=hbm_budget_bytes, large_cells=large_cells)
         self.chunk = chunk
         self.keep_state = keep_state
         self.edge = edge

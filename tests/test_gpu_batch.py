@@ -37,17 +37,42 @@ def _same(a, b):
     return all(np.array_equal(a[k], b[k], equal_nan=True) for k in a)
 
 
-@pytest.mark.parametrize("cluster,threads", [(4, 512), (1, 256), (2, 1024)])
-def test_batch_matches_single_cases_bitwise(cluster, threads):
+@pytest.mark.parametrize("cluster,threads,global_passes", [(4, 512, False), (1, 256, False), (2, 1024, True),
+                                                          (8, 512, True), (8, 256, False), (16, 256, False)])
+def test_batch_matches_single_cases_bitwise(cluster, threads, global_passes):
+    """2D cases keep their correction in shared memory unless global_passes;
+    both paths, every launch shape, must equal the single-case runs."""
     cases = _cases()
     steps = 4
     ref = [_single(s, shape, vals, steps) for (s, shape, vals) in cases]
-    with Batch(cluster=cluster, threads=threads) as b:
+    with Batch(cluster=cluster, threads=threads, global_passes=global_passes) as b:
         slots = [b.add(s, shape, vals) for (s, shape, vals) in cases]
-        b.step(steps)
+        try:
+            b.step(steps)
+        except PfError as exc:
+            if cluster == 16 and "scheduled" in str(exc):
+                pytest.skip("clusters of 16 CTAs cannot be scheduled on this device")
+            raise
         for k, sl in enumerate(slots):
             got = b.get_state(sl)
             assert _same(got, ref[k][0]), (k, cases[k][1])
+            assert np.array_equal(np.array(b.norms(sl)), np.array(ref[k][1]), equal_nan=True)
+
+
+def test_large_cases_on_own_streams_match_single_cases():
+    """With large_cells small, all but the smallest 2D case run full-GPU step
+    graphs on their own streams beside the persistent kernel: the fields are
+    still those of the single-case runs, and the launch count covers both."""
+    cases = _cases()
+    steps = 3
+    ref = [_single(s, shape, vals, steps) for (s, shape, vals) in cases]
+    with Batch(cluster=2, threads=512, large_cells=1000) as b:
+        slots = [b.add(s, shape, vals) for (s, shape, vals) in cases]
+        n0 = b.kernel_launches()
+        b.step(steps)
+        assert b.kernel_launches() - n0 > 2
+        for k, sl in enumerate(slots):
+            assert _same(b.get_state(sl), ref[k][0]), (k, cases[k][1])
             assert np.array_equal(np.array(b.norms(sl)), np.array(ref[k][1]), equal_nan=True)
 
 
