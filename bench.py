@@ -73,6 +73,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def fp64_peak_tflops(n: int = 4096, reps: int = 5) -> float:
+    """FP64 arithmetic peak of this GPU as delivered by cuBLAS DGEMM (2 n^3
+    flops, best of `reps`, CUDA events): the roof of the FP64 kernels."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / best / 1e12
+
+
 def ncu_traffic(name: str):
     """Per-launch DRAM bytes of the dominant kernel from a committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
@@ -376,6 +397,15 @@ def run_ours(args):
                 "traffic": traffic, "peak_source": peak_kind, "kernel": "k_sor_half",
                 "sor_share_of_step": prof["sor_ms"] / prof["step_ms"], "avg_launch_ms": sor_launch_ms,
                 "algorithmic_bytes_per_launch": alg_bytes}
+    if args.precision == "fp64":
+        # The FP64 sweep is bound by the FP64 units (2 FMA/clk/SM on GB300), not by
+        # HBM: 7 FMAs per cell update (6 neighbours, the (1-w) p term) = 14 flops.
+        fp64_peak = fp64_peak_tflops()
+        flops = cells / 2 * 14
+        alu = flops / (sor_launch_ms / 1e3) / 1e12
+        roofline["fp64_alu"] = {"achieved": alu, "peak": fp64_peak, "unit": "TFLOP/s", "frac": alu / fp64_peak,
+                                "flops_per_launch": flops, "peak_source": "cuBLAS DGEMM 4096^3 measured live"}
+        roofline["binding"] = "fp64_alu" if alu / fp64_peak > achieved / peak else "hbm"
 
     # ---- end to end through the C ABI with host buffers ----------------------
     host = case.get_state()

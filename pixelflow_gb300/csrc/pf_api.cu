@@ -84,6 +84,32 @@ int make_scal(const pf_params& p, Scal& s) {
   const double ai = p.dim == 3 ? p.aoa / 360.0 * pi : p.aoa / 180.0 * pi;
   s.init_u = p.inlet_velocity * std::cos(ai);
   s.init_v = p.inlet_velocity * std::sin(ai);
+  s.hx = 0.5 / s.dx;
+  s.hy = 0.5 / s.dy;
+  s.hz = p.dim == 3 ? 0.5 / s.dz : 0.0;
+  s.ix2 = 1.0 / (s.dx * s.dx);
+  s.iy2 = 1.0 / (s.dy * s.dy);
+  s.iz2 = p.dim == 3 ? 1.0 / (s.dz * s.dz) : 0.0;
+  s.dtnu = s.dt * s.xnue;
+  s.dtnl = s.dt * (s.xnue + s.xlambda);
+  const double cdt = s.dt / s.density;
+  s.pgx = cdt * 0.5 / s.dx;
+  s.pgy = cdt * 0.5 / s.dy;
+  s.pgz = p.dim == 3 ? cdt * 0.5 / s.dz : 0.0;
+  s.hxf = (float)s.hx;
+  s.hyf = (float)s.hy;
+  s.hzf = (float)s.hz;
+  s.ix2f = (float)s.ix2;
+  s.iy2f = (float)s.iy2;
+  s.iz2f = (float)s.iz2;
+  s.dtf = (float)s.dt;
+  s.nuf = (float)s.xnue;
+  s.lamf = (float)s.xlambda;
+  s.dtnuf = (float)s.dtnu;
+  s.dtnlf = (float)s.dtnl;
+  s.pgxf = (float)s.pgx;
+  s.pgyf = (float)s.pgy;
+  s.pgzf = (float)s.pgz;
   return PF_OK;
 }
 

@@ -42,10 +42,18 @@ __device__ __forceinline__ unsigned long long max_of_slots(const unsigned long l
   return r;
 }
 
+// Exact warp max of 64-bit patterns: max of the high words, then the max low
+// word among the lanes holding that high word (two hardware reductions).
+__device__ __forceinline__ void warp_max64(unsigned& hi, unsigned& lo) {
+  const unsigned h = __reduce_max_sync(0xffffffffu, hi);
+  lo = __reduce_max_sync(0xffffffffu, hi == h ? lo : 0u);
+  hi = h;
+}
+
 __device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned long long* out) {
   __shared__ unsigned long long red[32];
   unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
-  for (int o = 16; o > 0; o >>= 1) max_pair(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+  warp_max64(hi, lo);
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nthr = blockDim.x * blockDim.y * blockDim.z;
   const int lane = tid & 31, warp = tid >> 5;
@@ -55,8 +63,7 @@ __device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned 
     const unsigned long long w = (lane < (nthr + 31) / 32) ? red[lane] : 0ULL;
     hi = (unsigned)(w >> 32);
     lo = (unsigned)w;
-    for (int o = 16; o > 0; o >>= 1)
-      max_pair(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+    warp_max64(hi, lo);
     const unsigned long long r = ((unsigned long long)hi << 32) | lo;
     if (lane == 0 && r) atomicMax(out + red_slot(), r);
   }
@@ -78,6 +85,28 @@ __device__ __forceinline__ void block_max_atomic(unsigned v, unsigned long long*
   }
 }
 
+
+// Packed sweeps over a flat thread index: slot h = 0 .. m/2 of every
+// interior row, rows j fastest then planes k.  Warps are full across row
+// ends (a 32-wide tile of the padded row pitch would leave one lane of 32
+// working in the last warp of each row).
+__host__ __device__ __forceinline__ int packed_width(const Geo& g) { return (g.m >> 1) + 1; }
+__host__ __device__ __forceinline__ long long packed_items(const Geo& g) {
+  return (long long)packed_width(g) * g.n * (g.dim == 3 ? g.l : 1);
+}
+template <int DIM>
+__device__ __forceinline__ void packed_item(const Geo& g, int t, int& h, int& j, int& k) {
+  const int W = packed_width(g);
+  const int row = t / W;
+  h = t - row * W;
+  if (DIM == 3) {
+    k = row / g.n + 1;
+    j = row - (k - 1) * g.n + 1;
+  } else {
+    k = 0;
+    j = row + 1;
+  }
+}
 
 __device__ __forceinline__ idx_t pk_of(const Geo& g, int i, int j, int k, int& c) {
   c = colour_of(g, i, j, k);
@@ -122,9 +151,9 @@ __device__ __forceinline__ void c_divergence(Geo g, Scal s, const T* __restrict_
                              const T* __restrict__ wo, T* __restrict__ div, int i, int j, int k) {
   const idx_t q = nat_idx(g, i, j, k);
   const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
-  const T hx = (T)(0.5 / s.dx);
+  const T hx = pick<T>(s.hx, s.hxf);
   if (g.dim == 3) {
-    const T hy = (T)(0.5 / s.dy), hz = (T)(0.5 / s.dz);
+    const T hy = pick<T>(s.hy, s.hyf), hz = pick<T>(s.hz, s.hzf);
     T d = (uo[q + 1] - uo[q - 1]) * hx;
     d = fma(vo[q + X] - vo[q - X], hy, d);
     d = fma(wo[q + XY] - wo[q - XY], hz, d);
@@ -145,10 +174,10 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
                                                       TS* __restrict__ v, TS* __restrict__ w, int i, int j, int k) {
   const idx_t q = nat_idx(g, i, j, k);
   const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
-  const T hx = (T)(0.5 / s.dx), hy = (T)(0.5 / s.dy);
-  const T ix2 = (T)(1.0 / (s.dx * s.dx)), iy2 = (T)(1.0 / (s.dy * s.dy));
-  const T dt = (T)s.dt, nu = (T)s.xnue, lam = (T)s.xlambda;
-  const T dtnu = (T)(s.dt * s.xnue), dtnl = (T)(s.dt * (s.xnue + s.xlambda));
+  const T hx = pick<T>(s.hx, s.hxf), hy = pick<T>(s.hy, s.hyf);
+  const T ix2 = pick<T>(s.ix2, s.ix2f), iy2 = pick<T>(s.iy2, s.iy2f);
+  const T dt = pick<T>(s.dt, s.dtf), nu = pick<T>(s.xnue, s.nuf), lam = pick<T>(s.xlambda, s.lamf);
+  const T dtnu = pick<T>(s.dtnu, s.dtnuf), dtnl = pick<T>(s.dtnl, s.dtnlf);
   const T two = (T)2;
   // div neighbours with the periodic wrap of the y (and z) ghost rows
   const idx_t jn = (j == g.n) ? q - (idx_t)(g.n - 1) * X : q + X;
@@ -184,7 +213,7 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
     t = fma(rv, por, t);
     v[q] = sv[q] + (TS)fma(-vc, dp * ix2, t);
   } else {
-    const T hz = (T)(0.5 / s.dz), iz2 = (T)(1.0 / (s.dz * s.dz));
+    const T hz = pick<T>(s.hz, s.hzf), iz2 = pick<T>(s.iz2, s.iz2f);
     const idx_t kt = (k == g.l) ? q - (idx_t)(g.l - 1) * XY : q + XY;
     const idx_t kb = (k == 1) ? q + (idx_t)(g.l - 1) * XY : q - XY;
     const T dT = div[kt], dB = div[kb];
@@ -237,13 +266,13 @@ __device__ __forceinline__ void c_rhs(Geo g, Scal s, const T* __restrict__ u, co
                       Coef<double> c1, int i, int j, int k) {
   const idx_t q = nat_idx(g, i, j, k);
   const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
-  const double hx = 0.5 / s.dx, hy = 0.5 / s.dy;
+  const double hx = s.hx, hy = s.hy;
   double sd = ((double)u[q + 1] - (double)u[q - 1]) * hx;
   sd = fma((double)v[q + X] - (double)v[q - X], hy, sd);
   double sg = gxa[q] * (double)u[q];
   sg = fma(gya[q], (double)v[q], sg);
   if (DIM == 3) {
-    sd = fma((double)w[q + XY] - (double)w[q - XY], 0.5 / s.dz, sd);
+    sd = fma((double)w[q + XY] - (double)w[q - XY], s.hz, sd);
     sg = fma(gza[q], (double)w[q], sg);
   }
   const double bb = s.density * fma(po[q], sd, sg);
@@ -262,10 +291,9 @@ __device__ __forceinline__ void c_projection(Geo g, Scal s, const double* __rest
   const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
   const idx_t r = pk_idx(g, i >> 1, j, k);
   const int sx = i & 1;
-  const double cdt = s.dt / s.density;
-  u[q] = fma(-(T)(cdt * 0.5 / s.dx), (T)(P[r + sx] - P[r - 1 + sx]), u[q]);
-  v[q] = fma(-(T)(cdt * 0.5 / s.dy), (T)(P[r + H] - P[r - H]), v[q]);
-  if (DIM == 3) w[q] = fma(-(T)(cdt * 0.5 / s.dz), (T)(P[r + HY] - P[r - HY]), w[q]);
+  u[q] = fma(-pick<T>(s.pgx, s.pgxf), (T)(P[r + sx] - P[r - 1 + sx]), u[q]);
+  v[q] = fma(-pick<T>(s.pgy, s.pgyf), (T)(P[r + H] - P[r - H]), v[q]);
+  if (DIM == 3) w[q] = fma(-pick<T>(s.pgz, s.pgzf), (T)(P[r + HY] - P[r - HY]), w[q]);
 }
 
 template <typename T>

@@ -60,7 +60,28 @@ struct Scal {
   double init_u, init_v;             // initial_conditions() values
   double outlet_pressure, omega;
   int nonslip;
+  // Factors of the stencils, computed once on the host: an FP64 division per
+  // cell costs tens of FP64-pipe instructions, and FP64 runs at 1/57 of the
+  // FP32 rate on GB300.  Same correctly rounded values as computing them on
+  // the device; the f-suffixed copies are those values rounded to float.
+  double hx, hy, hz;     // 0.5/dx, 0.5/dy, 0.5/dz
+  double ix2, iy2, iz2;  // 1/(dx*dx), ...
+  double dtnu, dtnl;     // dt*nu, dt*(nu+lambda)
+  double pgx, pgy, pgz;  // dt/density*0.5/dx, ... (projection)
+  float hxf, hyf, hzf, ix2f, iy2f, iz2f, dtf, nuf, lamf, dtnuf, dtnlf, pgxf, pgyf, pgzf;
 };
+
+// The double or float copy of a factor, by the arithmetic type T.
+template <typename T>
+__host__ __device__ __forceinline__ T pick(double d, float f) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    (void)d;
+    return f;
+  } else {
+    (void)f;
+    return d;
+  }
+}
 
 // Time-invariant SOR operator of one colour, normalised by omega/ap:
 //   p_new = (1-omega) p + bbn - sum_nb a_nb p_nb

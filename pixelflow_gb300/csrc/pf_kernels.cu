@@ -48,9 +48,9 @@ __global__ void k_porosity_factors(Geo g, Scal s, const double* __restrict__ po,
   const idx_t q = nat_idx(g, i, j, k);
   const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
   const double e = po[q];
-  gx[q] = (po[q + 1] - po[q - 1]) * (0.5 / s.dx);
-  gy[q] = (po[q + X] - po[q - X]) * (0.5 / s.dy);
-  if (g.dim == 3) gz[q] = (po[q + XY] - po[q - XY]) * (0.5 / s.dz);
+  gx[q] = (po[q + 1] - po[q - 1]) * s.hx;
+  gy[q] = (po[q + X] - po[q - X]) * s.hy;
+  if (g.dim == 3) gz[q] = (po[q + XY] - po[q - XY]) * s.hz;
   rinv[q] = s.dt / e;
   damp[q] = s.nonslip ? s.xnue * s.dt * 32.0 * e * (1.0 - e) * (1.0 - e) / (s.thickness * s.thickness) : 0.0;
 }
@@ -166,16 +166,21 @@ __global__ void k_rhs(Geo g, Scal s, const T* __restrict__ u, const T* __restric
 //   p = (bb - sum a_nb p_old_nb)/ap*omega + p_old*(1-omega)
 // because no neighbour of a cell changes during its own colour's sweep.
 // With TRACK the block max of |p_new - p_old| goes to *err.
+constexpr int SWEEP_THREADS = 256;
+
 template <typename T, int DIM, bool TRACK>
-__global__ void __launch_bounds__(BX* BY) k_sor_half(Geo g, Coef<T> C, T* __restrict__ pc,
-                                                     const T* __restrict__ po, T omw, int colour,
-                                                     unsigned long long* __restrict__ err,
-                                                     const int* __restrict__ skip) {
+__global__ void __launch_bounds__(SWEEP_THREADS) k_sor_half(Geo g, Coef<T> C, T* __restrict__ pc,
+                                                            const T* __restrict__ po, T omw, int colour,
+                                                            unsigned long long* __restrict__ err,
+                                                            const int* __restrict__ skip) {
   if (skip && *skip) return;  // uniform over the grid: defect correction converged
-  const int h = blockIdx.x * BX + threadIdx.x;
-  const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
-  const auto e = c_sor_half<T, DIM, TRACK>(g, C, pc, po, omw, colour, h, j, k);
+  const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
+  decltype(abs_bits(T(0))) e = 0;
+  if (t < packed_items(g)) {
+    int h, j, k;
+    packed_item<DIM>(g, t, h, j, k);
+    e = c_sor_half<T, DIM, TRACK>(g, C, pc, po, omw, colour, h, j, k);
+  }
   if (TRACK) block_max_atomic(e, err);
 }
 
@@ -251,12 +256,12 @@ __global__ void k_div_diag(Geo g, Scal s, const T* __restrict__ u, const T* __re
   if (i <= g.m && j <= g.n) {
     const idx_t q = nat_idx(g, i, j, k);
     const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
-    double sd = ((double)u[q + 1] - (double)u[q - 1]) * (0.5 / s.dx);
-    sd = fma((double)v[q + X] - (double)v[q - X], 0.5 / s.dy, sd);
+    double sd = ((double)u[q + 1] - (double)u[q - 1]) * s.hx;
+    sd = fma((double)v[q + X] - (double)v[q - X], s.hy, sd);
     double sg = gxa[q] * (double)u[q];
     sg = fma(gya[q], (double)v[q], sg);
     if (g.dim == 3) {
-      sd = fma((double)w[q + XY] - (double)w[q - XY], 0.5 / s.dz, sd);
+      sd = fma((double)w[q + XY] - (double)w[q - XY], s.hz, sd);
       sg = fma(gza[q], (double)w[q], sg);
     }
     e = abs_bits(fma(po[q], sd, sg));
@@ -306,16 +311,20 @@ __global__ void k_gather_pk(Geo g, const double* p0, const double* p1, double* _
 // FP64 residual of one colour, stored as FP32 right-hand side of the
 // correction sweeps; also zeroes e of that colour and reduces max|r|.
 template <int DIM>
-__global__ void __launch_bounds__(BX* BY) k_residual(Geo g, Coef<double> C, const double* __restrict__ pc,
+__global__ void __launch_bounds__(SWEEP_THREADS) k_residual(Geo g, Coef<double> C, const double* __restrict__ pc,
                                                      const double* __restrict__ po, double omega, int colour,
                                                      float* __restrict__ rf, float* __restrict__ ec,
                                                      unsigned long long* __restrict__ rmax,
                                                      const int* __restrict__ skip) {
   if (skip && *skip) return;
-  const int h = blockIdx.x * BX + threadIdx.x;
-  const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
-  block_max_atomic(c_residual<DIM>(g, C, pc, po, omega, colour, rf, ec, h, j, k), rmax);
+  const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
+  unsigned long long r = 0;
+  if (t < packed_items(g)) {
+    int h, j, k;
+    packed_item<DIM>(g, t, h, j, k);
+    r = c_residual<DIM>(g, C, pc, po, omega, colour, rf, ec, h, j, k);
+  }
+  block_max_atomic(r, rmax);
 }
 
 // FP32 correction sweep, four consecutive cells of one packed row per
@@ -485,17 +494,17 @@ static dim3 grid_packed(const Geo& g) {
 template <typename T>
 void launch_sor_half(const Geo& g, const Coef<T>& cc, T* pc, const T* po, T one_minus_omega, int colour,
                      unsigned long long* err, const int* skip, cudaStream_t st) {
-  const dim3 grid = grid_packed(g);
+  const unsigned grid = (unsigned)((packed_items(g) + SWEEP_THREADS - 1) / SWEEP_THREADS);
   if (g.dim == 3) {
     if (err)
-      k_sor_half<T, 3, true><<<grid, dim3(BX, BY), 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      k_sor_half<T, 3, true><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
     else
-      k_sor_half<T, 3, false><<<grid, dim3(BX, BY), 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      k_sor_half<T, 3, false><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
   } else {
     if (err)
-      k_sor_half<T, 2, true><<<grid, dim3(BX, BY), 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      k_sor_half<T, 2, true><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
     else
-      k_sor_half<T, 2, false><<<grid, dim3(BX, BY), 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      k_sor_half<T, 2, false><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
   }
 }
 
@@ -538,10 +547,11 @@ void launch_div_diag(const Geo& g, const Scal& s, const TV* u, const TV* v, cons
 void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, const double* po, double omega,
                      int colour, float* rf, float* ec, unsigned long long* rmax, const int* skip,
                      cudaStream_t st) {
+  const unsigned grid = (unsigned)((packed_items(g) + SWEEP_THREADS - 1) / SWEEP_THREADS);
   if (g.dim == 3)
-    k_residual<3><<<grid_packed(g), dim3(BX, BY), 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
+    k_residual<3><<<grid, SWEEP_THREADS, 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
   else
-    k_residual<2><<<grid_packed(g), dim3(BX, BY), 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
+    k_residual<2><<<grid, SWEEP_THREADS, 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
 }
 
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
