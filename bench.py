@@ -341,7 +341,8 @@ def run_batch_line(args):
     rank, world, local = dist_setup()
     from pixelflow_gb300 import _lib
     _lib.check(_lib.load().pf_set_device(local))
-    r = bench_batch(steps=args.steps, warmup_steps=max(1, args.warmup // 2))
+    r = bench_batch(ncases=args.cases, steps=args.steps, warmup_steps=max(1, args.warmup // 2),
+                    baseline_sample=min(6, args.cases))
     line = {"metric": METRIC, "value": r["value"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
@@ -479,6 +480,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", type=int, default=1, help="also measure the precision and batched forms")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--cases", type=int, default=512, help="batch2d workload: number of 2D cases")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         raise SystemExit("--warmup must be >= 3")

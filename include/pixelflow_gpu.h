@@ -53,7 +53,10 @@ typedef struct pf_params {
   double inlet_velocity, outlet_pressure, aoa;
   int32_t istep_max, iter_max;
   double thickness, threshold, relux_factor;
-  int32_t nonslip, reserved;
+  int32_t nonslip;
+  int32_t inflow_porosity; /* 1: inflow and initial velocities scaled by the
+                              porosity, as ibm_2d_backstep_omp_cpu.f90 does
+                              (:533-534, :615-618); 0: the uniform programs */
 } pf_params;
 
 /* Options that only this library reads (the &gpu_control group). */
@@ -118,6 +121,16 @@ int pf_initial_conditions(pf_case *c);
 int pf_set_state(pf_case *c, const double *u, const double *v, const double *w, const double *p,
                  int ld1, int ld2);
 int pf_get_state(pf_case *c, double *u, double *v, double *w, double *p, int ld1, int ld2);
+
+/* Asynchronous output at istep_out (the reference writes its VTK files from
+ * the host arrays, lib/output.f90:421-537, :968-1088): pf_snapshot_begin
+ * copies the state as of the last enqueued step on the device and starts the
+ * device->host copy on a second stream, so the caller can enqueue further
+ * steps at once; pf_snapshot_wait waits for that copy and unpacks it into the
+ * caller's arrays (same layout as pf_get_state; a null field is skipped).  One
+ * snapshot may be in flight per case (PF_E_BUSY otherwise). */
+int pf_snapshot_begin(pf_case *c);
+int pf_snapshot_wait(pf_case *c, double *u, double *v, double *w, double *p, int ld1, int ld2);
 int pf_get_porosity(pf_case *c, double *poro, int ld1, int ld2);
 
 /* solve_p: divergence, predictor, coefficients/RHS, boundrary_matrix and the
@@ -140,6 +153,14 @@ int pf_synchronize(pf_case *c);
  * ibm_2d_uniform_omp_cpu.f90:400 / ibm_3d:608; 0 when tracking is off).
  * Returns PF_E_NONFINITE if max_div is NaN or Inf. */
 int pf_norms(pf_case *c, double *max_div, double *sor_error);
+
+/* Force sums of the current state, as output_force_log_2d / _3d compute them
+ * (lib/output.f90:244-305, :1090-1165; called every step by
+ * ibm_2d_drag_omp_cpu.f90:121): force_p = pressure part (x, y, z), force_v =
+ * wall-friction part; z = 0 in 2D.  F = force_p + force_v, and the reference's
+ * Cd/Cl are F / (density * inlet_velocity^2 * radius).  Deterministic (fixed
+ * summation order); waits for the case's stream. */
+int pf_forces(pf_case *c, double force_p[3], double force_v[3]);
 
 /* Pin a caller-owned host buffer so pf_set_state / pf_get_state copy it
  * asynchronously at full link speed (cudaHostRegister); optional. */

@@ -33,6 +33,8 @@ class NpCase:
         self.thickness, self.relux = T(s.thickness), T(s.relux_factor)
         self.U, self.pout, self.aoa = T(s.inlet_velocity), T(s.outlet_pressure), T(s.aoa)
         self.nonslip, self.iter_max = bool(s.nonslip), int(s.iter_max)
+        # backstep program: inflow and initial velocity times porosity
+        self.inflow_porosity = bool(getattr(s, "inflow_porosity", False))
         # grid.f90:50-52 / :297-300
         self.dx = T(s.width) / T(m - 1)
         self.dy = T(s.height) / T(n - 1)
@@ -69,11 +71,17 @@ class NpCase:
             I = (slice(1, self.n + 1), slice(1, self.m + 1))
             self.u[I] = self.U * T(np.cos(self.aoa / T(180) * pi))
             self.v[I] = self.U * T(np.sin(self.aoa / T(180) * pi))
+            if self.inflow_porosity:  # ibm_2d_backstep_omp_cpu.f90:615-618
+                self.u[I] = self.u[I] * self.poro[I]
+                self.v[I] = self.v[I] * self.poro[I]
             self.p[I] = self.pout
         else:
             I = (slice(1, self.l + 1), slice(1, self.n + 1), slice(1, self.m + 1))
             self.u[I] = self.U * T(np.cos(self.aoa / T(360) * pi))
             self.v[I] = self.U * T(np.sin(self.aoa / T(360) * pi))
+            if self.inflow_porosity:
+                self.u[I] = self.u[I] * self.poro[I]
+                self.v[I] = self.v[I] * self.poro[I]
             self.w[I] = T(0)
             self.p[I] = self.pout
         self.boundary()
@@ -87,6 +95,9 @@ class NpCase:
             J = slice(1, n + 1)
             u[J, 1] = self.U * T(np.cos(self.aoa / T(180.) * pi))
             v[J, 1] = self.U * T(np.sin(self.aoa / T(180.) * pi))
+            if self.inflow_porosity:  # ibm_2d_backstep_omp_cpu.f90:533-534
+                u[J, 1] = u[J, 1] * self.poro[J, 1]
+                v[J, 1] = v[J, 1] * self.poro[J, 1]
             u[J, 0] = u[J, 1]
             v[J, 0] = v[J, 1]
             p[J, 0] = p[J, 2]
@@ -100,6 +111,9 @@ class NpCase:
             J, K = slice(1, n + 1), slice(1, l + 1)
             u[K, J, 1] = self.U * T(np.cos(self.aoa / T(1300.) * pi))
             v[K, J, 1] = self.U * T(np.sin(self.aoa / T(1300.) * pi))
+            if self.inflow_porosity:
+                u[K, J, 1] = u[K, J, 1] * self.poro[K, J, 1]
+                v[K, J, 1] = v[K, J, 1] * self.poro[K, J, 1]
             w[K, J, 1] = T(0)
             u[K, J, 0] = u[K, J, 1]
             v[K, J, 0] = v[K, J, 1]
@@ -326,3 +340,41 @@ class NpCase:
             d = d + ((S(po, 0, 0, 1) * S(w) + pc * S(w, 0, 0, 1)) / two
                      - (S(po, 0, 0, -1) * S(w) + pc * S(w, 0, 0, -1)) / two) / self.dz
         return float(np.abs(d).max()), d
+
+
+def forces(poro, p, u, v, w, dx, dy, dz, thickness, density, xnue):
+    """Force sums of output_force_log_2d/_3d (output.f90:244-305, :1090-1165),
+    vectorised: returns (pressure part (3,), friction part (3,), sum of |term|
+    per component (6,)) -- the last one scales the tolerance of a comparison
+    whose summation order differs."""
+    small, alpha = 1.e-6, 32.0
+    dim = p.ndim
+    if dim == 2:
+        c = (slice(1, -1), slice(1, -1))
+        gx = (poro[1:-1, 2:] - poro[1:-1, :-2]) * 0.5
+        gy = (poro[2:, 1:-1] - poro[:-2, 1:-1]) * 0.5
+        gz = np.zeros_like(gx)
+        vol = dx * dy
+        na = np.sqrt(gx * gx + gy * gy)
+    else:
+        c = (slice(1, -1), slice(1, -1), slice(1, -1))
+        gx = (poro[1:-1, 1:-1, 2:] - poro[1:-1, 1:-1, :-2]) * 0.5
+        gy = (poro[1:-1, 2:, 1:-1] - poro[1:-1, :-2, 1:-1]) * 0.5
+        gz = (poro[2:, 1:-1, 1:-1] - poro[:-2, 1:-1, 1:-1]) * 0.5
+        vol = dx * dy * dz
+        na = np.sqrt(gx * gx + gy * gy + gz * gz)
+    e = poro[c]
+    ee = e * (1.0 - e)
+    nrm = np.maximum(na, small)
+    terms = []
+    for g, h in ((gx, dx), (gy, dy), (gz, dz)):
+        terms.append(-vol * p[c] * 2 * e * (1.0 - e) / (thickness * h) * (g / nrm) if h else np.zeros_like(e))
+    for f, h in ((u, dx), (v, dy), (w, dz)):
+        if f is None or not h:
+            terms.append(np.zeros_like(e))
+        else:
+            t = ee / (thickness * h)
+            terms.append(vol * alpha * density * xnue * (t * t) * f[c])
+    sums = np.array([t.sum() for t in terms])
+    mags = np.array([np.abs(t).sum() for t in terms])
+    return sums[:3], sums[3:], mags

@@ -32,7 +32,7 @@ class OrParams(ctypes.Structure):
         ("outlet_pressure", ctypes.c_double), ("aoa", ctypes.c_double),
         ("istep_max", ctypes.c_int32), ("iter_max", ctypes.c_int32),
         ("thickness", ctypes.c_double), ("threshold", ctypes.c_double),
-        ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("inflow_porosity", ctypes.c_int32),
     ]
 
 
@@ -41,7 +41,7 @@ def make_params(settings, m: int, n: int, l: int = 1, dim: int = 2) -> OrParams:
     return OrParams(dim, m, n, l if dim == 3 else 1, s.xnue, s.xlambda, s.density, s.width,
                     s.height, s.depth, s.time, s.inlet_velocity, s.outlet_pressure, s.aoa,
                     int(s.istep_max), int(s.iter_max), s.thickness, s.threshold, s.relux_factor,
-                    1 if s.nonslip else 0, 0)
+                    1 if s.nonslip else 0, 1 if getattr(s, "inflow_porosity", False) else 0)
 
 
 def lib():
@@ -75,6 +75,7 @@ def lib():
             getattr(L, "or_step" + sfx).argtypes = [vp, ctypes.c_int] + [vp] * 8
             getattr(L, "or_divergence_diag" + sfx).restype = ctypes.c_double
             getattr(L, "or_divergence_diag" + sfx).argtypes = [vp] * 6
+            getattr(L, "or_forces" + sfx).argtypes = [vp] * 7
         _LIB = L
     return _LIB
 
@@ -186,6 +187,14 @@ class OracleCase:
         mx = self._f("or_divergence_diag")(self.ctx, _ptr(self.u), _ptr(self.v), _ptr(self.w),
                                            _ptr(self.poro), _ptr(out))
         return (mx, out) if want_field else mx
+
+    def forces(self):
+        """(pressure part (x, y, z), wall-friction part (x, y, z)) of the
+        reference's force log sums."""
+        out = np.zeros(6)
+        self._f("or_forces")(self.ctx, _ptr(self.p), _ptr(self.u), _ptr(self.v), _ptr(self.w),
+                             _ptr(self.poro), _ptr(out))
+        return out[:3].copy(), out[3:].copy()
 
     def state(self):
         d = dict(u=self.u.copy(), v=self.v.copy(), p=self.p.copy())

@@ -52,7 +52,7 @@ typedef struct or_params {
   double inlet_velocity, outlet_pressure, aoa;
   int32_t istep_max, iter_max;
   double thickness, threshold, relux_factor;
-  int32_t nonslip, reserved;
+  int32_t nonslip, inflow_porosity;
 } or_params;
 
 typedef struct F(or_ctx) {
@@ -61,6 +61,8 @@ typedef struct F(or_ctx) {
   REAL inlet_velocity, outlet_pressure, aoa, thickness, threshold, relux;
   REAL dx, dy, dz, dt;
   int nonslip, iter_max, istep_max;
+  int inflow_porosity;   /* backstep program: inflow/initial velocity x porosity */
+  const REAL *poro;      /* porosity of the case (set by or_grid_conditions) */
   size_t ncell; /* (m+2)(n+2)[(l+2)] */
   /* solve_p locals (static in the reference through -fno-automatic) */
   REAL *ap, *ae, *aw, *an, *as, *at, *ab, *bb, *div, *p_old;
@@ -96,6 +98,7 @@ CTX *F(or_create)(const or_params *P) {
   c->threshold = R(P->threshold);
   c->relux = R(P->relux_factor);
   c->nonslip = P->nonslip;
+  c->inflow_porosity = P->inflow_porosity;
   c->iter_max = P->iter_max;
   c->istep_max = P->istep_max;
   /* grid.f90:50-52 (2D), :297-300 (3D) */
@@ -137,6 +140,7 @@ double F(or_last_error)(const CTX *c) { return (double)c->last_error; }
 /* vals: porosity values in CSV order (i fastest), already parsed.     */
 void F(or_grid_conditions)(CTX *c, const double *vals, REAL *poro) {
   const int m = c->m, n = c->n, l = c->l;
+  c->poro = poro;
   memset(poro, 0, c->ncell * sizeof(REAL)); /* static arrays start at zero */
   if (c->dim == 2) {
     size_t q = 0;
@@ -182,6 +186,10 @@ void F(or_boundary)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
     for (int j = 1; j <= n; j++) {
       u[I2(1, j)] = c->inlet_velocity * (REAL)cos(c->aoa / R(180.) * pai);
       v[I2(1, j)] = c->inlet_velocity * (REAL)sin(c->aoa / R(180.) * pai);
+      if (c->inflow_porosity) { /* ibm_2d_backstep_omp_cpu.f90:533-534 */
+        u[I2(1, j)] = u[I2(1, j)] * c->poro[I2(1, j)];
+        v[I2(1, j)] = v[I2(1, j)] * c->poro[I2(1, j)];
+      }
       u[I2(0, j)] = u[I2(1, j)];
       v[I2(0, j)] = v[I2(1, j)];
       p[I2(0, j)] = p[I2(2, j)];
@@ -206,6 +214,10 @@ void F(or_boundary)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
       for (int j = 1; j <= n; j++) {
         u[I3(1, j, k)] = c->inlet_velocity * (REAL)cos(c->aoa / R(1300.) * pi);
         v[I3(1, j, k)] = c->inlet_velocity * (REAL)sin(c->aoa / R(1300.) * pi);
+        if (c->inflow_porosity) { /* the 2D backstep rule applied in 3D */
+          u[I3(1, j, k)] = u[I3(1, j, k)] * c->poro[I3(1, j, k)];
+          v[I3(1, j, k)] = v[I3(1, j, k)] * c->poro[I3(1, j, k)];
+        }
         w[I3(1, j, k)] = R(0.);
         u[I3(0, j, k)] = u[I3(1, j, k)];
         v[I3(0, j, k)] = v[I3(1, j, k)];
@@ -262,6 +274,10 @@ void F(or_initialize)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
       for (int i = 1; i <= m; i++) {
         u[I2(i, j)] = c->inlet_velocity * (REAL)cos(c->aoa / R(180) * pai);
         v[I2(i, j)] = c->inlet_velocity * (REAL)sin(c->aoa / R(180) * pai);
+        if (c->inflow_porosity) { /* ibm_2d_backstep_omp_cpu.f90:615-618 */
+          u[I2(i, j)] = u[I2(i, j)] * c->poro[I2(i, j)];
+          v[I2(i, j)] = v[I2(i, j)] * c->poro[I2(i, j)];
+        }
         p[I2(i, j)] = c->outlet_pressure;
       }
   } else {
@@ -271,6 +287,10 @@ void F(or_initialize)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
         for (int i = 1; i <= m; i++) {
           u[I3(i, j, k)] = c->inlet_velocity * (REAL)cos(c->aoa / R(360) * pi);
           v[I3(i, j, k)] = c->inlet_velocity * (REAL)sin(c->aoa / R(360) * pi);
+          if (c->inflow_porosity) {
+            u[I3(i, j, k)] = u[I3(i, j, k)] * c->poro[I3(i, j, k)];
+            v[I3(i, j, k)] = v[I3(i, j, k)] * c->poro[I3(i, j, k)];
+          }
           w[I3(i, j, k)] = R(0.);
           p[I3(i, j, k)] = c->outlet_pressure;
         }
@@ -784,4 +804,59 @@ double F(or_divergence_diag)(CTX *c, const REAL *u, const REAL *v, const REAL *w
         }
   }
   return (double)mx;
+}
+
+/* ------------------------------------------------------------------ */
+/* Force sums of output_force_log_2d (output.f90:244-305) and           */
+/* output_force_log_3d (output.f90:1090-1165): pressure part out[0..2]  */
+/* and wall-friction part out[3..5], summed sequentially in the         */
+/* reference's loop order (2D: i outer, j inner; 3D: k, j, i).          */
+void F(or_forces)(CTX *c, const REAL *p, const REAL *u, const REAL *v, const REAL *w, const REAL *po,
+                  double *out) {
+  const int m = c->m, n = c->n, l = c->l;
+  const REAL small = R(1.e-6), alpha = R(32.0);
+  const REAL dx = c->dx, dy = c->dy, dz = c->dz, th = c->thickness;
+  REAL fpx = R(0), fpy = R(0), fpz = R(0), fvx = R(0), fvy = R(0), fvz = R(0);
+  if (c->dim == 2) {
+    for (int i = 1; i <= m; i++)
+      for (int j = 1; j <= n; j++) {
+        const size_t q = I2(i, j);
+        const REAL gx = (po[I2(i + 1, j)] - po[I2(i - 1, j)]) * R(0.5);
+        const REAL gy = (po[I2(i, j + 1)] - po[I2(i, j - 1)]) * R(0.5);
+        const REAL na = (REAL)sqrt((double)(gx * gx + gy * gy));
+        const REAL nx = gx / rmax(na, small), ny = gy / rmax(na, small);
+        const REAL e = po[q], ee = e * (R(1.0) - e);
+        fpx = fpx + (-dx * dy * p[q] * R(2) * e * (R(1.0) - e) / (th * dx) * nx);
+        fpy = fpy + (-dx * dy * p[q] * R(2) * e * (R(1.0) - e) / (th * dy) * ny);
+        const REAL tx = ee / (th * dx), ty = ee / (th * dy);
+        fvx = fvx + (dx * dy * alpha * c->density * c->xnue * (tx * tx) * u[q]);
+        fvy = fvy + (dx * dy * alpha * c->density * c->xnue * (ty * ty) * v[q]);
+      }
+  } else {
+    for (int k = 1; k <= l; k++)
+      for (int j = 1; j <= n; j++)
+        for (int i = 1; i <= m; i++) {
+          const size_t q = I3(i, j, k);
+          const REAL gx = (po[I3(i + 1, j, k)] - po[I3(i - 1, j, k)]) * R(0.5);
+          const REAL gy = (po[I3(i, j + 1, k)] - po[I3(i, j - 1, k)]) * R(0.5);
+          const REAL gz = (po[I3(i, j, k + 1)] - po[I3(i, j, k - 1)]) * R(0.5);
+          const REAL na = (REAL)sqrt((double)(gx * gx + gy * gy + gz * gz));
+          const REAL nx = gx / rmax(na, small), ny = gy / rmax(na, small), nz = gz / rmax(na, small);
+          const REAL e = po[q], ee = e * (R(1.0) - e);
+          const REAL vol = dx * dy * dz;
+          fpx = fpx + (-vol * p[q] * R(2) * e * (R(1.0) - e) / (th * dx) * nx);
+          fpy = fpy + (-vol * p[q] * R(2) * e * (R(1.0) - e) / (th * dy) * ny);
+          fpz = fpz + (-vol * p[q] * R(2) * e * (R(1.0) - e) / (th * dz) * nz);
+          const REAL tx = ee / (th * dx), ty = ee / (th * dy), tz = ee / (th * dz);
+          fvx = fvx + (vol * alpha * c->density * c->xnue * (tx * tx) * u[q]);
+          fvy = fvy + (vol * alpha * c->density * c->xnue * (ty * ty) * v[q]);
+          fvz = fvz + (vol * alpha * c->density * c->xnue * (tz * tz) * w[q]);
+        }
+  }
+  out[0] = (double)fpx;
+  out[1] = (double)fpy;
+  out[2] = (double)fpz;
+  out[3] = (double)fvx;
+  out[4] = (double)fvy;
+  out[5] = (double)fvz;
 }

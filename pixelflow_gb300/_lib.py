@@ -29,7 +29,7 @@ class PfParams(ctypes.Structure):
         ("outlet_pressure", ctypes.c_double), ("aoa", ctypes.c_double),
         ("istep_max", ctypes.c_int32), ("iter_max", ctypes.c_int32),
         ("thickness", ctypes.c_double), ("threshold", ctypes.c_double),
-        ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("inflow_porosity", ctypes.c_int32),
     ]
 
 
@@ -84,12 +84,15 @@ _PROTOS = {
     "pf_set_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
     "pf_get_state": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
     "pf_get_porosity": (_I, [_VP, _VP, _I, _I]),
+    "pf_snapshot_begin": (_I, [_VP]),
+    "pf_snapshot_wait": (_I, [_VP, _VP, _VP, _VP, _VP, _I, _I]),
     "pf_solve_p": (_I, [_VP]),
     "pf_projection": (_I, [_VP]),
     "pf_boundary": (_I, [_VP]),
     "pf_step": (_I, [_VP, _I]),
     "pf_synchronize": (_I, [_VP]),
     "pf_norms": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "pf_forces": (_I, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "pf_host_register": (_I, [_VP, ctypes.c_size_t]),
     "pf_host_unregister": (_I, [_VP]),
     "pf_profile_begin": (_I, [_VP]),

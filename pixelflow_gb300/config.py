@@ -30,7 +30,7 @@ GROUPS = {
     "solver_control": ["iter_max", "relux_factor"],
 }
 GPU_GROUP = "gpu_control"
-GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error"]
+GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity"]
 
 
 @dataclasses.dataclass
@@ -65,6 +65,9 @@ class Settings:
     inner_sweeps: int = 25           # mixed: FP32 SOR iterations per pass
     dc_tol: float = 0.0              # mixed: stop the passes once max|r| <= dc_tol (0: run all)
     track_sor_error: bool = True     # keep the reference's SOR max-change diagnostic
+    # inflow and initial velocities scaled by porosity: the boundary and initial
+    # conditions of ibm_2d_backstep_omp_cpu.f90 (:533-534, :615-618)
+    inflow_porosity: bool = False
 
     def replace(self, **kw) -> "Settings":
         return dataclasses.replace(self, **kw)

@@ -74,6 +74,7 @@ int make_scal(const pf_params& p, Scal& s) {
   s.outlet_pressure = p.outlet_pressure;
   s.omega = p.relux_factor;
   s.nonslip = p.nonslip ? 1 : 0;
+  s.inflow_poro = nullptr;  // set to the case's porosity once it is allocated
   const double pi = std::atan(1.0) * 4.0;
   // boundary(): 2D cos(AoA/180*pi) (ibm_2d:478), 3D cos(AoA/1300*pi) (ibm_3d:695)
   const double ab = p.dim == 3 ? p.aoa / 1300.0 * pi : p.aoa / 180.0 * pi;
@@ -222,6 +223,11 @@ static void case_free(pf_case* c) {
   if (c->base) cudaFree(c->base);
   mixed_free(c);
   if (c->hred) cudaFreeHost(c->hred);
+  if (c->snap) cudaFree(c->snap);
+  if (c->hsnap) cudaFreeHost(c->hsnap);
+  for (auto& e : c->ev_snap)
+    if (e) cudaEventDestroy(e);
+  if (c->st_snap) cudaStreamDestroy(c->st_snap);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -395,6 +401,7 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     case_free(c);
     return rc;
   }
+  c->s.inflow_poro = c->prm.inflow_porosity ? c->poro : nullptr;
   *out = c;
   return PF_OK;
 }
@@ -541,6 +548,62 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   return PF_OK;
 }
 
+int pf_snapshot_begin(pf_case* c) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (c->snap_pending) return fail(PF_E_BUSY, "pf_snapshot_begin: the previous snapshot was not collected");
+  const Geo& g = c->g;
+  const size_t dense = (size_t)(g.m + 2) * (g.n + 2) * g.Z;
+  const int nf = g.dim + 1;
+  if (!c->snap) {
+    PF_CUDA(cudaMalloc(&c->snap, nf * dense * sizeof(double)));
+    PF_CUDA(cudaHostAlloc(&c->hsnap, nf * dense * sizeof(double), cudaHostAllocDefault));
+    PF_CUDA(cudaStreamCreateWithFlags(&c->st_snap, cudaStreamNonBlocking));
+    for (auto& e : c->ev_snap) PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // device-side copies on the case's stream: the state as of the last enqueued step
+  const int b = c->cur;
+  const double* src[3] = {c->U[b], c->V[b], c->W[b]};
+  const size_t dp = (size_t)(g.m + 2) * sizeof(double);
+  for (int f = 0; f < g.dim; f++) {
+    cudaMemcpy3DParms P = copy_params(c, src[f], (size_t)g.X * sizeof(double), g.Y, c->snap + f * dense, dp, g.n + 2,
+                                      cudaMemcpyDeviceToDevice);
+    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+  }
+  launch_gather_pk(g, c->p[0], c->p[1], c->snap + g.dim * dense, c->st);
+  c->launches += 1;
+  int rc = check_launch("pf_snapshot_begin");
+  if (rc) return rc;
+  PF_CUDA(cudaEventRecord(c->ev_snap[0], c->st));
+  // the copy to the host runs on the second stream, overlapping later steps
+  PF_CUDA(cudaStreamWaitEvent(c->st_snap, c->ev_snap[0], 0));
+  PF_CUDA(cudaMemcpyAsync(c->hsnap, c->snap, nf * dense * sizeof(double), cudaMemcpyDeviceToHost, c->st_snap));
+  PF_CUDA(cudaEventRecord(c->ev_snap[1], c->st_snap));
+  c->snap_pending = true;
+  return PF_OK;
+}
+
+int pf_snapshot_wait(pf_case* c, double* u, double* v, double* w, double* p, int ld1, int ld2) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (!c->snap_pending) return fail(PF_E_STATE, "pf_snapshot_wait: no snapshot in flight");
+  int rc = check_ld(c, ld1, ld2);
+  if (rc) return rc;
+  PF_CUDA(cudaEventSynchronize(c->ev_snap[1]));
+  c->snap_pending = false;
+  const Geo& g = c->g;
+  const size_t dense = (size_t)(g.m + 2) * (g.n + 2) * g.Z, row = (size_t)(g.m + 2) * sizeof(double);
+  double* dst[4] = {u, v, g.dim == 3 ? w : p, p};
+  for (int f = 0; f < g.dim + 1; f++) {
+    double* d = dst[f];
+    if (!d) continue;
+    const double* s = c->hsnap + f * dense;
+    for (int k = 0; k < g.Z; k++)
+      for (int j = 0; j < g.n + 2; j++)
+        std::memcpy(d + (size_t)ld1 * ((size_t)j + (size_t)ld2 * k), s + (size_t)(g.m + 2) * (j + (size_t)(g.n + 2) * k),
+                    row);
+  }
+  return PF_OK;
+}
+
 int pf_get_porosity(pf_case* c, double* poro, int ld1, int ld2) {
   if (!c || !poro) return fail(PF_E_INVALID, "null argument");
   int rc = check_ld(c, ld1, ld2);
@@ -637,6 +700,28 @@ int pf_norms(pf_case* c, double* max_div, double* sor_error) {
   if (sor_error) *sor_error = e;
   if (max_div) *max_div = d;
   if (!std::isfinite(d)) return fail(PF_E_NONFINITE, "max|div u| is not finite");
+  return PF_OK;
+}
+
+int pf_forces(pf_case* c, double force_p[3], double force_v[3]) {
+  if (!c || !force_p || !force_v) return fail(PF_E_INVALID, "pf_forces: null argument");
+  const Geo& g = c->g;
+  const int b = c->cur;
+  // scratch: the staging array, (m+2)(n+2)[(l+2)] doubles >= 6 per 256 cells + 6
+  const long long cells = (long long)g.m * g.n * (g.dim == 3 ? g.l : 1);
+  const long long nb = (cells + 255) / 256;
+  double* out = c->stage + 6 * nb;
+  launch_forces(g, c->s, c->poro, c->p[0], c->p[1], c->U[b], c->V[b], c->W[b], c->stage, out, c->st);
+  c->launches += 2;
+  int rc = check_launch("pf_forces");
+  if (rc) return rc;
+  double h[6];
+  PF_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  for (int d = 0; d < 3; d++) {
+    force_p[d] = h[d];
+    force_v[d] = h[3 + d];
+  }
   return PF_OK;
 }
 

@@ -138,8 +138,9 @@ __device__ __forceinline__ void passes_smem_2d(const CaseDesc& d, cg::cluster_gr
     cl.sync();  // no CTA pushes into a halo before its owner has zeroed it
     for (int it = 0; it < d.inner; it++) {
       for (int col = 0; col < 2; col++) {
-        for (int x = threadIdx.x; x < nr * hc; x += blockDim.x) {
-          const int lr = 1 + x / hc, h = x - (lr - 1) * hc, j = j0 + lr - 1;
+        // (slot, row) walk without a division per cell
+        for (Walk3 w(threadIdx.x, blockDim.x, hc, nr > 0 ? nr : 1); w.c == 0 && nr > 0; w.next()) {
+          const int h = w.a, lr = 1 + w.b, j = j0 + w.b;
           const int sb = (col + j + 1) & 1, i = 2 * h + sb;
           if (i < 1 || i > m) continue;
           const float eold = E[col][lr * P + h];
@@ -495,7 +496,7 @@ int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
   const size_t nat4 = r256((size_t)g.nat * 4), pk4 = r256((size_t)g.pk * 4);
   const int d = g.dim;
   size_t b = nat8 * (6 + (d == 3) + 2 * d) + pk8 * (2 + 2 * (2 * d + 3));
-  b += r256((size_t)(g.m + 2) * (g.n + 2) * g.Z * 8) + 256;
+  b += r256((size_t)(g.m + 2) * (g.n + 2) * g.Z * 8) + RED_TOTAL * sizeof(unsigned long long);
   if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * 6 + 256;
   *bytes = b;
   return PF_OK;

@@ -33,6 +33,14 @@ struct pf_case {
   cudaEvent_t* ev_cur = nullptr;
   std::vector<double> step_times;  // ms, last profiling session
   int64_t launches = 0;            // kernels launched so far
+  // asynchronous snapshots (pf_snapshot_begin / _wait), allocated on first use:
+  // dense (m+2)(n+2)[(l+2)] copies of u, v, [w,] p on the device and pinned
+  // on the host, drained on a second stream while the case keeps stepping
+  double* snap = nullptr;
+  double* hsnap = nullptr;
+  cudaStream_t st_snap = nullptr;
+  cudaEvent_t ev_snap[2] = {nullptr, nullptr};
+  bool snap_pending = false;
   int64_t graph_kernels[2] = {0, 0};
 
   // ---- mixed precision form (pf_mixed.cu) ----

@@ -69,6 +69,18 @@ __device__ __forceinline__ void block_max_atomic(unsigned long long v, unsigned 
   }
 }
 
+// Warp max straight into the spread slots, without a block barrier: for
+// sweeps whose blocks should retire without waiting for each other.
+__device__ __forceinline__ void warp_max_atomic(unsigned long long v, unsigned long long* out) {
+  unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
+  warp_max64(hi, lo);
+  const unsigned long long r = ((unsigned long long)hi << 32) | lo;
+  if ((threadIdx.x & 31) == 0 && r) {
+    const unsigned wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    atomicMax(out + (wid & (RED_SLOTS - 1)), r);
+  }
+}
+
 // FP32 magnitudes: 32-bit patterns, max into the low 32 bits of *slot.
 __device__ __forceinline__ void block_max_atomic(unsigned v, unsigned long long* slot) {
   __shared__ unsigned red[32];
@@ -299,8 +311,13 @@ __device__ __forceinline__ void c_projection(Geo g, Scal s, const double* __rest
 template <typename T>
 __device__ __forceinline__ void c_initial(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1, int i, int j, int k) {
   const idx_t q = nat_idx(g, i, j, k);
-  u[q] = (T)s.init_u;
-  v[q] = (T)s.init_v;
+  if (s.inflow_poro) {  // ibm_2d_backstep_omp_cpu.f90:615-618
+    u[q] = (T)(s.init_u * s.inflow_poro[q]);
+    v[q] = (T)(s.init_v * s.inflow_poro[q]);
+  } else {
+    u[q] = (T)s.init_u;
+    v[q] = (T)s.init_v;
+  }
   if (g.dim == 3) w[q] = (T)0;
   pref(g, p0, p1, i, j, k) = s.outlet_pressure;
 }
@@ -425,8 +442,13 @@ template <typename T>
 __device__ __forceinline__ void c_bnd_x(const Geo& g, const Scal& s, T* u, T* v, T* w, double* p0, double* p1,
                                         int j, int k) {
   const idx_t q1 = nat_idx(g, 1, j, k), q0 = q1 - 1;
-  u[q1] = (T)s.inlet_u;
-  v[q1] = (T)s.inlet_v;
+  if (s.inflow_poro) {  // ibm_2d_backstep_omp_cpu.f90:533-534
+    u[q1] = (T)(s.inlet_u * s.inflow_poro[q1]);
+    v[q1] = (T)(s.inlet_v * s.inflow_poro[q1]);
+  } else {
+    u[q1] = (T)s.inlet_u;
+    v[q1] = (T)s.inlet_v;
+  }
   u[q0] = u[q1];
   v[q0] = v[q1];
   if (g.dim == 3) {

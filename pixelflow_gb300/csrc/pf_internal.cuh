@@ -69,6 +69,9 @@ struct Scal {
   double dtnu, dtnl;     // dt*nu, dt*(nu+lambda)
   double pgx, pgy, pgz;  // dt/density*0.5/dx, ... (projection)
   float hxf, hyf, hzf, ix2f, iy2f, iz2f, dtf, nuf, lamf, dtnuf, dtnlf, pgxf, pgyf, pgzf;
+  // non-null (the case's natural porosity array): inflow and initial
+  // velocities are scaled by the porosity (the backstep program)
+  const double* inflow_poro;
 };
 
 // The double or float copy of a factor, by the arithmetic type T.
@@ -140,6 +143,11 @@ void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cuda
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);
 void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st);
+// Force-log sums: scratch holds 6 doubles per block of 256 cells; out[0..2]
+// pressure part, out[3..5] friction part (device).  Returns the block count.
+int launch_forces(const Geo& g, const Scal& s, const double* poro, const double* p0, const double* p1,
+                  const double* u, const double* v, const double* w, double* scratch, double* out,
+                  cudaStream_t st);
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
 // staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sor_half(Geo g, Coef<T> C, T*
     packed_item<DIM>(g, t, h, j, k);
     e = c_sor_half<T, DIM, TRACK>(g, C, pc, po, omw, colour, h, j, k);
   }
-  if (TRACK) block_max_atomic(e, err);
+  if (TRACK) warp_max_atomic(e, err);
 }
 
 // Periodic ghost rows (and planes) of p for interior i, as the reference
@@ -267,6 +267,92 @@ __global__ void k_div_diag(Geo g, Scal s, const T* __restrict__ u, const T* __re
     e = abs_bits(fma(po[q], sd, sg));
   }
   block_max_atomic(e, out);
+}
+
+// Force sums of the reference's force log (output.f90:244-305 2D,
+// :1090-1165 3D): per cell the pressure part
+//   -vol p 2 eps (1-eps) / (thickness h_d) n_d,  n = grad eps / max(|grad eps|, 1e-6)
+// (central differences x 0.5) and the wall-friction part
+//   vol alpha rho nu (eps (1-eps) / (thickness h_d))^2 u_d,  alpha = 32.
+// Fluid cells (eps (1-eps) == 0) skip the normal (a square root and
+// divisions in FP64) but still multiply their zero factors by p and u, so a
+// non-finite field still makes the sums non-finite, as in the reference.
+// Each block writes its six sums to part[6*block]; k_forces_sum adds the
+// blocks in a fixed order, so the result does not depend on scheduling.
+constexpr int FORCE_THREADS = 256;
+
+__device__ __forceinline__ double block_sum_fixed(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += sh[w];
+  return r;  // valid in thread 0
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(FORCE_THREADS) k_forces(Geo g, Scal s, const double* __restrict__ po,
+                                                          const double* __restrict__ p0,
+                                                          const double* __restrict__ p1,
+                                                          const double* __restrict__ u,
+                                                          const double* __restrict__ v,
+                                                          const double* __restrict__ w, double* __restrict__ part) {
+  __shared__ double sh[FORCE_THREADS / 32];
+  const long long t = (long long)blockIdx.x * FORCE_THREADS + threadIdx.x;
+  const long long cells = (long long)g.m * g.n * (DIM == 3 ? g.l : 1);
+  double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (t < cells) {
+    const int i = (int)(t % g.m) + 1;
+    const long long r = t / g.m;
+    const int j = (int)(r % g.n) + 1;
+    const int k = DIM == 3 ? (int)(r / g.n) + 1 : 0;
+    const idx_t q = nat_idx(g, i, j, k);
+    const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
+    const double e = po[q], ee = e * (1.0 - e);
+    double fp[3] = {0.0, 0.0, 0.0}, fv[3] = {0.0, 0.0, 0.0};
+    if (ee != 0.0) {
+      const double small = 1.e-6, alpha = 32.0, th = s.thickness;
+      const double gx = (po[q + 1] - po[q - 1]) * 0.5, gy = (po[q + X] - po[q - X]) * 0.5;
+      const double gz = DIM == 3 ? (po[q + XY] - po[q - XY]) * 0.5 : 0.0;
+      const double na = fmax(sqrt(gx * gx + gy * gy + gz * gz), small);
+      const double vol = DIM == 3 ? s.dx * s.dy * s.dz : s.dx * s.dy;
+      const double cp = -vol * 2.0 * e * (1.0 - e);
+      const double cv = vol * alpha * s.density * s.xnue;
+      const double h[3] = {s.dx, s.dy, s.dz}, gn[3] = {gx, gy, gz};
+#pragma unroll
+      for (int d = 0; d < DIM; d++) {
+        const double td = ee / (th * h[d]);
+        fp[d] = cp / (th * h[d]) * (gn[d] / na);
+        fv[d] = cv * (td * td);
+      }
+    }
+    const double pc = pref(g, p0, p1, i, j, k);
+    f[0] = fp[0] * pc;
+    f[1] = fp[1] * pc;
+    f[3] = fv[0] * u[q];
+    f[4] = fv[1] * v[q];
+    if (DIM == 3) {
+      f[2] = fp[2] * pc;
+      f[5] = fv[2] * w[q];
+    }
+  }
+  for (int c = 0; c < 6; c++) {
+    const double r = block_sum_fixed(f[c], sh);
+    if (threadIdx.x == 0) part[6 * (long long)blockIdx.x + c] = r;
+  }
+}
+
+__global__ void k_forces_sum(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double sh[FORCE_THREADS / 32];
+  for (int c = 0; c < 6; c++) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += FORCE_THREADS) v += part[6 * (long long)b + c];
+    const double r = block_sum_fixed(v, sh);
+    if (threadIdx.x == 0) out[c] = r;
+  }
 }
 
 // staging <-> layouts ---------------------------------------------------
@@ -578,6 +664,19 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
     else
       k_sor_dc4<2, false><<<blocks, DC4_THREADS, 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
   }
+}
+
+int launch_forces(const Geo& g, const Scal& s, const double* poro, const double* p0, const double* p1,
+                  const double* u, const double* v, const double* w, double* scratch, double* out,
+                  cudaStream_t st) {
+  const long long cells = (long long)g.m * g.n * (g.dim == 3 ? g.l : 1);
+  const int nb = (int)((cells + FORCE_THREADS - 1) / FORCE_THREADS);
+  if (g.dim == 3)
+    k_forces<3><<<nb, FORCE_THREADS, 0, st>>>(g, s, poro, p0, p1, u, v, w, scratch);
+  else
+    k_forces<2><<<nb, FORCE_THREADS, 0, st>>>(g, s, poro, p0, p1, u, v, w, scratch);
+  k_forces_sum<<<1, FORCE_THREADS, 0, st>>>(scratch, nb, out);
+  return nb;
 }
 
 void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st) {

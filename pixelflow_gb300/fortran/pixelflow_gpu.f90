@@ -16,7 +16,7 @@ module pixelflow_gpu
     real(c_double) :: inlet_velocity, outlet_pressure, aoa
     integer(c_int32_t) :: istep_max, iter_max
     real(c_double) :: thickness, threshold, relux_factor
-    integer(c_int32_t) :: nonslip, reserved
+    integer(c_int32_t) :: nonslip, inflow_porosity
   end type pf_params
 
   type, bind(C) :: pf_options
@@ -89,6 +89,24 @@ module pixelflow_gpu
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: h
       real(c_double), intent(out) :: max_div, sor_error
+    end function
+
+    integer(c_int) function pf_forces(h, force_p, force_v) bind(C, name="pf_forces")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: force_p(3), force_v(3)
+    end function
+
+    integer(c_int) function pf_snapshot_begin(h) bind(C, name="pf_snapshot_begin")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    integer(c_int) function pf_snapshot_wait(h, u, v, w, p, ld1, ld2) bind(C, name="pf_snapshot_wait")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: u(*), v(*), w(*), p(*)
+      integer(c_int), value :: ld1, ld2
     end function
 
     type(c_ptr) function pf_last_error() bind(C, name="pf_last_error")

@@ -31,7 +31,8 @@ def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
     l = int(shape[2]) if dim == 3 else 1
     return PfParams(dim, m, n, l, s.xnue, s.xlambda, s.density, s.width, s.height, s.depth, s.time,
                     s.inlet_velocity, s.outlet_pressure, s.aoa, int(s.istep_max), int(s.iter_max),
-                    s.thickness, s.threshold, s.relux_factor, 1 if s.nonslip else 0, 0)
+                    s.thickness, s.threshold, s.relux_factor, 1 if s.nonslip else 0,
+                    1 if s.inflow_porosity else 0)
 
 
 def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
@@ -143,6 +144,32 @@ class Case:
 
     def step(self, nsteps: int = 1):
         check(self.L.pf_step(self.h, int(nsteps)))
+        self.steps_done = getattr(self, "steps_done", 0) + int(nsteps)
+
+    # -- checkpoint / restart ------------------------------------------------
+    def save_checkpoint(self, path: str):
+        """Everything a restart needs, in one .npz: the settings, the grid,
+        the porosity values, the state with its ghost layers (the next step
+        reads the lagged ghosts) and the number of steps taken.  A case
+        restored from it continues bit for bit as the original would."""
+        import dataclasses
+        import json
+        st = self.get_state()
+        por = self.porosity()
+        inner = por[1:-1, 1:-1] if self.dim == 2 else por[1:-1, 1:-1, 1:-1]
+        np.savez(path, settings=json.dumps(dataclasses.asdict(self.settings)),
+                 shape=np.array(self.shape), porosity=inner, steps_done=getattr(self, "steps_done", 0), **st)
+
+    @classmethod
+    def from_checkpoint(cls, path: str, **kw) -> "Case":
+        import json
+        with np.load(path, allow_pickle=False) as z:
+            s = Settings(**json.loads(str(z["settings"])))
+            shape = tuple(int(x) for x in z["shape"])
+            self = cls(s, shape, z["porosity"], **kw)
+            self.set_state(z["u"], z["v"], z["p"], z["w"] if "w" in z.files else None)
+            self.steps_done = int(z["steps_done"])
+        return self
 
     def synchronize(self):
         check(self.L.pf_synchronize(self.h))
@@ -180,10 +207,44 @@ class Case:
                                   ld1, ld2))
         return out
 
+    def snapshot_begin(self):
+        """Start copying the state as of the last enqueued step to the host
+        without waiting (the copy overlaps the steps enqueued after it)."""
+        check(self.L.pf_snapshot_begin(self.h))
+
+    def snapshot_wait(self, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        """The state captured by the last snapshot_begin (waits for its copy)."""
+        if out is None:
+            out = {k: np.empty(self.field_shape) for k in (("u", "v", "p") + (("w",) if self.dim == 3 else ()))}
+        ld1, ld2 = self._check_field(out["u"])
+        check(self.L.pf_snapshot_wait(self.h, _ptr(out["u"]), _ptr(out["v"]), _ptr(out.get("w")), _ptr(out["p"]),
+                                      ld1, ld2))
+        return out
+
     def porosity(self) -> np.ndarray:
         a = np.empty(self.field_shape)
         check(self.L.pf_get_porosity(self.h, _ptr(a), a.shape[-1], a.shape[-2]))
         return a
+
+    def forces(self, radius: Optional[float] = None) -> Dict[str, np.ndarray]:
+        """The reference's force log (output_force_log_2d/_3d): pressure part
+        Fp, wall-friction part Fv and F = Fp + Fv (x, y[, z]); with `radius`
+        also the coefficients F/(density * inlet_velocity^2 * radius) as
+        Cd, Cl (2D) or Cd_x, Cl, Cd_z (3D)."""
+        fp = (ctypes.c_double * 3)()
+        fv = (ctypes.c_double * 3)()
+        check(self.L.pf_forces(self.h, fp, fv))
+        d = self.dim
+        out = {"Fp": np.array(fp[:d]), "Fv": np.array(fv[:d])}
+        out["F"] = out["Fp"] + out["Fv"]
+        if radius is not None:
+            ref = self.settings.density * self.settings.inlet_velocity ** 2 * radius
+            c = out["F"] / ref
+            if d == 2:
+                out["Cd"], out["Cl"] = float(c[0]), float(c[1])
+            else:
+                out["Cd_x"], out["Cl"], out["Cd_z"] = float(c[0]), float(c[1]), float(c[2])
+        return out
 
     def kernel_launches(self) -> int:
         n = ctypes.c_int64()

@@ -118,3 +118,10 @@ def test_batch_launch_is_persistent_one_per_dimension():
         n0 = b.kernel_launches()
         b.step(3)
         assert b.kernel_launches() - n0 == 2  # one 2D launch + one 3D launch for 3 steps of 5 cases
+
+
+def test_admission_bytes_equal_the_allocation():
+    """The admission estimate (pf_case_bytes) is the case's real allocation."""
+    for (s, shape, vals) in _cases():
+        with Case(s.replace(precision="mixed"), shape, vals) as c:
+            assert c.memory_bytes() == case_bytes(s, shape), shape

@@ -254,3 +254,73 @@ def test_mixed_precision_error_against_fp64(dim):
     print(f"mixed vs fp64 {dim}D {shape}: after 1 step {e1}, after {steps} steps {e}")
     assert e1["vel"] < 1e-6 and e1["p"] < 1e-5, e1
     assert e["vel"] < 1e-6 and e["p"] < pbound, e
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_force_log_matches_oracle(dim, precision):
+    """pf_forces against the oracle's force sums on the GPU's own state (so
+    only the reduction is compared), to rounding of the summation order, and
+    reproducible bit for bit from call to call."""
+    from oracle import np_oracle
+    if dim == 2:
+        s = G.settings_cylinder_2d(iter_max=40, precision=precision)
+        shape, vals = (128, 64), G.cylinder_2d(128, 64, radius=0.2, cx=0.6, cy=0.5)
+    else:
+        s = G.settings_spheres_3d(iter_max=20, precision=precision)
+        shape, vals = (40, 36, 32), G.spheres_3d(40, 36, 32, count=4, seed=2)
+    with Case(s, shape, vals) as c:
+        c.initial_conditions()
+        c.step(5)
+        f1 = c.forces(radius=0.2)
+        f2 = c.forces(radius=0.2)
+        st = c.get_state()
+        por = c.porosity()
+    o = OracleCase(s.replace(precision="fp64"), shape, vals.ravel())
+    sc = o.scalars()
+    bp, bv, mag = np_oracle.forces(por, st["p"], st["u"], st["v"], st.get("w"), sc["dx"], sc["dy"], sc["dz"],
+                                   s.thickness, s.density, s.xnue)
+    got = np.r_[f1["Fp"], f1["Fv"]]
+    want = np.r_[bp[:dim], bv[:dim]]
+    scale = np.r_[mag[:dim], mag[3:3 + dim]]
+    assert np.all(np.abs(got - want) <= 1e-12 * np.maximum(scale, 1e-300)), (got, want)
+    for k in f1:
+        assert np.array_equal(np.asarray(f1[k]), np.asarray(f2[k])), k
+    key = "Cd" if dim == 2 else "Cd_x"
+    assert np.isfinite(f1[key])
+
+
+@pytest.mark.parametrize("shape,steps", [((64, 32), 40), ((63, 33), 30), ((24, 20, 16), 10)])
+def test_backstep_inflow_parity(shape, steps):
+    """The backstep program (inflow and initial velocities times porosity,
+    ibm_2d_backstep_omp_cpu.f90:533-534, 615-618) against the oracle, with an
+    obstacle across the inlet so the inflow profile is not uniform; the batch
+    kernel gives the single-case bits for the same settings."""
+    from pixelflow_gb300.batch import Batch
+    dim = len(shape)
+    if dim == 2:
+        s = G.settings_cylinder_2d(iter_max=30, inflow_porosity=True)
+        vals = np.minimum(G.cylinder_2d(*shape, radius=0.15, cx=0.6, cy=0.5),
+                          G.cylinder_2d(*shape, radius=0.3, cx=0.0, cy=0.3))
+    else:
+        s = G.settings_spheres_3d(iter_max=20, inflow_porosity=True)
+        vals = G.spheres_3d(*shape, spheres=np.array([[0.0, 0.5, 0.5, 0.3], [0.6, 0.4, 0.5, 0.2]]))
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        u0 = c.get_state()["u"]
+        c.step(steps)
+        got = c.get_state()
+    inlet = (slice(1, -1), 1) if dim == 2 else (slice(1, -1), slice(1, -1), 1)
+    assert np.array_equal(u0[inlet], ref.u[inlet])
+    ref.step(steps)
+    e = errors(got, ref, dim)
+    assert e["vel"] < 1e-11 and e["p"] < 1e-11, e
+    sm = s.replace(precision="mixed")
+    with Case(sm, shape, vals) as one, Batch(cluster=2, threads=256) as b:
+        one.initial_conditions()
+        one.step(3)
+        slot = b.add(sm, shape, vals)
+        b.step(3)
+        a, bb = one.get_state(), b.get_state(slot)
+        assert all(np.array_equal(a[k], bb[k]) for k in a)
