@@ -57,6 +57,13 @@ typedef struct pf_params {
   int32_t inflow_porosity; /* 1: inflow and initial velocities scaled by the
                               porosity, as ibm_2d_backstep_omp_cpu.f90 does
                               (:533-534, :615-618); 0: the uniform programs */
+  int32_t wall_mode;       /* 1 (3D, plain FP64 only): the air-condition
+                              program, ibm_3d_air_condition_omp_cpu.f90 --
+                              walls on all six faces by the table below,
+                              non-periodic ghosts; 0: the uniform programs */
+  int32_t walls[6];        /* wall table, faces top, bottom, east, west,
+                              north, south (:10-15): 0 wall, 1 inlet (where
+                              porosity >= 0.9), 2 outlet (where >= 0.9) */
 } pf_params;
 
 /* Options that only this library reads (the &gpu_control group). */

@@ -35,6 +35,10 @@ class NpCase:
         self.nonslip, self.iter_max = bool(s.nonslip), int(s.iter_max)
         # backstep program: inflow and initial velocity times porosity
         self.inflow_porosity = bool(getattr(s, "inflow_porosity", False))
+        # air-condition program: wall table (top, bottom, east, west, north, south)
+        walls = getattr(s, "walls", None)
+        self.wall_mode = self.dim == 3 and walls is not None
+        self.walls = tuple(int(x) for x in walls) if self.wall_mode else None
         # grid.f90:50-52 / :297-300
         self.dx = T(s.width) / T(m - 1)
         self.dy = T(s.height) / T(n - 1)
@@ -49,6 +53,14 @@ class NpCase:
             po[1:n + 2, m + 1] = po[1:n + 2, m]
             po[0, :] = po[n, :]
             po[n + 1, :] = po[1, :]
+        elif self.wall_mode:  # grid_conditions_wall (grid.f90:208-244): copies x, y, z
+            po[1:l + 1, 1:n + 1, 1:m + 1] = vals
+            po[:, :, 0] = po[:, :, 1]
+            po[:, :, m + 1] = po[:, :, m]
+            po[:, 0, :] = po[:, 1, :]
+            po[:, n + 1, :] = po[:, n, :]
+            po[0, :, :] = po[1, :, :]
+            po[l + 1, :, :] = po[l, :, :]
         else:
             po[1:l + 1, 1:n + 1, 1:m + 1] = vals
             po[1:l + 2, 1:n + 2, 0] = po[1:l + 2, 1:n + 2, 1]
@@ -75,6 +87,12 @@ class NpCase:
                 self.u[I] = self.u[I] * self.poro[I]
                 self.v[I] = self.v[I] * self.poro[I]
             self.p[I] = self.pout
+        elif self.wall_mode:  # air-condition initial_conditions: at rest, p = outlet
+            I = (slice(1, self.l + 1), slice(1, self.n + 1), slice(1, self.m + 1))
+            self.u[I] = T(0)
+            self.v[I] = T(0)
+            self.w[I] = T(0)
+            self.p[I] = self.pout
         else:
             I = (slice(1, self.l + 1), slice(1, self.n + 1), slice(1, self.m + 1))
             self.u[I] = self.U * T(np.cos(self.aoa / T(360) * pi))
@@ -86,7 +104,49 @@ class NpCase:
             self.p[I] = self.pout
         self.boundary()
 
+    def _wall_boundary(self):
+        """boundary() of the air-condition program, face by face (top, bottom,
+        west, east, north, south), whole faces at once."""
+        T = self.T
+        u, v, w, p, po = self.u, self.v, self.w, self.p, self.poro
+        m, n, l = self.m, self.n, self.l
+        lim, U, pout = T(0.9), self.U, self.pout
+        # (face index in the table, face slice, ghost slice, inner slice, inlet sign,
+        #  inlet component, mirrored component, outlet copies the inner (True) or face plane)
+        faces = [
+            (0, (l,), (l + 1,), (l - 1,), -1, "w", "w", True),
+            (1, (1,), (0,), (2,), 1, "w", "w", False),
+            (3, (slice(None), slice(None), 1), (slice(None), slice(None), 0), (slice(None), slice(None), 2),
+             1, "u", "u", False),
+            (2, (slice(None), slice(None), m), (slice(None), slice(None), m + 1), (slice(None), slice(None), m - 1),
+             -1, "u", "u", False),
+            (4, (slice(None), n), (slice(None), n + 1), (slice(None), n - 1), -1, "u", "u", False),
+            (5, (slice(None), 1), (slice(None), 0), (slice(None), 2), 1, "u", "v", True),
+        ]
+        F = {"u": u, "v": v, "w": w}
+        for (idx, fs, gs, bs, sign, incomp, mirror, out_inner) in faces:
+            t = self.walls[idx]
+            pf = po[(l,)] if (idx == 1) else po[fs]  # the bottom inlet tests the top plane
+            inlet = (t == 1) & (pf >= lim)
+            outlet = (t == 2) & (po[fs] >= lim)
+            wall = ~(inlet | outlet)
+            for name, a in F.items():
+                face_val = a[fs].copy()
+                # inlet: the face takes the inflow, the ghost copies the face
+                inl = T(sign) * U if name == incomp else T(0)
+                a[fs] = np.where(inlet, inl, np.where(wall, T(0), face_val))
+                src = a[bs] if out_inner else a[fs]
+                g_old = a[gs].copy()
+                g_new = np.where(inlet, a[fs], np.where(outlet, src, g_old))
+                if name == mirror:
+                    g_new = np.where(wall, -a[bs], g_new)
+                a[gs] = g_new
+            p[gs] = np.where(outlet, pout, p[bs])
+
     def boundary(self):
+        if self.wall_mode:
+            self._wall_boundary()
+            return
         T = self.T
         m, n, l = self.m, self.n, self.l
         pi = T(np.arctan(T(1.0))) * T(4.0)
@@ -170,6 +230,8 @@ class NpCase:
                                      + (S(wo, 0, 0, 1) - S(wo, 0, 0, -1)) / dz * T(.5))
             div[1:l + 1, 1:n + 1, 0] = 0
             div[1:l + 1, 1:n + 1, m + 1] = 0
+            if self.wall_mode:  # every face ghost stays 0
+                return div
             div[1:l + 1, 0, 1:m + 1] = div[1:l + 1, n, 1:m + 1]
             div[1:l + 1, n + 1, 1:m + 1] = div[1:l + 1, 1, 1:m + 1]
             div[0, 1:n + 1, 1:m + 1] = div[l, 1:n + 1, 1:m + 1]
@@ -260,6 +322,9 @@ class NpCase:
         else:
             C["ap"] = -C["ae"] - C["aw"] - C["an"] - C["as"]
         C["bb"] = bb
+        if self.wall_mode:
+            self._wall_matrix(C)
+            return C
         # boundrary_matrix
         C["ae"][..., 0] = C["ae"][..., 0] + C["aw"][..., 0]
         C["aw"][..., 0] = 0
@@ -269,7 +334,37 @@ class NpCase:
                 C[key][..., -1] = 0
         return C
 
+    def _wall_matrix(self, C):
+        """boundary_matrix of the air-condition program on the interior
+        arrays [k, j, i]: faces top, bottom, east, west, north, south."""
+        T = self.T
+        lim = T(0.9)
+        pc = self._s(self.poro)
+        p = self.p
+        m, n, l = self.m, self.n, self.l
+        bb1 = C["bb"][0].copy()  # plane 1 before any edit (the top outlet starts from it)
+        # (table index, face slice of the interior arrays, outward key, inward key, p ghost slice)
+        faces = [(0, (-1,), "at", "ab", (l + 1, slice(1, n + 1), slice(1, m + 1))),
+                 (1, (0,), "ab", "at", (0, slice(1, n + 1), slice(1, m + 1))),
+                 (2, (slice(None), slice(None), -1), "ae", "aw", (slice(1, l + 1), slice(1, n + 1), m + 1)),
+                 (3, (slice(None), slice(None), 0), "aw", "ae", (slice(1, l + 1), slice(1, n + 1), 0)),
+                 (4, (slice(None), -1), "an", "as", (slice(1, l + 1), n + 1, slice(1, m + 1))),
+                 (5, (slice(None), 0), "as", "an", (slice(1, l + 1), 0, slice(1, m + 1)))]
+        keys = ("ae", "aw", "an", "as", "at", "ab")
+        for (idx, fs, out, inw, gs) in faces:
+            t = self.walls[idx]
+            outlet = (t == 2) & (pc[fs] >= lim)
+            a_out = C[out][fs].copy()
+            C[inw][fs] = np.where(outlet, C[inw][fs], C[inw][fs] + a_out)
+            C[out][fs] = np.where(outlet, C[out][fs], T(0))
+            base = bb1 if idx == 0 else C["bb"][fs]
+            C["bb"][fs] = np.where(outlet, base + a_out * p[gs], C["bb"][fs])
+            for k in keys:
+                C[k][fs] = np.where(outlet, T(0), C[k][fs])
+
     def _halo_p(self):
+        if self.wall_mode:  # the air-condition program keeps its ghosts during the sweeps
+            return
         p, m, n, l = self.p, self.m, self.n, self.l
         if self.dim == 2:
             p[0, 1:m + 1] = p[n, 1:m + 1]

@@ -28,6 +28,8 @@
  * Reference files (paths inside nobu-n2002/PixelFlow):
  *   2D: src/omp_parallel/ibm_2d_uniform_omp_cpu.f90
  *   3D: src/omp_parallel/ibm_3d_uniform_omp_cpu.f90
+ *   3D with the wall table (wall_mode = 1):
+ *       src/omp_parallel/ibm_3d_air_condition_omp_cpu.f90
  *   grid: src/omp_parallel/lib/grid.f90, divergence: lib/output.f90
  */
 #include <math.h>
@@ -53,6 +55,8 @@ typedef struct or_params {
   int32_t istep_max, iter_max;
   double thickness, threshold, relux_factor;
   int32_t nonslip, inflow_porosity;
+  int32_t wall_mode;  /* 1: the air-condition program (3D) */
+  int32_t walls[6];   /* top, bottom, east, west, north, south: 0 wall, 1 inlet, 2 outlet */
 } or_params;
 
 typedef struct F(or_ctx) {
@@ -62,6 +66,7 @@ typedef struct F(or_ctx) {
   REAL dx, dy, dz, dt;
   int nonslip, iter_max, istep_max;
   int inflow_porosity;   /* backstep program: inflow/initial velocity x porosity */
+  int wall_mode, walls[6];
   const REAL *poro;      /* porosity of the case (set by or_grid_conditions) */
   size_t ncell; /* (m+2)(n+2)[(l+2)] */
   /* solve_p locals (static in the reference through -fno-automatic) */
@@ -99,6 +104,8 @@ CTX *F(or_create)(const or_params *P) {
   c->relux = R(P->relux_factor);
   c->nonslip = P->nonslip;
   c->inflow_porosity = P->inflow_porosity;
+  c->wall_mode = (P->dim == 3) ? P->wall_mode : 0;
+  for (int f = 0; f < 6; f++) c->walls[f] = P->walls[f];
   c->iter_max = P->iter_max;
   c->istep_max = P->istep_max;
   /* grid.f90:50-52 (2D), :297-300 (3D) */
@@ -159,6 +166,24 @@ void F(or_grid_conditions)(CTX *c, const double *vals, REAL *poro) {
     for (int k = 1; k <= l; k++)
       for (int j = 1; j <= n; j++)
         for (int i = 1; i <= m; i++) poro[I3(i, j, k)] = rmax(R(vals[q++]), c->threshold);
+    if (c->wall_mode) { /* grid_conditions_wall, grid.f90:208-244: copies, x then y then z */
+      for (int j = 0; j <= n + 1; j++)
+        for (int k = 0; k <= l + 1; k++) {
+          poro[I3(0, j, k)] = poro[I3(1, j, k)];
+          poro[I3(m + 1, j, k)] = poro[I3(m, j, k)];
+        }
+      for (int i = 0; i <= m + 1; i++)
+        for (int k = 0; k <= l + 1; k++) {
+          poro[I3(i, 0, k)] = poro[I3(i, 1, k)];
+          poro[I3(i, n + 1, k)] = poro[I3(i, n, k)];
+        }
+      for (int i = 0; i <= m + 1; i++)
+        for (int j = 0; j <= n + 1; j++) {
+          poro[I3(i, j, 0)] = poro[I3(i, j, 1)];
+          poro[I3(i, j, l + 1)] = poro[I3(i, j, l)];
+        }
+      return;
+    }
     for (int j = 1; j <= n + 1; j++)
       for (int k = 1; k <= l + 1; k++) {
         poro[I3(0, j, k)] = poro[I3(1, j, k)];
@@ -179,8 +204,107 @@ void F(or_grid_conditions)(CTX *c, const double *vals, REAL *poro) {
 
 /* ------------------------------------------------------------------ */
 /* boundary: 2D ibm_2d_uniform_omp_cpu.f90:460-538, 3D ibm_3d:669-752 */
+/* boundary() of the air-condition program (:873-1170): faces in the order
+   top, bottom, west, east, north, south over the ghost-inclusive ranges, each
+   a wall, an inlet or an outlet by the wall table, inlet and outlet applying
+   where the face cell's porosity is >= 0.9 (the bottom inlet tests the top
+   plane's porosity, as the reference does).  Walls zero the face velocity and
+   mirror one component into the ghost, which component by face as written. */
+static void F(wall_boundary)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
+  const int m = c->m, n = c->n, l = c->l;
+  const REAL *po = c->poro, lim = R(0.9), U = c->inlet_velocity, pout = c->outlet_pressure;
+  for (int i = 0; i <= m + 1; i++) /* top */
+    for (int j = 0; j <= n + 1; j++) {
+      const size_t f = I3(i, j, l), g = I3(i, j, l + 1), b = I3(i, j, l - 1);
+      const int t = c->walls[0];
+      if (t == 1 && po[f] >= lim) {
+        u[f] = R(0.); v[f] = R(0.); w[f] = -U;
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[b]; v[g] = v[b]; w[g] = w[b]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        w[g] = -w[b]; p[g] = p[b];
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* bottom */
+    for (int j = 0; j <= n + 1; j++) {
+      const size_t f = I3(i, j, 1), g = I3(i, j, 0), b = I3(i, j, 2);
+      const int t = c->walls[1];
+      if (t == 1 && po[I3(i, j, l)] >= lim) {
+        u[f] = R(0.); v[f] = R(0.); w[f] = U;
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        w[g] = -w[b]; p[g] = p[b];
+      }
+    }
+  for (int j = 0; j <= n + 1; j++) /* west */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t f = I3(1, j, k), g = I3(0, j, k), b = I3(2, j, k);
+      const int t = c->walls[3];
+      if (t == 1 && po[f] >= lim) {
+        u[f] = U; v[f] = R(0.); w[f] = R(0.);
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        u[g] = -u[b]; p[g] = p[b];
+      }
+    }
+  for (int j = 0; j <= n + 1; j++) /* east */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t f = I3(m, j, k), g = I3(m + 1, j, k), b = I3(m - 1, j, k);
+      const int t = c->walls[2];
+      if (t == 1 && po[f] >= lim) {
+        u[f] = -U; v[f] = R(0.); w[f] = R(0.);
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        u[g] = -u[b]; p[g] = p[b];
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* north */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t f = I3(i, n, k), g = I3(i, n + 1, k), b = I3(i, n - 1, k);
+      const int t = c->walls[4];
+      if (t == 1 && po[f] >= lim) {
+        u[f] = -U; v[f] = R(0.); w[f] = R(0.);
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        u[g] = -u[b]; p[g] = p[b];
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* south */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t f = I3(i, 1, k), g = I3(i, 0, k), b = I3(i, 2, k);
+      const int t = c->walls[5];
+      if (t == 1 && po[f] >= lim) {
+        u[f] = U; v[f] = R(0.); w[f] = R(0.);
+        u[g] = u[f]; v[g] = v[f]; w[g] = w[f]; p[g] = p[b];
+      } else if (t == 2 && po[f] >= lim) {
+        u[g] = u[b]; v[g] = v[b]; w[g] = w[b]; p[g] = pout;
+      } else {
+        u[f] = R(0.); v[f] = R(0.); w[f] = R(0.);
+        v[g] = -v[b]; p[g] = p[b];
+      }
+    }
+}
+
 void F(or_boundary)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
   const int m = c->m, n = c->n, l = c->l;
+  if (c->wall_mode) {
+    F(wall_boundary)(c, p, u, v, w);
+    return;
+  }
   if (c->dim == 2) {
     const REAL pai = (REAL)atan(R(1.)) * R(4.);
     for (int j = 1; j <= n; j++) {
@@ -280,6 +404,15 @@ void F(or_initialize)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
         }
         p[I2(i, j)] = c->outlet_pressure;
       }
+  } else if (c->wall_mode) { /* air-condition initial_conditions (:1174-1209) */
+    for (int k = 1; k <= l; k++)
+      for (int j = 1; j <= n; j++)
+        for (int i = 1; i <= m; i++) {
+          u[I3(i, j, k)] = R(0.);
+          v[I3(i, j, k)] = R(0.);
+          w[I3(i, j, k)] = R(0.);
+          p[I3(i, j, k)] = c->outlet_pressure;
+        }
   } else {
     const REAL pi = (REAL)atan(R(1.)) * R(4.);
     for (int k = 1; k <= l; k++)
@@ -333,6 +466,19 @@ void F(or_divergence)(CTX *c, const REAL *uo, const REAL *vo, const REAL *wo) {
         div[I3(0, j, k)] = R(0.);
         div[I3(m + 1, j, k)] = R(0.);
       }
+    if (c->wall_mode) { /* air-condition :210-238: every face ghost 0 */
+      for (int j = 1; j <= n; j++)
+        for (int i = 1; i <= m; i++) {
+          div[I3(i, j, 0)] = R(0.);
+          div[I3(i, j, l + 1)] = R(0.);
+        }
+      for (int k = 1; k <= l; k++)
+        for (int i = 1; i <= m; i++) {
+          div[I3(i, 0, k)] = R(0.);
+          div[I3(i, n + 1, k)] = R(0.);
+        }
+      return;
+    }
 #pragma omp parallel for
     for (int k = 1; k <= l; k++)
       for (int i = 1; i <= m; i++) {
@@ -555,8 +701,98 @@ void F(or_coefficients)(CTX *c, const REAL *u, const REAL *v, const REAL *w, con
 }
 
 /* boundrary_matrix: 2D :410-454, 3D :618-663 (omp semantics). */
+/* boundary_matrix of the air-condition program (:665-867), face by face in
+   the reference's order over the ghost-inclusive ranges: a wall (or an inlet)
+   folds the outward coefficient into the inward one (dp/dn = 0); an outlet
+   cell with porosity >= 0.9 adds a_out * p_ghost to bb and zeroes all six
+   coefficients (the top outlet starts from bb of plane 1, as the reference
+   writes it). */
+static void F(wall_matrix)(CTX *c, const REAL *p) {
+  const int m = c->m, n = c->n, l = c->l;
+  REAL *ae = c->ae, *aw = c->aw, *an = c->an, *as = c->as, *at = c->at, *ab = c->ab, *bb = c->bb;
+  const REAL *po = c->poro, lim = R(0.9);
+#define PF_ZERO6(q) (ae[q] = aw[q] = an[q] = as[q] = at[q] = ab[q] = R(0.))
+  for (int i = 0; i <= m + 1; i++) /* top, k = l */
+    for (int j = 0; j <= n + 1; j++) {
+      const size_t q = I3(i, j, l);
+      const int t = c->walls[0];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        ab[q] = ab[q] + at[q];
+        at[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[I3(i, j, 1)] + at[q] * p[I3(i, j, l + 1)];
+        PF_ZERO6(q);
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* bottom, k = 1 */
+    for (int j = 0; j <= n + 1; j++) {
+      const size_t q = I3(i, j, 1);
+      const int t = c->walls[1];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        at[q] = at[q] + ab[q];
+        ab[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[q] + ab[q] * p[I3(i, j, 0)];
+        PF_ZERO6(q);
+      }
+    }
+  for (int j = 0; j <= n + 1; j++) /* east, i = m */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t q = I3(m, j, k);
+      const int t = c->walls[2];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        aw[q] = aw[q] + ae[q];
+        ae[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[q] + ae[q] * p[I3(m + 1, j, k)];
+        PF_ZERO6(q);
+      }
+    }
+  for (int j = 0; j <= n + 1; j++) /* west, i = 1 */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t q = I3(1, j, k);
+      const int t = c->walls[3];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        ae[q] = ae[q] + aw[q];
+        aw[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[q] + aw[q] * p[I3(0, j, k)];
+        PF_ZERO6(q);
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* north, j = n */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t q = I3(i, n, k);
+      const int t = c->walls[4];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        as[q] = as[q] + an[q];
+        an[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[q] + an[q] * p[I3(i, n + 1, k)];
+        PF_ZERO6(q);
+      }
+    }
+  for (int i = 0; i <= m + 1; i++) /* south, j = 1 */
+    for (int k = 0; k <= l + 1; k++) {
+      const size_t q = I3(i, 1, k);
+      const int t = c->walls[5];
+      if (t == 0 || t == 1 || (t == 2 && po[q] < lim)) {
+        an[q] = an[q] + as[q];
+        as[q] = R(0.);
+      } else if (t == 2) {
+        bb[q] = bb[q] + as[q] * p[I3(i, 0, k)];
+        PF_ZERO6(q);
+      }
+    }
+#undef PF_ZERO6
+}
+
 void F(or_boundary_matrix)(CTX *c, const REAL *p) {
   const int m = c->m, n = c->n, l = c->l;
+  if (c->wall_mode) {
+    F(wall_matrix)(c, p);
+    return;
+  }
   if (c->dim == 2) {
     for (int j = 1; j <= n; j++) {
       c->ae[I2(1, j)] = c->ae[I2(1, j)] + c->aw[I2(1, j)];
@@ -649,14 +885,15 @@ double F(or_sor)(CTX *c, REAL *p) {
     const long mn = (long)m * n, mnl = (long)m * n * l;
     for (int iter = 1; iter <= c->iter_max; iter++) {
       for (int pass = 0; pass < 2; pass++) {
-#pragma omp parallel for
-        for (int i = 1; i <= m; i++)
+        /* the air-condition program has no periodic refresh (:507-526) */
+#pragma omp parallel for if (!c->wall_mode)
+        for (int i = 1; i <= (c->wall_mode ? 0 : m); i++)
           for (int k = 1; k <= l; k++) {
             p[I3(i, 0, k)] = p[I3(i, n, k)];
             p[I3(i, n + 1, k)] = p[I3(i, 1, k)];
           }
-#pragma omp parallel for
-        for (int i = 1; i <= m; i++)
+#pragma omp parallel for if (!c->wall_mode)
+        for (int i = 1; i <= (c->wall_mode ? 0 : m); i++)
           for (int j = 1; j <= n; j++) {
             p[I3(i, j, 0)] = p[I3(i, j, l)];
             p[I3(i, j, l + 1)] = p[I3(i, j, 1)];
@@ -697,18 +934,20 @@ double F(or_sor)(CTX *c, REAL *p) {
             error = rmax(error, d);
           }
     }
+    if (!c->wall_mode) {
 #pragma omp parallel for
-    for (int i = 1; i <= m; i++)
-      for (int k = 1; k <= l; k++) {
-        p[I3(i, 0, k)] = p[I3(i, n, k)];
-        p[I3(i, n + 1, k)] = p[I3(i, 1, k)];
-      }
+      for (int i = 1; i <= m; i++)
+        for (int k = 1; k <= l; k++) {
+          p[I3(i, 0, k)] = p[I3(i, n, k)];
+          p[I3(i, n + 1, k)] = p[I3(i, 1, k)];
+        }
 #pragma omp parallel for
-    for (int i = 1; i <= m; i++)
-      for (int j = 1; j <= n; j++) {
-        p[I3(i, j, 0)] = p[I3(i, j, l)];
-        p[I3(i, j, l + 1)] = p[I3(i, j, 1)];
-      }
+      for (int i = 1; i <= m; i++)
+        for (int j = 1; j <= n; j++) {
+          p[I3(i, j, 0)] = p[I3(i, j, l)];
+          p[I3(i, j, l + 1)] = p[I3(i, j, 1)];
+        }
+    }
   }
   c->last_error = error;
   return (double)error;

@@ -30,7 +30,8 @@ GROUPS = {
     "solver_control": ["iter_max", "relux_factor"],
 }
 GPU_GROUP = "gpu_control"
-GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity"]
+GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls"]
+WALL_FACES = ("top", "bottom", "east", "west", "north", "south")
 
 
 @dataclasses.dataclass
@@ -68,6 +69,12 @@ class Settings:
     # inflow and initial velocities scaled by porosity: the boundary and initial
     # conditions of ibm_2d_backstep_omp_cpu.f90 (:533-534, :615-618)
     inflow_porosity: bool = False
+    # the air-condition program (3D): its wall table, one entry per face in the
+    # order top, bottom, east, west, north, south, each 0 wall, 1 inlet,
+    # 2 outlet (ibm_3d_air_condition_omp_cpu.f90:4-16); None: the uniform
+    # programs' x inflow/outflow with periodic y and z.  In a namelist:
+    # walls = "1,0,0,0,0,2".
+    walls: Optional[Tuple[int, ...]] = None
 
     def replace(self, **kw) -> "Settings":
         return dataclasses.replace(self, **kw)
@@ -141,10 +148,23 @@ def read_settings(path: str) -> Settings:
             if k not in GPU_KEYS:
                 raise ValueError(f"{path}: &{GPU_GROUP} has no member {k!r}")
             setattr(s, k, v)
+    if isinstance(s.walls, str):
+        s.walls = parse_walls(s.walls)
     s.nonslip = bool(s.nonslip)
     s.istep_max = int(s.istep_max)
     s.iter_max = int(s.iter_max)
     return s
+
+
+def parse_walls(text: str) -> Optional[Tuple[int, ...]]:
+    """"1,0,0,0,0,2" -> (1, 0, 0, 0, 0, 2); "" -> None."""
+    parts = [x for x in re.split(r"[,\s]+", text.strip()) if x]
+    if not parts:
+        return None
+    vals = tuple(int(x) for x in parts)
+    if len(vals) != 6 or any(v not in (0, 1, 2) for v in vals):
+        raise ValueError(f"walls: six entries of 0, 1 or 2 expected, got {text!r}")
+    return vals
 
 
 def write_settings(path: str, s: Settings, gpu_group: bool = False) -> None:
@@ -154,6 +174,10 @@ def write_settings(path: str, s: Settings, gpu_group: bool = False) -> None:
             return ".true." if v else ".false."
         if isinstance(v, str):
             return f'"{v}"'
+        if v is None:
+            return '""'
+        if isinstance(v, tuple):
+            return '"' + ",".join(str(int(x)) for x in v) + '"'
         if isinstance(v, int):
             return str(v)
         return repr(float(v))

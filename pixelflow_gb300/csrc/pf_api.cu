@@ -49,10 +49,21 @@ int make_geo(const pf_params& p, Geo& g) {
   const long long dense = (long long)(g.m + 2) * (g.n + 2) * g.Z;
   if (g.nat >= (1LL << 31) || g.pk >= (1LL << 31) || dense >= (1LL << 31))
     return fail(PF_E_INVALID, "grid too large: arrays are limited to 2^31 elements");
-  g.jn_n = (g.n % 2 == 0) ? 1 : g.n + 1;
-  g.js_1 = (g.n % 2 == 0) ? g.n : 0;
-  g.kt_l = (g.l % 2 == 0) ? 1 : g.l + 1;
-  g.kb_1 = (g.l % 2 == 0) ? g.l : 0;
+  g.wall = p.wall_mode ? 1 : 0;
+  if (g.wall && p.dim != 3) return fail(PF_E_INVALID, "wall_mode: the air-condition program is 3D");
+  for (int f = 0; g.wall && f < 6; f++)
+    if (p.walls[f] < 0 || p.walls[f] > 2) return fail(PF_E_INVALID, "walls: each entry must be 0, 1 or 2");
+  if (g.wall) {  // non-periodic: the edge rows' neighbours are the ghost rows
+    g.jn_n = g.n + 1;
+    g.js_1 = 0;
+    g.kt_l = g.l + 1;
+    g.kb_1 = 0;
+  } else {
+    g.jn_n = (g.n % 2 == 0) ? 1 : g.n + 1;
+    g.js_1 = (g.n % 2 == 0) ? g.n : 0;
+    g.kt_l = (g.l % 2 == 0) ? 1 : g.l + 1;
+    g.kb_1 = (g.l % 2 == 0) ? g.l : 0;
+  }
   return PF_OK;
 }
 
@@ -75,12 +86,15 @@ int make_scal(const pf_params& p, Scal& s) {
   s.omega = p.relux_factor;
   s.nonslip = p.nonslip ? 1 : 0;
   s.inflow_poro = nullptr;  // set to the case's porosity once it is allocated
+  s.wall_poro = nullptr;
+  for (int f = 0; f < 6; f++) s.walls[f] = p.wall_mode ? p.walls[f] : 0;
   const double pi = std::atan(1.0) * 4.0;
   // boundary(): 2D cos(AoA/180*pi) (ibm_2d:478), 3D cos(AoA/1300*pi) (ibm_3d:695)
   const double ab = p.dim == 3 ? p.aoa / 1300.0 * pi : p.aoa / 180.0 * pi;
   s.inlet_u = p.inlet_velocity * std::cos(ab);
   s.inlet_v = p.inlet_velocity * std::sin(ab);
   s.inlet_w = 0.0;
+  s.inlet_velocity = p.inlet_velocity;
   // initial_conditions(): 2D AoA/180 (ibm_2d:560), 3D AoA/360 (ibm_3d:782)
   const double ai = p.dim == 3 ? p.aoa / 360.0 * pi : p.aoa / 180.0 * pi;
   s.init_u = p.inlet_velocity * std::cos(ai);
@@ -130,6 +144,24 @@ void build_porosity(const Geo& g, double threshold, const double* vals, std::vec
         const double v = vals[q++];
         at(i, j, k) = v > threshold ? v : threshold;
       }
+  if (g.wall) {  // grid_conditions_wall (grid.f90:208-244): copies x, y, z
+    for (int j = 0; j <= n + 1; j++)
+      for (int k = 0; k <= l + 1; k++) {
+        at(0, j, k) = at(1, j, k);
+        at(m + 1, j, k) = at(m, j, k);
+      }
+    for (int i = 0; i <= m + 1; i++)
+      for (int k = 0; k <= l + 1; k++) {
+        at(i, 0, k) = at(i, 1, k);
+        at(i, n + 1, k) = at(i, n, k);
+      }
+    for (int i = 0; i <= m + 1; i++)
+      for (int j = 0; j <= n + 1; j++) {
+        at(i, j, 0) = at(i, j, 1);
+        at(i, j, l + 1) = at(i, j, l);
+      }
+    return;
+  }
   if (g.dim == 2) {
     for (int j = 1; j <= n + 1; j++) {
       at(0, j, 0) = at(1, j, 0);
@@ -246,7 +278,7 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
                                    c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
-  const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
+  const bool halo = periodic_halo(g);
   const double omw = 1.0 - s.omega;
   for (int it = 0; it < c->prm.iter_max; it++) {
     for (int col = 0; col < 2; col++) {
@@ -257,8 +289,8 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
     }
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
-  launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
-  c->launches += 4 + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
+  if (!g.wall) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
+  c->launches += 3 + (g.wall ? 0 : 1) + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
   c->cur = nw;
 }
 
@@ -270,7 +302,7 @@ static void enqueue_projection(pf_case* c) {
 
 static void enqueue_boundary(pf_case* c) {
   const int b = c->cur;
-  c->launches += c->g.dim == 3 ? 3 : 2;
+  c->launches += c->g.wall ? 6 : (c->g.dim == 3 ? 3 : 2);
   launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
 }
 
@@ -382,6 +414,8 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "unknown precision");
   if (rc == PF_OK && c->opt.precision == PF_PREC_MIXED && (c->opt.outer_max < 0 || c->opt.inner_sweeps < 0))
     rc = fail(PF_E_INVALID, "outer_max and inner_sweeps must be >= 0");
+  if (rc == PF_OK && c->g.wall && c->opt.precision != PF_PREC_FP64)
+    rc = fail(PF_E_INVALID, "wall_mode: the air-condition program runs in the plain FP64 form only");
   if (rc != PF_OK) {
     delete c;
     return rc;
@@ -402,6 +436,7 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     return rc;
   }
   c->s.inflow_poro = c->prm.inflow_porosity ? c->poro : nullptr;
+  c->s.wall_poro = c->g.wall ? c->poro : nullptr;
   *out = c;
   return PF_OK;
 }
@@ -476,7 +511,7 @@ int pf_initial_conditions(pf_case* c) {
   PF_CUDA(cudaMemsetAsync(c->p[1], 0, pk, c->st));
   launch_initial<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
   launch_boundary<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
-  c->launches += 1 + (g.dim == 3 ? 3 : 2);
+  c->launches += 1 + (g.wall ? 6 : (g.dim == 3 ? 3 : 2));
   if (c->opt.precision == PF_PREC_MIXED) mixed_sync_from_fp64(c);
   return check_launch("pf_initial_conditions");
 }

@@ -192,8 +192,9 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
   const T dtnu = pick<T>(s.dtnu, s.dtnuf), dtnl = pick<T>(s.dtnl, s.dtnlf);
   const T two = (T)2;
   // div neighbours with the periodic wrap of the y (and z) ghost rows
-  const idx_t jn = (j == g.n) ? q - (idx_t)(g.n - 1) * X : q + X;
-  const idx_t js = (j == 1) ? q + (idx_t)(g.n - 1) * X : q - X;
+  // (walls: the ghost rows, which hold 0)
+  const idx_t jn = (j == g.n && !g.wall) ? q - (idx_t)(g.n - 1) * X : q + X;
+  const idx_t js = (j == 1 && !g.wall) ? q + (idx_t)(g.n - 1) * X : q - X;
   const T dc = div[q], dE = div[q + 1], dW = div[q - 1], dN = div[jn], dS = div[js];
   const T gx = gxa[q], gy = gya[q], rv = rinva[q], dp = dampa[q];
 
@@ -226,8 +227,8 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
     v[q] = sv[q] + (TS)fma(-vc, dp * ix2, t);
   } else {
     const T hz = pick<T>(s.hz, s.hzf), iz2 = pick<T>(s.iz2, s.iz2f);
-    const idx_t kt = (k == g.l) ? q - (idx_t)(g.l - 1) * XY : q + XY;
-    const idx_t kb = (k == 1) ? q + (idx_t)(g.l - 1) * XY : q - XY;
+    const idx_t kt = (k == g.l && !g.wall) ? q - (idx_t)(g.l - 1) * XY : q + XY;
+    const idx_t kb = (k == 1 && !g.wall) ? q + (idx_t)(g.l - 1) * XY : q - XY;
     const T dT = div[kt], dB = div[kb];
     const T gz = gza[q];
     const T ut = uo[q + XY], ub = uo[q - XY], vt = vo[q + XY], vb = vo[q - XY];
@@ -276,18 +277,24 @@ __device__ __forceinline__ void c_rhs(Geo g, Scal s, const T* __restrict__ u, co
                       const double* __restrict__ po, const double* __restrict__ gxa,
                       const double* __restrict__ gya, const double* __restrict__ gza, Coef<double> c0,
                       Coef<double> c1, int i, int j, int k) {
-  const idx_t q = nat_idx(g, i, j, k);
   const idx_t X = g.X, XY = (idx_t)g.X * g.Y;
   const double hx = s.hx, hy = s.hy;
-  double sd = ((double)u[q + 1] - (double)u[q - 1]) * hx;
-  sd = fma((double)v[q + X] - (double)v[q - X], hy, sd);
-  double sg = gxa[q] * (double)u[q];
-  sg = fma(gya[q], (double)v[q], sg);
-  if (DIM == 3) {
-    sd = fma((double)w[q + XY] - (double)w[q - XY], s.hz, sd);
-    sg = fma(gza[q], (double)w[q], sg);
-  }
-  const double bb = s.density * fma(po[q], sd, sg);
+  auto raw = [&](idx_t q) {
+    double sd = ((double)u[q + 1] - (double)u[q - 1]) * hx;
+    sd = fma((double)v[q + X] - (double)v[q - X], hy, sd);
+    double sg = gxa[q] * (double)u[q];
+    sg = fma(gya[q], (double)v[q], sg);
+    if (DIM == 3) {
+      sd = fma((double)w[q + XY] - (double)w[q - XY], s.hz, sd);
+      sg = fma(gza[q], (double)w[q], sg);
+    }
+    return s.density * fma(po[q], sd, sg);
+  };
+  const idx_t q = nat_idx(g, i, j, k);
+  // the air-condition program's top outlet starts from bb of plane 1
+  // (ibm_3d_air_condition_omp_cpu.f90:701)
+  const bool top_copy = DIM == 3 && g.wall && s.walls[0] == 2 && k == g.l && po[q] >= 0.9;
+  const double bb = raw(top_copy ? nat_idx(g, i, j, 1) : q);
   const int c = colour_of(g, i, j, k);
   const Coef<double> C = c ? c1 : c0;
   const idx_t r = pk_idx(g, i >> 1, j, k);
@@ -311,7 +318,11 @@ __device__ __forceinline__ void c_projection(Geo g, Scal s, const double* __rest
 template <typename T>
 __device__ __forceinline__ void c_initial(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1, int i, int j, int k) {
   const idx_t q = nat_idx(g, i, j, k);
-  if (s.inflow_poro) {  // ibm_2d_backstep_omp_cpu.f90:615-618
+  if (g.wall) {  // the air-condition program starts at rest (:1194-1203)
+    u[q] = (T)0;
+    v[q] = (T)0;
+    w[q] = (T)0;
+  } else if (s.inflow_poro) {  // ibm_2d_backstep_omp_cpu.f90:615-618
     u[q] = (T)(s.init_u * s.inflow_poro[q]);
     v[q] = (T)(s.init_v * s.inflow_poro[q]);
   } else {
@@ -461,6 +472,62 @@ __device__ __forceinline__ void c_bnd_x(const Geo& g, const Scal& s, T* u, T* v,
   v[qm] = v[qm - 2];
   if (g.dim == 3) w[qm] = w[qm - 2];
   pref(g, p0, p1, g.m + 1, j, k) = s.outlet_pressure;
+}
+
+// boundary() of the air-condition program (ibm_3d_air_condition_omp_cpu.f90:
+// 873-1170) on one face, FACE = 0 top, 1 bottom, 2 east, 3 west, 4 north,
+// 5 south (the wall table's order), at face coordinates (a, b) over the
+// ghost-inclusive range.  An inlet (table 1) applies where the face cell's
+// porosity is >= 0.9 -- for the bottom face the top plane's, as written --
+// an outlet (2) likewise; everything else is a wall.  The inflow component
+// and sign, the component a wall mirrors into the ghost and whether an
+// outlet ghost copies the face or the inner cell follow each face's code.
+template <int FACE, typename T>
+__device__ __forceinline__ void c_wall_face(const Geo& g, const Scal& s, T* u, T* v, T* w, double* p0,
+                                            double* p1, int a, int b) {
+  const int m = g.m, n = g.n, l = g.l;
+  int fi, fj, fk, gi, gj, gk, bi, bj, bk;
+  int sign, comp, mirror;  // comp, mirror: 0 u, 1 v, 2 w
+  bool out_inner;
+  if (FACE == 0) {
+    fi = gi = bi = a; fj = gj = bj = b; fk = l; gk = l + 1; bk = l - 1;
+    sign = -1; comp = 2; mirror = 2; out_inner = true;
+  } else if (FACE == 1) {
+    fi = gi = bi = a; fj = gj = bj = b; fk = 1; gk = 0; bk = 2;
+    sign = 1; comp = 2; mirror = 2; out_inner = false;
+  } else if (FACE == 2) {
+    fj = gj = bj = a; fk = gk = bk = b; fi = m; gi = m + 1; bi = m - 1;
+    sign = -1; comp = 0; mirror = 0; out_inner = false;
+  } else if (FACE == 3) {
+    fj = gj = bj = a; fk = gk = bk = b; fi = 1; gi = 0; bi = 2;
+    sign = 1; comp = 0; mirror = 0; out_inner = false;
+  } else if (FACE == 4) {
+    fi = gi = bi = a; fk = gk = bk = b; fj = n; gj = n + 1; bj = n - 1;
+    sign = -1; comp = 0; mirror = 0; out_inner = false;
+  } else {
+    fi = gi = bi = a; fk = gk = bk = b; fj = 1; gj = 0; bj = 2;
+    sign = 1; comp = 0; mirror = 1; out_inner = true;
+  }
+  const idx_t qf = nat_idx(g, fi, fj, fk), qg = nat_idx(g, gi, gj, gk), qb = nat_idx(g, bi, bj, bk);
+  const int t = s.walls[FACE];
+  const double pin = s.wall_poro[FACE == 1 ? nat_idx(g, fi, fj, l) : qf];
+  const bool inlet = t == 1 && pin >= 0.9;
+  const bool outlet = t == 2 && s.wall_poro[qf] >= 0.9;
+  T* F[3] = {u, v, w};
+  double& pg = pref(g, p0, p1, gi, gj, gk);
+  if (inlet) {
+    for (int d = 0; d < 3; d++) F[d][qf] = d == comp ? (T)(sign * s.inlet_velocity) : (T)0;
+    for (int d = 0; d < 3; d++) F[d][qg] = F[d][qf];
+    pg = pref(g, p0, p1, bi, bj, bk);
+  } else if (outlet) {
+    const idx_t qs = out_inner ? qb : qf;
+    for (int d = 0; d < 3; d++) F[d][qg] = F[d][qs];
+    pg = s.outlet_pressure;
+  } else {
+    for (int d = 0; d < 3; d++) F[d][qf] = (T)0;
+    F[mirror][qg] = -F[mirror][qb];
+    pg = pref(g, p0, p1, bi, bj, bk);
+  }
 }
 
 // boundary, y faces: periodic ghost rows at column i of plane k.

@@ -78,6 +78,33 @@ __global__ void k_stage_ghost_z(Geo g, double* st) {
   st[i + M * (j + N * (long long)(g.l + 1))] = st[i + M * (j + N * 1LL)];
 }
 
+// grid_conditions_wall (grid.f90:208-244): ghosts copy the adjacent interior
+// plane, x then y then z, over the ghost-inclusive ranges.
+__global__ void k_stage_wall_x(Geo g, double* st) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;  // 0..n+1
+  const int k = blockIdx.y;                               // 0..l+1
+  if (j > g.n + 1) return;
+  const long long M = g.m + 2, N = g.n + 2, r = M * ((long long)j + N * k);
+  st[r] = st[r + 1];
+  st[r + g.m + 1] = st[r + g.m];
+}
+__global__ void k_stage_wall_y(Geo g, double* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // 0..m+1
+  const int k = blockIdx.y;                               // 0..l+1
+  if (i > g.m + 1) return;
+  const long long M = g.m + 2, N = g.n + 2;
+  st[i + M * (0 + N * k)] = st[i + M * (1 + N * k)];
+  st[i + M * (g.n + 1 + N * k)] = st[i + M * (g.n + N * k)];
+}
+__global__ void k_stage_wall_z(Geo g, double* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // 0..m+1
+  const int j = blockIdx.y;                               // 0..n+1
+  if (i > g.m + 1) return;
+  const long long M = g.m + 2, N = g.n + 2;
+  st[i + M * (j + N * 0LL)] = st[i + M * (j + N * 1LL)];
+  st[i + M * (j + N * (long long)(g.l + 1))] = st[i + M * (j + N * (long long)g.l)];
+}
+
 }  // namespace
 
 // Fill c->stage with the clamped, ghost-filled porosity of the shapes.
@@ -98,9 +125,15 @@ int geometry_to_stage(pf_case* c, const pf_shape* shapes, int nshapes, double ed
   PF_CUDA(cudaMemsetAsync(c->stage, 0, (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double), c->st));
   k_shapes_porosity<<<dim3((g.m + 31) / 32, (g.n + 7) / 8, g.dim == 3 ? g.l : 1), dim3(32, 8), 0, c->st>>>(
       g, c->s, d, nshapes, edge, c->prm.threshold, c->stage);
-  k_stage_ghost_x<<<dim3((g.n + 1 + 127) / 128, g.dim == 3 ? g.l + 1 : 1), 128, 0, c->st>>>(g, c->stage);
-  k_stage_ghost_y<<<dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), 128, 0, c->st>>>(g, c->stage);
-  if (g.dim == 3) k_stage_ghost_z<<<dim3((g.m + 2 + 127) / 128, g.n + 2), 128, 0, c->st>>>(g, c->stage);
+  if (g.wall) {
+    k_stage_wall_x<<<dim3((g.n + 2 + 127) / 128, g.l + 2), 128, 0, c->st>>>(g, c->stage);
+    k_stage_wall_y<<<dim3((g.m + 2 + 127) / 128, g.l + 2), 128, 0, c->st>>>(g, c->stage);
+    k_stage_wall_z<<<dim3((g.m + 2 + 127) / 128, g.n + 2), 128, 0, c->st>>>(g, c->stage);
+  } else {
+    k_stage_ghost_x<<<dim3((g.n + 1 + 127) / 128, g.dim == 3 ? g.l + 1 : 1), 128, 0, c->st>>>(g, c->stage);
+    k_stage_ghost_y<<<dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), 128, 0, c->st>>>(g, c->stage);
+    if (g.dim == 3) k_stage_ghost_z<<<dim3((g.m + 2 + 127) / 128, g.n + 2), 128, 0, c->st>>>(g, c->stage);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "geometry kernels");
   c->launches += g.dim == 3 ? 4 : 3;

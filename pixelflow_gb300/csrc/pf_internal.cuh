@@ -34,7 +34,15 @@ struct Geo {
   // opposite interior row when it has the other colour (even n / l), else
   // the ghost row, refreshed before every half-sweep like the reference.
   int jn_n, js_1, kt_l, kb_1;
+  // 1: the air-condition program -- walls on every face, no periodic wrap
+  // (the edge neighbours are the ghost rows, which hold boundary values)
+  int wall;
 };
+
+// Ghost rows of p refreshed before each half-sweep (odd periodic sizes).
+__host__ __device__ inline bool periodic_halo(const Geo& g) {
+  return !g.wall && ((g.n % 2) || (g.dim == 3 && (g.l % 2)));
+}
 
 // Element indices are 32-bit (make_geo rejects grids whose arrays exceed
 // 2^31 elements): 64-bit index arithmetic was a large share of the
@@ -57,6 +65,7 @@ struct Scal {
   double dx, dy, dz, dt;
   double xnue, xlambda, density, thickness, threshold;
   double inlet_u, inlet_v, inlet_w;  // boundary() inflow values
+  double inlet_velocity;             // the namelist value (wall-table inlets)
   double init_u, init_v;             // initial_conditions() values
   double outlet_pressure, omega;
   int nonslip;
@@ -72,6 +81,11 @@ struct Scal {
   // non-null (the case's natural porosity array): inflow and initial
   // velocities are scaled by the porosity (the backstep program)
   const double* inflow_poro;
+  // the air-condition program's wall table (top, bottom, east, west, north,
+  // south: 0 wall, 1 inlet, 2 outlet) and the porosity its faces test, when
+  // Geo::wall
+  int walls[6];
+  const double* wall_poro;
 };
 
 // The double or float copy of a factor, by the arithmetic type T.

@@ -74,6 +74,30 @@ __device__ __forceinline__ void coef_set(const Geo& g, const Scal& s, double e, 
   }
 }
 
+// boundary_matrix of the air-condition program (ibm_3d_air_condition_omp_cpu.f90:
+// 665-867) for one cell, faces in the reference's order (top, bottom, east,
+// west, north, south; a = e, w, n, s, t, b): a wall or an inlet folds the
+// outward coefficient into the inward one; an outlet cell (porosity >= 0.9)
+// adds a_out * outlet_pressure (the ghost's value there) to bb and zeroes all
+// six.  ap keeps the sum of the unedited coefficients.
+__device__ __forceinline__ void wall_edits(const Geo& g, const Scal& s, int i, int j, int k, double e, double a[6],
+                                           double& oadd) {
+  const int face_on[6] = {k == g.l, k == 1, i == g.m, i == 1, j == g.n, j == 1};
+  const int out_d[6] = {4, 5, 0, 1, 2, 3}, in_d[6] = {5, 4, 1, 0, 3, 2};
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    if (!face_on[f]) continue;
+    const int t = s.walls[f];
+    if (t == 2 && e >= 0.9) {
+      oadd = oadd + a[out_d[f]] * s.outlet_pressure;
+      for (int d = 0; d < 6; d++) a[d] = 0.0;
+    } else {
+      a[in_d[f]] = a[in_d[f]] + a[out_d[f]];
+      a[out_d[f]] = 0.0;
+    }
+  }
+}
+
 // SOR operator of both colours, with boundrary_matrix applied, normalised
 // by omega/ap.  Face coefficients follow the reference formula
 // dt*max(small,(eps_a+eps_b)*0.5)/h/h with small = 1e-6.
@@ -88,15 +112,19 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
   double a[6], ap;
   coef_set(g, s, e, po[q + 1], po[q - 1], po[q + X], po[q - X], g.dim == 3 ? po[q + XY] : 0.0,
            g.dim == 3 ? po[q - XY] : 0.0, a, ap);
-  // boundrary_matrix: inlet row i=1 (Neumann), outlet row i=m (Dirichlet p(m+1)).
-  if (i == 1) {
-    a[0] = a[0] + a[1];
-    a[1] = 0.0;
-  }
   double oadd = 0.0;
-  if (i == g.m) {
-    oadd = a[0] * s.outlet_pressure;
-    for (int d = 0; d < 6; d++) a[d] = 0.0;
+  if (g.wall) {
+    wall_edits(g, s, i, j, k, e, a, oadd);
+  } else {
+    // boundrary_matrix: inlet row i=1 (Neumann), outlet row i=m (Dirichlet p(m+1)).
+    if (i == 1) {
+      a[0] = a[0] + a[1];
+      a[1] = 0.0;
+    }
+    if (i == g.m) {
+      oadd = a[0] * s.outlet_pressure;
+      for (int d = 0; d < 6; d++) a[d] = 0.0;
+    }
   }
   const double wap = s.omega / ap;
   const int c = colour_of(g, i, j, k);
@@ -232,6 +260,16 @@ template <typename T>
 __global__ void k_bnd_z(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= g.m + 1) c_bnd_z(g, u, v, w, p0, p1, i, blockIdx.y);
+}
+
+// boundary of the air-condition program, one face per launch (the faces run
+// in the reference's order: top, bottom, west, east, north, south).
+template <int FACE, typename T>
+__global__ void k_wall_face(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  const int na = (FACE == 2 || FACE == 3) ? g.n + 2 : g.m + 2;
+  if (a < na) c_wall_face<FACE, T>(g, s, u, v, w, p0, p1, a, b);
 }
 
 template <typename T>
@@ -612,6 +650,17 @@ void launch_projection(const Geo& g, const Scal& s, const double* p0, const doub
 template <typename TV>
 void launch_boundary(const Geo& g, const Scal& s, TV* u, TV* v, TV* w, double* p0, double* p1,
                      cudaStream_t st) {
+  if (g.wall) {
+    const dim3 xy((g.m + 2 + 127) / 128, g.n + 2), yz((g.n + 2 + 127) / 128, g.l + 2),
+        xz((g.m + 2 + 127) / 128, g.l + 2);
+    k_wall_face<0, TV><<<xy, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    k_wall_face<1, TV><<<xy, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    k_wall_face<3, TV><<<yz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    k_wall_face<2, TV><<<yz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    k_wall_face<4, TV><<<xz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    k_wall_face<5, TV><<<xz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    return;
+  }
   k_bnd_x<TV><<<dim3((g.n + 127) / 128, g.dim == 3 ? g.l : 1), 128, 0, st>>>(g, s, u, v, w, p0, p1);
   k_bnd_y<TV><<<dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), 128, 0, st>>>(g, u, v, w, p0, p1);
   if (g.dim == 3) k_bnd_z<TV><<<dim3((g.m + 2 + 127) / 128, g.n + 2), 128, 0, st>>>(g, u, v, w, p0, p1);

@@ -104,7 +104,7 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
                                   c->dampf, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
-  const bool halo = (g.n % 2) || (g.dim == 3 && (g.l % 2));
+  const bool halo = periodic_halo(g);
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
     cudaMemsetAsync(&c->red[RED_RMAX], 0, RED_SLOTS * sizeof(unsigned long long), st);
     for (int col = 0; col < 2; col++)
@@ -137,7 +137,7 @@ void enqueue_projection_mixed(pf_case* c) {
 
 void enqueue_boundary_mixed(pf_case* c) {
   const int b = c->cur;
-  c->launches += c->g.dim == 3 ? 3 : 2;
+  c->launches += c->g.wall ? 6 : (c->g.dim == 3 ? 3 : 2);
   launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
   mixed_sync_from_fp64(c);
 }

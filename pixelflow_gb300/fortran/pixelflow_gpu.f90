@@ -17,6 +17,7 @@ module pixelflow_gpu
     integer(c_int32_t) :: istep_max, iter_max
     real(c_double) :: thickness, threshold, relux_factor
     integer(c_int32_t) :: nonslip, inflow_porosity
+    integer(c_int32_t) :: wall_mode, walls(6)
   end type pf_params
 
   type, bind(C) :: pf_options

@@ -32,7 +32,8 @@ def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
     return PfParams(dim, m, n, l, s.xnue, s.xlambda, s.density, s.width, s.height, s.depth, s.time,
                     s.inlet_velocity, s.outlet_pressure, s.aoa, int(s.istep_max), int(s.iter_max),
                     s.thickness, s.threshold, s.relux_factor, 1 if s.nonslip else 0,
-                    1 if s.inflow_porosity else 0)
+                    1 if s.inflow_porosity else 0, 1 if s.walls is not None else 0,
+                    (ctypes.c_int32 * 6)(*(s.walls or (0,) * 6)))
 
 
 def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
@@ -164,7 +165,10 @@ class Case:
     def from_checkpoint(cls, path: str, **kw) -> "Case":
         import json
         with np.load(path, allow_pickle=False) as z:
-            s = Settings(**json.loads(str(z["settings"])))
+            d = json.loads(str(z["settings"]))
+            if d.get("walls") is not None:
+                d["walls"] = tuple(d["walls"])
+            s = Settings(**d)
             shape = tuple(int(x) for x in z["shape"])
             self = cls(s, shape, z["porosity"], **kw)
             self.set_state(z["u"], z["v"], z["p"], z["w"] if "w" in z.files else None)

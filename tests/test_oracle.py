@@ -220,3 +220,59 @@ def test_backstep_inflow_c_matches_numpy(shape):
     plain = OracleCase(s.replace(inflow_porosity=False), shape, vals)
     plain.initialize()
     assert not np.array_equal(plain.u, a.u)
+
+
+AIR_CONDITION_TABLE = (1, 0, 0, 0, 0, 2)  # ibm_3d_air_condition_omp_cpu.f90:10-15
+
+
+def _room(shape):
+    """A room with an opening in the ceiling (inlet) and one in the south wall
+    (outlet), an obstacle inside: porosity 1 in the openings, low elsewhere
+    on those faces."""
+    m, n, l = shape
+    s = G.settings_spheres_3d(iter_max=6, walls=AIR_CONDITION_TABLE, inlet_velocity=0.5)
+    vals = G.spheres_3d(m, n, l, spheres=np.array([[0.5, 0.5, 0.4, 0.2]]))
+    vals[-1, : n // 2, : m // 2] = 0.05   # ceiling: inlet only over part of it
+    vals[:, 0, m // 2:] = 0.05            # south wall: outlet only on one side
+    return s, vals
+
+
+@pytest.mark.parametrize("shape", [(8, 7, 6), (7, 8, 7), (9, 6, 8)])
+@pytest.mark.parametrize("table", [AIR_CONDITION_TABLE, (2, 1, 0, 1, 2, 0), (0, 2, 2, 0, 1, 1)])
+def test_air_condition_c_matches_numpy(shape, table):
+    """The air-condition program (wall table, non-periodic ghosts): the C and
+    numpy restatements agree bit for bit over several steps, for the
+    reference's table and for tables exercising every face type."""
+    s, vals = _room(shape)
+    s = s.replace(walls=table)
+    a, b = OracleCase(s, shape, vals), NpCase(s, shape, vals)
+    assert np.array_equal(a.poro, b.poro)
+    a.initialize()
+    b.initialize()
+    for f in ("u", "v", "w", "p"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), ("init", f)
+    for it in range(3):
+        assert a.step(1) == b.step(1)
+        for f in ("u", "v", "w", "p"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), (it, f)
+    assert np.isfinite(a.p).all() and np.abs(a.w).max() > 0
+
+
+def test_air_condition_walls_hold():
+    """Wall faces keep zero velocity, the inlet opening carries the inflow,
+    the outlet ghosts hold the outlet pressure."""
+    shape = (10, 9, 8)
+    s, vals = _room(shape)
+    a = OracleCase(s, shape, vals)
+    a.initialize()
+    a.step(2)
+    m, n, l = shape
+    po = a.poro
+    # away from the edges the later faces (west, east, north, south) overwrite
+    top = a.w[l, 2:n, 2:m]
+    open_top = po[l, 2:n, 2:m] >= 0.9
+    assert open_top.any() and (~open_top).any()
+    assert np.all(top[open_top] == -s.inlet_velocity) and np.all(top[~open_top] == 0)
+    assert np.all(a.u[1:l + 1, 1:n + 1, 1] == 0) and np.all(a.u[1:l + 1, 1:n + 1, m] == 0)
+    south_open = po[1:l + 1, 1, 1:m + 1] >= 0.9
+    assert np.all(a.p[1:l + 1, 0, 1:m + 1][south_open] == s.outlet_pressure)
