@@ -383,6 +383,8 @@ def run_ours(args):
     per_step = case.profile_step_times()
     value = world * cells * args.steps / (step_ms / 1e3) / 1e6
     max_div, sor_err = case.norms()
+    # the plain state after warmup + steps, for the precision form's error below
+    plain_state = case.get_state() if (args.forms and args.precision == "fp64") else None
 
     # ---- roofline of the dominant kernel (the red-black half-sweep) --------
     word = 8 if args.precision == "fp64" else 4
@@ -454,10 +456,19 @@ def run_ours(args):
         mc.step(args.steps)
         mp = mc.profile_end()
         mdiv, _ = mc.norms()
+        mstate = mc.get_state()
         mc.close()
+        # relative L2 of the precision form against the plain FP64 run after the
+        # same number of steps from the same initial state (interior cells)
+        inner = tuple(slice(1, -1) for _ in range(len(shape)))
+        err = {}
+        for f in plain_state:
+            a, b = mstate[f][inner], plain_state[f][inner]
+            err[f] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
         mval = world * cells * args.steps / (reduce_max(mp["step_ms"], world) / 1e3) / 1e6
         line["forms"] = {"mixed_same_case": {"value": mval, "unit": UNIT, "max_div": mdiv,
                                              "speedup_vs_plain_fp64": mval / value,
+                                             "rel_l2_vs_fp64": err, "after_steps": args.warmup + args.steps,
                                              "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation"}}
         if not args.no_batch:
             line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
