@@ -543,13 +543,28 @@ int pf_set_state(pf_case* c, const double* u, const double* v, const double* w, 
   const int b = c->cur;
   const double* src[3] = {u, v, w};
   double* dst[3] = {c->U[b], c->V[b], c->W[b]};
+  // Host blocks with exactly the ghosted extents are contiguous: one flat copy
+  // into the staging array, then a device kernel into the pitched layout
+  // (a pitched copy from the host moves one row per DMA descriptor).
+  const bool flat = ld1 == g.m + 2 && ld2 == g.n + 2;
+  const size_t dense = (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double);
   for (int f = 0; f < g.dim; f++) {
-    cudaMemcpy3DParms P = copy_params(c, src[f], hp, ld2, dst[f], dp, g.Y, cudaMemcpyHostToDevice);
+    if (flat) {
+      PF_CUDA(cudaMemcpyAsync(c->stage, src[f], dense, cudaMemcpyHostToDevice, c->st));
+      launch_scatter_nat(g, c->stage, dst[f], c->st);
+      c->launches += 1;
+    } else {
+      cudaMemcpy3DParms P = copy_params(c, src[f], hp, ld2, dst[f], dp, g.Y, cudaMemcpyHostToDevice);
+      PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+    }
+  }
+  if (flat) {
+    PF_CUDA(cudaMemcpyAsync(c->stage, p, dense, cudaMemcpyHostToDevice, c->st));
+  } else {
+    cudaMemcpy3DParms P = copy_params(c, p, hp, ld2, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2,
+                                      cudaMemcpyHostToDevice);
     PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
   }
-  cudaMemcpy3DParms P = copy_params(c, p, hp, ld2, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2,
-                                    cudaMemcpyHostToDevice);
-  PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
   launch_scatter_pk(g, c->stage, c->p[0], c->p[1], c->st);
   c->launches += 1;
   if (c->opt.precision == PF_PREC_MIXED) mixed_sync_from_fp64(c);
@@ -565,17 +580,29 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   const int b = c->cur;
   double* dst[3] = {u, v, w};
   const double* src[3] = {c->U[b], c->V[b], c->W[b]};
+  const bool flat = ld1 == g.m + 2 && ld2 == g.n + 2;  // contiguous host blocks (see pf_set_state)
+  const size_t dense = (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double);
   for (int f = 0; f < g.dim; f++) {
     if (!dst[f]) continue;
-    cudaMemcpy3DParms P = copy_params(c, src[f], dp, g.Y, dst[f], hp, ld2, cudaMemcpyDeviceToHost);
-    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+    if (flat) {
+      launch_gather_nat(g, src[f], c->stage, c->st);
+      c->launches += 1;
+      PF_CUDA(cudaMemcpyAsync(dst[f], c->stage, dense, cudaMemcpyDeviceToHost, c->st));
+    } else {
+      cudaMemcpy3DParms P = copy_params(c, src[f], dp, g.Y, dst[f], hp, ld2, cudaMemcpyDeviceToHost);
+      PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+    }
   }
   if (p) {
     launch_gather_pk(g, c->p[0], c->p[1], c->stage, c->st);
     c->launches += 1;
-    cudaMemcpy3DParms P = copy_params(c, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2, p, hp, ld2,
-                                      cudaMemcpyDeviceToHost);
-    PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+    if (flat) {
+      PF_CUDA(cudaMemcpyAsync(p, c->stage, dense, cudaMemcpyDeviceToHost, c->st));
+    } else {
+      cudaMemcpy3DParms P = copy_params(c, c->stage, (size_t)(g.m + 2) * sizeof(double), g.n + 2, p, hp, ld2,
+                                        cudaMemcpyDeviceToHost);
+      PF_CUDA(cudaMemcpy3DAsync(&P, c->st));
+    }
   }
   rc = check_launch("pf_get_state");
   if (rc) return rc;

@@ -166,6 +166,7 @@ void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
 // staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts
 void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st);
+void launch_gather_nat(const Geo& g, const double* src, double* stage, cudaStream_t st);
 void launch_scatter_pk(const Geo& g, const double* stage, double* p0, double* p1, cudaStream_t st);
 void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* stage, cudaStream_t st);
 

@@ -402,6 +402,14 @@ __global__ void k_scatter_nat(Geo g, const double* __restrict__ st, double* __re
   const idx_t d = (idx_t)i + (idx_t)(g.m + 2) * ((idx_t)j + (idx_t)(g.n + 2) * k);
   dst[nat_idx(g, i, j, k)] = st[d];
 }
+__global__ void k_gather_nat(Geo g, const double* __restrict__ src, double* __restrict__ st) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int j = blockIdx.y * BY + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i > g.m + 1 || j > g.n + 1) return;
+  const idx_t d = (idx_t)i + (idx_t)(g.m + 2) * ((idx_t)j + (idx_t)(g.n + 2) * k);
+  st[d] = src[nat_idx(g, i, j, k)];
+}
 __global__ void k_scatter_pk(Geo g, const double* __restrict__ st, double* p0, double* p1) {
   const int i = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y;
@@ -755,6 +763,9 @@ void launch_to_double(const float* src, double* dst, long long n, cudaStream_t s
 
 void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st) {
   k_scatter_nat<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, stage, dst);
+}
+void launch_gather_nat(const Geo& g, const double* src, double* stage, cudaStream_t st) {
+  k_gather_nat<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, src, stage);
 }
 void launch_scatter_pk(const Geo& g, const double* stage, double* p0, double* p1, cudaStream_t st) {
   k_scatter_pk<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, stage, p0, p1);
