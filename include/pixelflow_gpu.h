@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 1
+#define PF_ABI_VERSION 2
 
 enum {
   PF_OK = 0,
