@@ -262,7 +262,8 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
 
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
-                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 300000):
+                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 300000,
+                  policy: str = "srpt"):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
     100-1000 steps each, admitted by a 150 GB HBM budget into one resident
@@ -275,7 +276,8 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
     from pixelflow_gb300.solver import Case
     reqs = G.serving_requests(count=count, rate=rate, seed=seed)
     t0 = time.perf_counter()
-    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True, large_cells=large_cells) as srv:
+    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True, large_cells=large_cells,
+                policy=policy) as srv:
         res = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         summ = summarize(res, wall)
@@ -294,13 +296,15 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
             prof = c.profile_end()
         tot_cells += r.cells * baseline_steps
         tot_ms += prof["step_ms"]
-    plain = tot_cells / (tot_ms / 1e3) / 1e6
     summ["workload"] = (f"{count} requests, Poisson {rate:g}/s, 70% 2D 128^2-1024^2 / 30% 3D 64^3-192^3, "
                         f"100-1000 steps, 150 GB budget, chunk {chunk}, large cases > {large_cells} cells "
-                        f"on own streams")
-    summ["plain_fp64_sequential"] = {"value": plain, "unit": UNIT, "sample_requests": int(min(baseline_sample, len(reqs))),
-                                     "steps_each": baseline_steps}
-    summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain
+                        f"on own streams, round policy {policy}")
+    if tot_ms > 0:
+        plain = tot_cells / (tot_ms / 1e3) / 1e6
+        summ["plain_fp64_sequential"] = {"value": plain, "unit": UNIT,
+                                         "sample_requests": int(min(baseline_sample, len(reqs))),
+                                         "steps_each": baseline_steps}
+        summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain
     return summ
 
 
@@ -472,7 +476,8 @@ def run_ours(args):
                                              "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation"}}
         if not args.no_batch:
             line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
-            line["forms"]["serving"] = bench_serving()
+            line["forms"]["serving"] = bench_serving(policy="srpt")
+            line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_sample=0)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)
     barrier(world)

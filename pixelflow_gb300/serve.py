@@ -13,6 +13,12 @@ fields and norms) is read back, its slot and memory freed, and its latency
 
 Each case's arithmetic is independent of what else is in the batch, so a
 result is the same alone and in any mix (bit for bit; tests/test_gpu_serve.py).
+
+Round policy: "rr" advances every active case each round; "srpt" advances
+the cases with the least remaining work (cells x steps left) first, adding
+cases in that order until a round holds at least `round_cells` cells, so the
+GPU stays full while short requests finish early (a lower p50 at the same
+throughput; the longest requests still finish last).
 """
 from __future__ import annotations
 
@@ -47,9 +53,15 @@ class Result:
 
 class Server:
     def __init__(self, hbm_budget_bytes: int = 150 * GIB, chunk: int = 25, cluster: int = 4, threads: int = 512,
-                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 300000):
-        self.batch = Batch(cluster=cluster, threads=threads, max_cases=max_cases,
-                           hbm_budget_bytes=hbm_budget_bytes, large_cells=large_cells)
+                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 300000,
+                 policy: str = "rr", round_cells: int = 24_000_000, batch=None):
+        if policy not in ("rr", "srpt"):
+            raise ValueError(f"unknown policy {policy!r}")
+        self.batch = batch if batch is not None else Batch(cluster=cluster, threads=threads, max_cases=max_cases,
+                                                           hbm_budget_bytes=hbm_budget_bytes,
+                                                           large_cells=large_cells)
+        self.policy = policy
+        self.round_cells = round_cells
         self.chunk = chunk
         self.keep_state = keep_state
         self.edge = edge
@@ -101,7 +113,7 @@ class Server:
                 if incoming and realtime:
                     time.sleep(max(0.0, min(0.005, incoming[0].arrival_s - now())))
                 continue
-            slots = list(active)
+            slots = self._select(active)
             steps = [min(self.chunk, active[s]["left"]) for s in slots]
             self.batch.step_slots(slots, steps)
             self.rounds += 1
@@ -117,6 +129,19 @@ class Server:
                     self.batch.remove(s)
                     del active[s]
         return sorted(results, key=lambda x: x.rid)
+
+    def _select(self, active: Dict[int, dict]) -> List[int]:
+        """The slots advanced this round (see the module docstring)."""
+        if self.policy == "rr":
+            return list(active)
+        order = sorted(active, key=lambda s: (active[s]["req"].cells * active[s]["left"], active[s]["req"].rid))
+        chosen, cells = [], 0
+        for s in order:
+            chosen.append(s)
+            cells += active[s]["req"].cells
+            if cells >= self.round_cells:
+                break
+        return chosen
 
 
 def summarize(results: List[Result], wall_s: float) -> dict:

@@ -31,11 +31,12 @@ def test_gpu_shapes_match_host_generator():
     ref.close()
 
 
-def test_served_results_equal_single_runs():
+@pytest.mark.parametrize("policy", ["rr", "srpt"])
+def test_served_results_equal_single_runs(policy):
     reqs = _small_requests()
     # budget for ~2 of the requests at a time forces queueing and slot reuse
     budget = int(2.2 * max(case_bytes(r.settings, r.shape) for r in reqs))
-    with Server(hbm_budget_bytes=budget, chunk=4) as srv:
+    with Server(hbm_budget_bytes=budget, chunk=4, policy=policy, round_cells=20_000) as srv:
         res = srv.run(reqs, realtime=True)
         assert srv.peak_bytes <= budget
     assert [r.rid for r in res] == [r.rid for r in reqs]
