@@ -32,6 +32,17 @@ __device__ __forceinline__ void max_pair(unsigned& hi, unsigned& lo, unsigned h2
   lo = gt ? l2 : lo;
 }
 
+// Programmatic dependent launch: the sweeps of the SOR loop are launched so
+// that the next kernel may be scheduled while this one finishes.  Every CTA
+// first waits for the previous grid to complete (its writes visible), then
+// allows the next grid to launch; that grid can start only once every CTA of
+// this one has reached this point, i.e. is already resident, so the waiting
+// CTAs of the next grid never hold SM slots this grid still needs.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ int red_slot() {
   return (int)((blockIdx.x + 37u * blockIdx.y + 101u * blockIdx.z) & (RED_SLOTS - 1));
 }

@@ -27,6 +27,25 @@ namespace pf {
 
 namespace {
 
+// Launch with programmatic stream serialization (the kernel starts with
+// pdl_begin): the launch of the next kernel of the SOR loop overlaps the
+// tail of the current one; CUDA graph capture keeps these as programmatic
+// edges.
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 inline dim3 grid_interior(const Geo& g) {
   return dim3((g.m + BX - 1) / BX, (g.n + BY - 1) / BY, g.dim == 3 ? g.l : 1);
 }
@@ -201,6 +220,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sor_half(Geo g, Coef<T> C, T*
                                                             const T* __restrict__ po, T omw, int colour,
                                                             unsigned long long* __restrict__ err,
                                                             const int* __restrict__ skip) {
+  pdl_begin();
   if (skip && *skip) return;  // uniform over the grid: defect correction converged
   const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
   decltype(abs_bits(T(0))) e = 0;
@@ -216,6 +236,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_sor_half(Geo g, Coef<T> C, T*
 // refreshes them before each half-sweep (ibm_2d:322-327; ibm_3d:463-480).
 template <typename T>
 __global__ void k_p_halo(Geo g, T* p0, T* p1, const int* __restrict__ skip) {
+  pdl_begin();
   if (skip && *skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int a = blockIdx.y + 1;  // k for the y rows (3D), j for the z planes
@@ -448,6 +469,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_residual(Geo g, Coef<double> 
                                                      float* __restrict__ rf, float* __restrict__ ec,
                                                      unsigned long long* __restrict__ rmax,
                                                      const int* __restrict__ skip) {
+  pdl_begin();
   if (skip && *skip) return;
   const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
   unsigned long long r = 0;
@@ -481,6 +503,7 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
                                                          const float* __restrict__ eo, int colour, int chunks,
                                                          unsigned long long* __restrict__ err,
                                                          const int* __restrict__ skip) {
+  pdl_begin();
   if (skip && *skip) return;
   const int t = blockIdx.x * DC4_THREADS + threadIdx.x;
   const int rows = DIM == 3 ? g.n * g.l : g.n;
@@ -545,6 +568,7 @@ __global__ void k_pack_eps(Geo g, const double* __restrict__ po, float* e0, floa
 template <int DIM>
 __global__ void k_accumulate(Geo g, double* __restrict__ p0, double* __restrict__ p1, const float* __restrict__ e0,
                              const float* __restrict__ e1, const int* __restrict__ skip) {
+  pdl_begin();
   if (skip && *skip) return;
   const int h = blockIdx.x * BX + threadIdx.x;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
@@ -629,21 +653,21 @@ void launch_sor_half(const Geo& g, const Coef<T>& cc, T* pc, const T* po, T one_
   const unsigned grid = (unsigned)((packed_items(g) + SWEEP_THREADS - 1) / SWEEP_THREADS);
   if (g.dim == 3) {
     if (err)
-      k_sor_half<T, 3, true><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      launch_pdl(k_sor_half<T, 3, true>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
     else
-      k_sor_half<T, 3, false><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      launch_pdl(k_sor_half<T, 3, false>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
   } else {
     if (err)
-      k_sor_half<T, 2, true><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      launch_pdl(k_sor_half<T, 2, true>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
     else
-      k_sor_half<T, 2, false><<<grid, SWEEP_THREADS, 0, st>>>(g, cc, pc, po, one_minus_omega, colour, err, skip);
+      launch_pdl(k_sor_half<T, 2, false>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
   }
 }
 
 template <typename T>
 void launch_p_halo(const Geo& g, T* p0, T* p1, const int* skip, cudaStream_t st) {
   const int a = g.dim == 3 ? (g.n > g.l ? g.n : g.l) : 1;
-  k_p_halo<T><<<dim3((g.m + 127) / 128, a, g.dim == 3 ? 2 : 1), 128, 0, st>>>(g, p0, p1, skip);
+  launch_pdl(k_p_halo<T>, dim3((g.m + 127) / 128, a, g.dim == 3 ? 2 : 1), dim3(128), st, g, p0, p1, skip);
 }
 
 template <typename TV>
@@ -692,9 +716,9 @@ void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, cons
                      cudaStream_t st) {
   const unsigned grid = (unsigned)((packed_items(g) + SWEEP_THREADS - 1) / SWEEP_THREADS);
   if (g.dim == 3)
-    k_residual<3><<<grid, SWEEP_THREADS, 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
+    launch_pdl(k_residual<3>, grid, SWEEP_THREADS, st, g, C, pc, po, omega, colour, rf, ec, rmax, skip);
   else
-    k_residual<2><<<grid, SWEEP_THREADS, 0, st>>>(g, C, pc, po, omega, colour, rf, ec, rmax, skip);
+    launch_pdl(k_residual<2>, grid, SWEEP_THREADS, st, g, C, pc, po, omega, colour, rf, ec, rmax, skip);
 }
 
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
@@ -712,14 +736,14 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
   const unsigned blocks = (unsigned)((threads + DC4_THREADS - 1) / DC4_THREADS);
   if (g.dim == 3) {
     if (err)
-      k_sor_dc4<3, true><<<blocks, DC4_THREADS, 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      launch_pdl(k_sor_dc4<3, true>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
     else
-      k_sor_dc4<3, false><<<blocks, DC4_THREADS, 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      launch_pdl(k_sor_dc4<3, false>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
   } else {
     if (err)
-      k_sor_dc4<2, true><<<blocks, DC4_THREADS, 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      launch_pdl(k_sor_dc4<2, true>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
     else
-      k_sor_dc4<2, false><<<blocks, DC4_THREADS, 0, st>>>(g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      launch_pdl(k_sor_dc4<2, false>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
   }
 }
 
@@ -745,9 +769,9 @@ void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, co
   dim3 grid = grid_packed(g);
   grid.z *= 2;
   if (g.dim == 3)
-    k_accumulate<3><<<grid, dim3(BX, BY), 0, st>>>(g, p0, p1, e0, e1, skip);
+    launch_pdl(k_accumulate<3>, grid, dim3(BX, BY), st, g, p0, p1, e0, e1, skip);
   else
-    k_accumulate<2><<<grid, dim3(BX, BY), 0, st>>>(g, p0, p1, e0, e1, skip);
+    launch_pdl(k_accumulate<2>, grid, dim3(BX, BY), st, g, p0, p1, e0, e1, skip);
 }
 
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st) {
