@@ -272,7 +272,7 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
   cudaStream_t st = c->st;
   const int o = c->cur, nw = 1 - c->cur;
   const bool track = c->opt.track_sor_error != 0;
-  if (track) cudaMemsetAsync(&c->red[RED_ERR], 0, RED_SLOTS * sizeof(unsigned long long), st);
+  if (track) launch_zero_u64(&c->red[RED_ERR], RED_SLOTS, st);
   launch_divergence<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, st);
   launch_predictor<double, double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv,
                                    c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
@@ -290,7 +290,7 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
   if (!g.wall) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
-  c->launches += 3 + (g.wall ? 0 : 1) + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
+  c->launches += 3 + (track ? 1 : 0) + (g.wall ? 0 : 1) + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
   c->cur = nw;
 }
 

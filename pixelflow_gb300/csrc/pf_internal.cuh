@@ -153,6 +153,8 @@ void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, cons
                      cudaStream_t st);
 void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, const float* e1, const int* skip,
                        cudaStream_t st);
+void launch_zero_u64(unsigned long long* p, int n, cudaStream_t st);
+void launch_zero_int(int* p, cudaStream_t st);
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);

@@ -161,6 +161,7 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
 template <typename T>
 __global__ void k_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* __restrict__ vo,
                              const T* __restrict__ wo, T* __restrict__ div) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __
                                                       const TS* __restrict__ su, const TS* __restrict__ sv,
                                                       const TS* __restrict__ sw, TS* __restrict__ u,
                                                       TS* __restrict__ v, TS* __restrict__ w) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
@@ -200,6 +202,7 @@ __global__ void k_rhs(Geo g, Scal s, const T* __restrict__ u, const T* __restric
                       const double* __restrict__ po, const double* __restrict__ gxa,
                       const double* __restrict__ gya, const double* __restrict__ gza, Coef<double> c0,
                       Coef<double> c1) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
@@ -254,6 +257,7 @@ __global__ void k_p_halo(Geo g, T* p0, T* p1, const int* __restrict__ skip) {
 template <typename T, int DIM>
 __global__ void k_projection(Geo g, Scal s, const double* __restrict__ p0, const double* __restrict__ p1, T* u,
                              T* v, T* w) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
@@ -264,6 +268,7 @@ __global__ void k_projection(Geo g, Scal s, const double* __restrict__ p0, const
 // boundary, x faces: inflow at i=1 and its ghost, outflow copy at m+1.
 template <typename T>
 __global__ void k_bnd_x(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1) {
+  pdl_begin();
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int k = (g.dim == 3) ? blockIdx.y + 1 : 0;
   if (j <= g.n) c_bnd_x(g, s, u, v, w, p0, p1, j, k);
@@ -272,6 +277,7 @@ __global__ void k_bnd_x(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1)
 // boundary, y faces: periodic ghost rows over i = 0..m+1 (and k = 0..l+1).
 template <typename T>
 __global__ void k_bnd_y(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
+  pdl_begin();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= g.m + 1) c_bnd_y(g, u, v, w, p0, p1, i, blockIdx.y);  // k = 0 in 2D, 0..l+1 in 3D
 }
@@ -279,6 +285,7 @@ __global__ void k_bnd_y(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
 // boundary, z faces (3D): periodic ghost planes over i = 0..m+1, j = 0..n+1.
 template <typename T>
 __global__ void k_bnd_z(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
+  pdl_begin();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= g.m + 1) c_bnd_z(g, u, v, w, p0, p1, i, blockIdx.y);
 }
@@ -287,6 +294,7 @@ __global__ void k_bnd_z(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
 // in the reference's order: top, bottom, west, east, north, south).
 template <int FACE, typename T>
 __global__ void k_wall_face(Geo g, Scal s, T* u, T* v, T* w, double* p0, double* p1) {
+  pdl_begin();
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   const int na = (FACE == 2 || FACE == 3) ? g.n + 2 : g.m + 2;
@@ -577,13 +585,26 @@ __global__ void k_accumulate(Geo g, double* __restrict__ p0, double* __restrict_
   c_accumulate<DIM>(g, colour ? p1 : p0, colour ? e1 : e0, colour, h, j, k);
 }
 
+// Zero n reduction slots (or one int flag) inside a step: a kernel, not a
+// memset, so the programmatic launch chain of the step is not interrupted.
+__global__ void k_zero_u64(unsigned long long* p, int n) {
+  pdl_begin();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = 0ULL;
+}
+__global__ void k_zero_int(int* p) {
+  pdl_begin();
+  *p = 0;
+}
+
 // Stop the remaining passes of this step once max|r|/w <= tol.
 __global__ void k_dc_check(const unsigned long long* rmax, double tol_w, int* skip) {
+  pdl_begin();
   const double r = __longlong_as_double((long long)max_of_slots(rmax));
   if (r <= tol_w) *skip = 1;
 }
 
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  pdl_begin();
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) b[q] = (float)a[q];
 }
@@ -608,7 +629,7 @@ void launch_setup_coef(const Geo& g, const Scal& s, const double* poro, Coef<dou
 template <typename TV>
 void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, TV* div,
                        cudaStream_t st) {
-  k_divergence<TV><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div);
+  launch_pdl(k_divergence<TV>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div);
 }
 
 template <typename T, typename TS>
@@ -616,10 +637,10 @@ void launch_predictor(const Geo& g, const Scal& s, const T* uo, const T* vo, con
                       const T* gx, const T* gy, const T* gz, const T* rinv, const T* damp, const TS* us,
                       const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st) {
   if (g.dim == 3)
-    k_predictor<T, TS, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
+    launch_pdl(k_predictor<T, TS, 3>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv,
                                                                      damp, us, vs, ws, u, v, w);
   else
-    k_predictor<T, TS, 2><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, uo, vo, wo, div, gx, gy, gz, rinv,
+    launch_pdl(k_predictor<T, TS, 2>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv,
                                                                      damp, us, vs, ws, u, v, w);
 }
 template void launch_predictor<double, double>(const Geo&, const Scal&, const double*, const double*,
@@ -637,9 +658,9 @@ void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV*
                 const double* gx, const double* gy, const double* gz, Coef<double> c0, Coef<double> c1,
                 cudaStream_t st) {
   if (g.dim == 3)
-    k_rhs<TV, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, u, v, w, poro, gx, gy, gz, c0, c1);
+    launch_pdl(k_rhs<TV, 3>, grid_interior(g), dim3(BX, BY), st, g, s, u, v, w, poro, gx, gy, gz, c0, c1);
   else
-    k_rhs<TV, 2><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, u, v, w, poro, gx, gy, gz, c0, c1);
+    launch_pdl(k_rhs<TV, 2>, grid_interior(g), dim3(BX, BY), st, g, s, u, v, w, poro, gx, gy, gz, c0, c1);
 }
 
 static dim3 grid_packed(const Geo& g) {
@@ -674,9 +695,9 @@ template <typename TV>
 void launch_projection(const Geo& g, const Scal& s, const double* p0, const double* p1, TV* u, TV* v, TV* w,
                        cudaStream_t st) {
   if (g.dim == 3)
-    k_projection<TV, 3><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, p0, p1, u, v, w);
+    launch_pdl(k_projection<TV, 3>, grid_interior(g), dim3(BX, BY), st, g, s, p0, p1, u, v, w);
   else
-    k_projection<TV, 2><<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, p0, p1, u, v, w);
+    launch_pdl(k_projection<TV, 2>, grid_interior(g), dim3(BX, BY), st, g, s, p0, p1, u, v, w);
 }
 
 template <typename TV>
@@ -685,17 +706,17 @@ void launch_boundary(const Geo& g, const Scal& s, TV* u, TV* v, TV* w, double* p
   if (g.wall) {
     const dim3 xy((g.m + 2 + 127) / 128, g.n + 2), yz((g.n + 2 + 127) / 128, g.l + 2),
         xz((g.m + 2 + 127) / 128, g.l + 2);
-    k_wall_face<0, TV><<<xy, 128, 0, st>>>(g, s, u, v, w, p0, p1);
-    k_wall_face<1, TV><<<xy, 128, 0, st>>>(g, s, u, v, w, p0, p1);
-    k_wall_face<3, TV><<<yz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
-    k_wall_face<2, TV><<<yz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
-    k_wall_face<4, TV><<<xz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
-    k_wall_face<5, TV><<<xz, 128, 0, st>>>(g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<0, TV>, xy, dim3(128), st, g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<1, TV>, xy, dim3(128), st, g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<3, TV>, yz, dim3(128), st, g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<2, TV>, yz, dim3(128), st, g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<4, TV>, xz, dim3(128), st, g, s, u, v, w, p0, p1);
+    launch_pdl(k_wall_face<5, TV>, xz, dim3(128), st, g, s, u, v, w, p0, p1);
     return;
   }
-  k_bnd_x<TV><<<dim3((g.n + 127) / 128, g.dim == 3 ? g.l : 1), 128, 0, st>>>(g, s, u, v, w, p0, p1);
-  k_bnd_y<TV><<<dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), 128, 0, st>>>(g, u, v, w, p0, p1);
-  if (g.dim == 3) k_bnd_z<TV><<<dim3((g.m + 2 + 127) / 128, g.n + 2), 128, 0, st>>>(g, u, v, w, p0, p1);
+  launch_pdl(k_bnd_x<TV>, dim3((g.n + 127) / 128, g.dim == 3 ? g.l : 1), dim3(128), st, g, s, u, v, w, p0, p1);
+  launch_pdl(k_bnd_y<TV>, dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), dim3(128), st, g, u, v, w, p0, p1);
+  if (g.dim == 3) launch_pdl(k_bnd_z<TV>, dim3((g.m + 2 + 127) / 128, g.n + 2), dim3(128), st, g, u, v, w, p0, p1);
 }
 
 template <typename TV>
@@ -774,12 +795,17 @@ void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, co
     launch_pdl(k_accumulate<2>, grid, dim3(BX, BY), st, g, p0, p1, e0, e1, skip);
 }
 
+void launch_zero_u64(unsigned long long* p, int n, cudaStream_t st) {
+  launch_pdl(k_zero_u64, dim3(1), dim3(256), st, p, n);
+}
+void launch_zero_int(int* p, cudaStream_t st) { launch_pdl(k_zero_int, dim3(1), dim3(1), st, p); }
+
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st) {
-  k_dc_check<<<1, 1, 0, st>>>(rmax, tol, skip);
+  launch_pdl(k_dc_check, dim3(1), dim3(1), st, rmax, tol, skip);
 }
 
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st) {
-  k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);
+  launch_pdl(k_to_float, dim3((unsigned)((n + 255) / 256)), dim3(256), st, src, dst, n);
 }
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st) {
   k_to_double<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);

@@ -97,8 +97,8 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   const bool track = c->opt.track_sor_error != 0;
   const bool early = c->opt.dc_tol > 0.0;
   const int* skip = early ? c->skip : nullptr;
-  if (track) cudaMemsetAsync(&c->red[RED_ERRF], 0, RED_SLOTS * sizeof(unsigned long long), st);
-  if (early) cudaMemsetAsync(c->skip, 0, sizeof(int), st);
+  if (track) launch_zero_u64(&c->red[RED_ERRF], RED_SLOTS, st);
+  if (early) launch_zero_int(c->skip, st);
   launch_divergence<float>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, st);
   launch_predictor<float, double>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, c->gxf, c->gyf, c->gzf, c->rinvf,
                                   c->dampf, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
@@ -106,7 +106,7 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
-    cudaMemsetAsync(&c->red[RED_RMAX], 0, RED_SLOTS * sizeof(unsigned long long), st);
+    launch_zero_u64(&c->red[RED_RMAX], RED_SLOTS, st);
     for (int col = 0; col < 2; col++)
       launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col],
                       &c->red[RED_RMAX], skip, st);
@@ -124,8 +124,9 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
   launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
-  c->launches += 4 + (int64_t)c->opt.outer_max *
-                         (3 + (early ? 1 : 0) + (halo ? 1 : 0) + (int64_t)c->opt.inner_sweeps * 2 * (halo ? 2 : 1));
+  c->launches += 4 + (track ? 1 : 0) + (early ? 1 : 0) +
+                 (int64_t)c->opt.outer_max *
+                     (4 + (early ? 1 : 0) + (halo ? 1 : 0) + (int64_t)c->opt.inner_sweeps * 2 * (halo ? 2 : 1));
   c->cur = nw;
 }
 
