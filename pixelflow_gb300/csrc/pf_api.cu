@@ -616,11 +616,28 @@ int pf_snapshot_begin(pf_case* c) {
   const Geo& g = c->g;
   const size_t dense = (size_t)(g.m + 2) * (g.n + 2) * g.Z;
   const int nf = g.dim + 1;
-  if (!c->snap) {
-    PF_CUDA(cudaMalloc(&c->snap, nf * dense * sizeof(double)));
-    PF_CUDA(cudaHostAlloc(&c->hsnap, nf * dense * sizeof(double), cudaHostAllocDefault));
-    PF_CUDA(cudaStreamCreateWithFlags(&c->st_snap, cudaStreamNonBlocking));
-    for (auto& e : c->ev_snap) PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (!c->snap) {  // first use: all four resources or none
+    double *dsnap = nullptr, *hsnap = nullptr;
+    cudaStream_t ss = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaMalloc(&dsnap, nf * dense * sizeof(double));
+    if (e == cudaSuccess) e = cudaHostAlloc(&hsnap, nf * dense * sizeof(double), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      if (dsnap) cudaFree(dsnap);
+      if (hsnap) cudaFreeHost(hsnap);
+      if (ss) cudaStreamDestroy(ss);
+      for (auto x : ev)
+        if (x) cudaEventDestroy(x);
+      return cuda_fail(e, "pf_snapshot_begin: snapshot buffers");
+    }
+    c->snap = dsnap;
+    c->hsnap = hsnap;
+    c->st_snap = ss;
+    c->ev_snap[0] = ev[0];
+    c->ev_snap[1] = ev[1];
   }
   // device-side copies on the case's stream: the state as of the last enqueued step
   const int b = c->cur;
@@ -772,6 +789,7 @@ int pf_forces(pf_case* c, double force_p[3], double force_v[3]) {
   // scratch: the staging array, (m+2)(n+2)[(l+2)] doubles >= 6 per 256 cells + 6
   const long long cells = (long long)g.m * g.n * (g.dim == 3 ? g.l : 1);
   const long long nb = (cells + 255) / 256;
+  if (6 * nb + 6 > (long long)(g.m + 2) * (g.n + 2) * g.Z) return fail(PF_E_INVALID, "pf_forces: grid too small");
   double* out = c->stage + 6 * nb;
   launch_forces(g, c->s, c->poro, c->p[0], c->p[1], c->U[b], c->V[b], c->W[b], c->stage, out, c->st);
   c->launches += 2;

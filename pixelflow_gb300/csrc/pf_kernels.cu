@@ -499,12 +499,17 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_residual(Geo g, Coef<double> 
 // outside 1 <= i <= m store their old value back.
 constexpr int DC4_THREADS = 256;
 
-__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ float f4(const float4& v, int u) {
-  return u == 0 ? v.x : (u == 1 ? v.y : (u == 2 ? v.z : v.w));
+// V consecutive floats loaded as one aligned vector access.
+template <int V>
+struct alignas(4 * V) VecF {
+  float a[V];
+};
+template <int V>
+__device__ __forceinline__ VecF<V> ldv(const float* p) {
+  return *reinterpret_cast<const VecF<V>*>(p);
 }
 
-template <int DIM, bool TRACK>
+template <int DIM, bool TRACK, int V>
 __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const float* __restrict__ epsc,
                                                          const float* __restrict__ epso,
                                                          const float* __restrict__ r, float* __restrict__ ec,
@@ -518,7 +523,7 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
   unsigned e = 0;
   if (t < chunks * rows) {
     const int row = t / chunks;
-    const int h0 = (t - row * chunks) * 4;
+    const int h0 = (t - row * chunks) * V;
     const int k = DIM == 3 ? row / g.n + 1 : 0;
     const int j = DIM == 3 ? row - (k - 1) * g.n + 1 : row + 1;
     const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
@@ -526,37 +531,37 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
     const idx_t q = pk_idx(g, h0, j, k);
     const idx_t qn = (j == g.n) ? pk_idx(g, h0, g.jn_n, k) : q + H;
     const idx_t qs = (j == 1) ? pk_idx(g, h0, g.js_1, k) : q - H;
-    const float4 EC = ld4(ec + q), R = ld4(r + q), PC = ld4(epsc + q);
-    const float4 XO = ld4(eo + q), PO = ld4(epso + q);
-    const float xx = s ? eo[q + 4] : eo[q - 1];
-    const float px = s ? epso[q + 4] : epso[q - 1];
-    const float4 XN = ld4(eo + qn), XS = ld4(eo + qs), PN = ld4(epso + q + H), PS = ld4(epso + q - H);
-    float4 XT = make_float4(0.f, 0.f, 0.f, 0.f), XB = XT, PT = XT, PB = XT;
+    const VecF<V> EC = ldv<V>(ec + q), R = ldv<V>(r + q), PC = ldv<V>(epsc + q);
+    const VecF<V> XO = ldv<V>(eo + q), PO = ldv<V>(epso + q);
+    const float xx = s ? eo[q + V] : eo[q - 1];
+    const float px = s ? epso[q + V] : epso[q - 1];
+    const VecF<V> XN = ldv<V>(eo + qn), XS = ldv<V>(eo + qs), PN = ldv<V>(epso + q + H), PS = ldv<V>(epso + q - H);
+    VecF<V> XT{}, XB{}, PT{}, PB{};
     if (DIM == 3) {
       const idx_t qt = (k == g.l) ? pk_idx(g, h0, j, g.kt_l) : q + HY;
       const idx_t qb = (k == 1) ? pk_idx(g, h0, j, g.kb_1) : q - HY;
-      XT = ld4(eo + qt);
-      XB = ld4(eo + qb);
-      PT = ld4(epso + q + HY);
-      PB = ld4(epso + q - HY);
+      XT = ldv<V>(eo + qt);
+      XB = ldv<V>(eo + qb);
+      PT = ldv<V>(epso + q + HY);
+      PB = ldv<V>(epso + q - HY);
     }
-    float out[4];
+    VecF<V> out;
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < V; u++) {
       const int i = 2 * (h0 + u) + s;
-      const float eold = f4(EC, u);
+      const float eold = EC.a[u];
       // east = other colour at h + s, west at h - 1 + s
-      const float xe = s ? (u < 3 ? f4(XO, u + 1) : xx) : f4(XO, u);
-      const float xw = s ? f4(XO, u) : (u > 0 ? f4(XO, u - 1) : xx);
-      const float pe = s ? (u < 3 ? f4(PO, u + 1) : px) : f4(PO, u);
-      const float pw = s ? f4(PO, u) : (u > 0 ? f4(PO, u - 1) : px);
-      const float v = dc_cell<DIM>(K, f4(PC, u), pe, pw, f4(PN, u), f4(PS, u), f4(PT, u), f4(PB, u), xe, xw,
-                                   f4(XN, u), f4(XS, u), f4(XT, u), f4(XB, u), f4(R, u), eold, i == 1, i == g.m);
+      const float xe = s ? (u < V - 1 ? XO.a[u + 1] : xx) : XO.a[u];
+      const float xw = s ? XO.a[u] : (u > 0 ? XO.a[u - 1] : xx);
+      const float pe = s ? (u < V - 1 ? PO.a[u + 1] : px) : PO.a[u];
+      const float pw = s ? PO.a[u] : (u > 0 ? PO.a[u - 1] : px);
+      const float v = dc_cell<DIM>(K, PC.a[u], pe, pw, PN.a[u], PS.a[u], PT.a[u], PB.a[u], xe, xw, XN.a[u],
+                                   XS.a[u], XT.a[u], XB.a[u], R.a[u], eold, i == 1, i == g.m);
       const bool in = i >= 1 && i <= g.m;
-      out[u] = in ? v : eold;
+      out.a[u] = in ? v : eold;
       if (TRACK && in) e = max(e, abs_bits(v - eold));
     }
-    *reinterpret_cast<float4*>(ec + q) = make_float4(out[0], out[1], out[2], out[3]);
+    *reinterpret_cast<VecF<V>*>(ec + q) = out;
   }
   if (TRACK) block_max_atomic(e, err);
 }
@@ -751,21 +756,29 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
   K.small = 1.e-6f;
   K.omega = (float)sc.omega;
   K.omw = (float)(1.0 - sc.omega);
-  // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell)
-  const int chunks = (g.m >> 1) / 4 + 1;
+  // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
+  // 4 beat 2 per thread at 256^3 (1511 vs 1336 Mcell-steps/s for the step):
+  // the extra occupancy of narrower chunks does not pay for their extra
+  // instructions
+  constexpr int V = 4;
+  const int chunks = (g.m >> 1) / V + 1;
   const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
   const unsigned blocks = (unsigned)((threads + DC4_THREADS - 1) / DC4_THREADS);
+#define PF_DC(DIMV, TR) \
+  launch_pdl(k_sor_dc4<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo, colour, \
+             chunks, err, skip)
   if (g.dim == 3) {
     if (err)
-      launch_pdl(k_sor_dc4<3, true>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      PF_DC(3, true);
     else
-      launch_pdl(k_sor_dc4<3, false>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      PF_DC(3, false);
   } else {
     if (err)
-      launch_pdl(k_sor_dc4<2, true>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      PF_DC(2, true);
     else
-      launch_pdl(k_sor_dc4<2, false>, blocks, DC4_THREADS, st, g, K, epsc, epso, r, ec, eo, colour, chunks, err, skip);
+      PF_DC(2, false);
   }
+#undef PF_DC
 }
 
 int launch_forces(const Geo& g, const Scal& s, const double* poro, const double* p0, const double* p1,
