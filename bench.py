@@ -393,15 +393,21 @@ def run_ours(args):
     # ---- roofline of the dominant kernel (the red-black half-sweep) --------
     word = 8 if args.precision == "fp64" else 4
     sor_launch_ms = prof["sor_ms"] / max(prof["sor_launches"], 1)
-    # algorithmic bytes per half-sweep: the updated half of the cells x 5 words
-    # (own p read, neighbour p read, p write, bb, porosity)
-    alg_bytes = cells / 2 * 5 * word
+    # algorithmic bytes per launch: the cells one launch updates (half of them
+    # for a half-sweep, all of them for the fused full sweep of the precision
+    # form) x 5 words (own p read, neighbour p read, p write, bb, porosity)
+    sweeps = s.iter_max if args.precision == "fp64" else s.outer_max * s.inner_sweeps
+    updates = cells * sweeps * prof["steps"] / max(prof["sor_launches"], 1)
+    alg_bytes = updates * 5 * word
     achieved = alg_bytes / (sor_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    kname = f"sor_half_{args.precision}_{args.workload}"
+    fused = args.precision == "mixed" and prof["sor_launches"] == sweeps * prof["steps"]
+    kernel = "k_sor_half" if args.precision == "fp64" else ("k_sor_fused3" if fused else "k_sor_dc4")
+    kname = f"{'sor_fused' if fused else 'sor_half'}_{args.precision}_{args.workload}"
     traffic = ncu_traffic(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_kind, "kernel": "k_sor_half",
+                "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
+                "cell_updates_per_launch": updates,
                 "sor_share_of_step": prof["sor_ms"] / prof["step_ms"], "avg_launch_ms": sor_launch_ms,
                 "algorithmic_bytes_per_launch": alg_bytes}
     if args.precision == "fp64":

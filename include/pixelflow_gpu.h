@@ -76,8 +76,16 @@ typedef struct pf_options {
   int32_t track_sor_error; /* 1: compute the reference's SOR max-change */
   double dc_tol;           /* mixed: stop passes once max|r| <= dc_tol */
   int32_t use_graph;       /* 1: replay each step from a CUDA graph */
-  int32_t reserved[5];
+  int32_t sweep_form;      /* mixed: PF_SWEEP_AUTO fuses both colours of an
+                              FP32 sweep into one launch where the case allows
+                              it (3D, even n and l); PF_SWEEP_SPLIT launches
+                              one kernel per colour.  Same results bit for bit */
+  int32_t fused_rows;      /* mixed, fused sweep: y rows per CTA (0: auto) */
+  int32_t fused_planes;    /* mixed, fused sweep: z planes per CTA (0: auto) */
+  int32_t reserved[2];
 } pf_options;
+
+enum { PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1 };
 
 typedef struct pf_case pf_case;
 
@@ -262,6 +270,16 @@ int pf_batch_last_ms(pf_batch *b, double *ms);
 #define PF_NOALLOC_MAX_ROWS 262144
 int pf_max_div_noalloc(const pf_params *prm, const double *u, const double *v, const double *w,
                        const double *porosity, int ld1, int ld2, double *max_div, void *stream);
+
+/* Testing of the failure path of the fused correction sweep (no reference
+ * counterpart): from the next step on, the sweep's producer skips staging
+ * step `stage` of each run, so the consumers' bounded wait for it runs out
+ * (about 0.2 s), every CTA drains its own copies and the case's error word
+ * is set; pf_synchronize, pf_get_state and pf_norms then return
+ * PF_E_TIMEOUT for the rest of the case's life.  stage < 0 restores normal
+ * operation of later steps (the error word stays).  PF_E_STATE when the case
+ * does not run the fused sweep. */
+int pf_debug_fused_drop_stage(pf_case *c, int stage);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libpixelflow_gb300.so")
 PF_OK = 0
 PF_PREC_FP64 = 0
 PF_PREC_MIXED = 1
+PF_SWEEP_AUTO, PF_SWEEP_SPLIT = 0, 1
 ERRORS = {
     -1: "PF_E_INVALID", -2: "PF_E_CUDA", -3: "PF_E_NOMEM", -4: "PF_E_NONFINITE",
     -5: "PF_E_TIMEOUT", -6: "PF_E_STATE", -7: "PF_E_BUSY",
@@ -38,7 +39,8 @@ class PfOptions(ctypes.Structure):
     _fields_ = [
         ("precision", ctypes.c_int32), ("outer_max", ctypes.c_int32), ("inner_sweeps", ctypes.c_int32),
         ("track_sor_error", ctypes.c_int32), ("dc_tol", ctypes.c_double), ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("sweep_form", ctypes.c_int32), ("fused_rows", ctypes.c_int32), ("fused_planes", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 
@@ -102,6 +104,7 @@ _PROTOS = {
     "pf_profile_step_times": (_I, [_VP, _VP, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
+    "pf_debug_fused_drop_stage": (_I, [_VP, _I]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
     "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfBatchOptions), ctypes.POINTER(_VP)]),

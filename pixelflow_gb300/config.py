@@ -30,7 +30,8 @@ GROUPS = {
     "solver_control": ["iter_max", "relux_factor"],
 }
 GPU_GROUP = "gpu_control"
-GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls"]
+GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls",
+            "sweep_form", "fused_rows", "fused_planes"]
 WALL_FACES = ("top", "bottom", "east", "west", "north", "south")
 
 
@@ -66,6 +67,13 @@ class Settings:
     inner_sweeps: int = 25           # mixed: FP32 SOR iterations per pass
     dc_tol: float = 0.0              # mixed: stop the passes once max|r| <= dc_tol (0: run all)
     track_sor_error: bool = True     # keep the reference's SOR max-change diagnostic
+    # mixed: "auto" runs both colours of an FP32 sweep in one launch where the
+    # case allows it (3D, even n and l), "split" one launch per colour; the
+    # results are the same bit for bit.  fused_rows / fused_planes: the fused
+    # sweep's rows and planes per CTA (0: chosen from the grid and the device)
+    sweep_form: str = "auto"
+    fused_rows: int = 0
+    fused_planes: int = 0
     # inflow and initial velocities scaled by porosity: the boundary and initial
     # conditions of ibm_2d_backstep_omp_cpu.f90 (:533-534, :615-618)
     inflow_porosity: bool = False

@@ -416,6 +416,10 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "outer_max and inner_sweeps must be >= 0");
   if (rc == PF_OK && c->g.wall && c->opt.precision != PF_PREC_FP64)
     rc = fail(PF_E_INVALID, "wall_mode: the air-condition program runs in the plain FP64 form only");
+  if (rc == PF_OK && c->opt.sweep_form != PF_SWEEP_AUTO && c->opt.sweep_form != PF_SWEEP_SPLIT)
+    rc = fail(PF_E_INVALID, "unknown sweep_form");
+  if (rc == PF_OK && (c->opt.fused_rows < 0 || c->opt.fused_planes < 0))
+    rc = fail(PF_E_INVALID, "fused_rows and fused_planes must be >= 0");
   if (rc != PF_OK) {
     delete c;
     return rc;
@@ -533,6 +537,20 @@ static cudaMemcpy3DParms copy_params(const pf_case* c, const void* src, size_t s
   return P;
 }
 
+// The device error word: a bounded wait inside a kernel that gave up.
+static int flags_fail(unsigned long long f) {
+  if (f & PF_FLAG_FUSED_TIMEOUT)
+    return fail(PF_E_TIMEOUT, "fused correction sweep: a shared-memory staging wait expired");
+  return fail(PF_E_CUDA, "unknown device error flag");
+}
+static int check_flags(pf_case* c) {
+  PF_CUDA(cudaMemcpyAsync(&c->hred[RED_FLAGS], &c->red[RED_FLAGS], sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, c->st));
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  const unsigned long long f = c->hred[RED_FLAGS];
+  return f ? flags_fail(f) : PF_OK;
+}
+
 int pf_set_state(pf_case* c, const double* u, const double* v, const double* w, const double* p, int ld1,
                  int ld2) {
   if (!c || !u || !v || !p || (c->g.dim == 3 && !w)) return fail(PF_E_INVALID, "pf_set_state: null argument");
@@ -607,7 +625,7 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   rc = check_launch("pf_get_state");
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st));
-  return PF_OK;
+  return check_flags(c);
 }
 
 int pf_snapshot_begin(pf_case* c) {
@@ -748,7 +766,7 @@ int pf_step(pf_case* c, int nsteps) {
 int pf_synchronize(pf_case* c) {
   if (!c) return fail(PF_E_INVALID, "null handle");
   PF_CUDA(cudaStreamSynchronize(c->st));
-  return PF_OK;
+  return check_flags(c);
 }
 
 int pf_norms(pf_case* c, double* max_div, double* sor_error) {
@@ -778,6 +796,7 @@ int pf_norms(pf_case* c, double* max_div, double* sor_error) {
   if (std::isnan(ef) || (double)ef > e) e = (double)ef;  // NaN propagates
   if (sor_error) *sor_error = e;
   if (max_div) *max_div = d;
+  if (c->hred[RED_FLAGS]) return flags_fail(c->hred[RED_FLAGS]);
   if (!std::isfinite(d)) return fail(PF_E_NONFINITE, "max|div u| is not finite");
   return PF_OK;
 }
@@ -858,6 +877,18 @@ int pf_profile_step_times(pf_case* c, double* ms, int64_t max_steps, int64_t* n)
 int pf_kernel_launches(pf_case* c, int64_t* count) {
   if (!c || !count) return fail(PF_E_INVALID, "null argument");
   *count = c->launches;
+  return PF_OK;
+}
+
+int pf_debug_fused_drop_stage(pf_case* c, int stage) {
+  if (!c) return fail(PF_E_INVALID, "null handle");
+  if (!c->e2[0]) return fail(PF_E_STATE, "the case does not run the fused correction sweep");
+  c->fused.drop_stage = stage < 0 ? -1 : stage;
+  for (int b = 0; b < 2; b++)  // captured launches hold the old value
+    if (c->gexec[b]) {
+      cudaGraphExecDestroy(c->gexec[b]);
+      c->gexec[b] = nullptr;
+    }
   return PF_OK;
 }
 

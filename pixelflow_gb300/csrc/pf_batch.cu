@@ -497,7 +497,7 @@ int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
   const int d = g.dim;
   size_t b = nat8 * (6 + (d == 3) + 2 * d) + pk8 * (2 + 2 * (2 * d + 3));
   b += r256((size_t)(g.m + 2) * (g.n + 2) * g.Z * 8) + RED_TOTAL * sizeof(unsigned long long);
-  if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * 6 + 256;
+  if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * (mixed_fused(g, *opt) ? 8 : 6) + 256;
   *bytes = b;
   return PF_OK;
 }
@@ -605,12 +605,7 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
     std::memset(&d, 0, sizeof(d));
     d.g = c->g;
     d.s = c->s;
-    d.K.kx = (float)(c->s.dt / c->s.dx / c->s.dx);
-    d.K.ky = (float)(c->s.dt / c->s.dy / c->s.dy);
-    d.K.kz = c->g.dim == 3 ? (float)(c->s.dt / c->s.dz / c->s.dz) : 0.f;
-    d.K.small = 1.e-6f;
-    d.K.omega = (float)c->s.omega;
-    d.K.omw = (float)(1.0 - c->s.omega);
+    d.K = make_dc_const(c->s.dt, c->s.dx, c->s.dy, c->s.dz, c->g.dim, c->s.omega);
     d.poro = c->poro;
     d.gx = c->gx;
     d.gy = c->gy;

@@ -581,9 +581,25 @@ __device__ __forceinline__ void c_bnd_z(const Geo& g, T* u, T* v, T* w, double* 
 //   inlet/outlet edits), inlet: a_e += a_w, a_w = 0; outlet: all a_f = 0,
 //   e = (1-w) e + r - (w/ap) sum a_f e_f.
 struct DCConst {
-  float kx, ky, kz;  // dt/dx^2 etc.
-  float small, omega, omw;
+  // half face factors 0.5*dt/dx^2 etc. (exact halves of the float dt/dx^2)
+  // and twice the porosity floor: kx*max(small, (a+b)*0.5) is computed as
+  // hx*max(small2, a+b), the same float because the scalings by 2 are exact
+  float hx, hy, hz;
+  float small2, omega, omw;
 };
+// From the case's double scalars: dt/dx^2 etc., omega and 1 - omega, each
+// rounded to float once.
+__host__ __device__ inline DCConst make_dc_const(double dt, double dx, double dy, double dz, int dim,
+                                                 double omega) {
+  DCConst K;
+  K.hx = (float)(dt / dx / dx) * 0.5f;
+  K.hy = (float)(dt / dy / dy) * 0.5f;
+  K.hz = dim == 3 ? (float)(dt / dz / dz) * 0.5f : 0.f;
+  K.small2 = 2.e-6f;  // 2 * 1e-6f, exactly
+  K.omega = (float)omega;
+  K.omw = (float)(1.0 - omega);
+  return K;
+}
 
 // One cell of the correction sweep from its loaded operands.  Every form of
 // the sweep (the vectorised single-case kernel, the persistent batch kernel's
@@ -592,14 +608,14 @@ template <int DIM>
 __device__ __forceinline__ float dc_cell(const DCConst& K, float pc, float pe, float pw, float pn, float ps,
                                          float pt, float pb, float xe, float xw, float xn, float xs, float xt,
                                          float xb, float rr, float eold, bool inlet, bool outlet) {
-  float ae = K.kx * fmaxf(K.small, (pe + pc) * 0.5f);
-  float aw = K.kx * fmaxf(K.small, (pc + pw) * 0.5f);
-  const float an = K.ky * fmaxf(K.small, (pn + pc) * 0.5f);
-  const float as = K.ky * fmaxf(K.small, (pc + ps) * 0.5f);
+  float ae = K.hx * fmaxf(K.small2, pe + pc);
+  float aw = K.hx * fmaxf(K.small2, pc + pw);
+  const float an = K.hy * fmaxf(K.small2, pn + pc);
+  const float as = K.hy * fmaxf(K.small2, pc + ps);
   float at = 0.f, ab = 0.f;
   if (DIM == 3) {
-    at = K.kz * fmaxf(K.small, (pt + pc) * 0.5f);
-    ab = K.kz * fmaxf(K.small, (pc + pb) * 0.5f);
+    at = K.hz * fmaxf(K.small2, pt + pc);
+    ab = K.hz * fmaxf(K.small2, pc + pb);
   }
   const float ap = -ae - aw - an - as - at - ab;
   float enew = fmaf(K.omw, eold, rr);

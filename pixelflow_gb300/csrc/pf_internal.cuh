@@ -58,7 +58,10 @@ __host__ __device__ inline int colour_of(const Geo& g, int i, int j, int k) {
 // atomics over RED_SLOTS addresses (one address would serialise tens of
 // thousands of atomics per launch in L2); readers take the max of the slots.
 constexpr int RED_SLOTS = 256;
-enum { RED_ERR = 0, RED_ERRF = 256, RED_DIV = 512, RED_RMAX = 768, RED_TOTAL = 1024 };
+enum { RED_ERR = 0, RED_ERRF = 256, RED_DIV = 512, RED_RMAX = 768, RED_FLAGS = 1024, RED_TOTAL = 1056 };
+// Bits of the case's device error word (red[RED_FLAGS]), sticky until the
+// case is destroyed; the host reports them as PF_E_TIMEOUT.
+enum { PF_FLAG_FUSED_TIMEOUT = 1 };
 
 // Scalars of one case, derived once on the host in double.
 struct Scal {
@@ -158,6 +161,25 @@ void launch_zero_int(int* p, cudaStream_t st);
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);
+// Fused full correction sweep (both colours in one launch, 3D with even n
+// and l): launch shape chosen once per case.
+struct FusedShape {
+  int ty = 0;              // rows per tile
+  int per_cta = 0;         // (tile, plane) pairs per CTA
+  int threads = 0, chunks = 0, ntiles = 0, grid = 0;
+  size_t smem = 0;         // dynamic shared memory per CTA
+  int drop_stage = -1;     // testing: a stage never issued, so its bounded wait runs out
+};
+// 3D, no walls, even n and l, and the staging rings of two-row tiles fit in
+// shared memory.
+bool fused_eligible(const Geo& g);
+// ty_req <= 0 picks the tile height; tz_req > 0 caps the planes of a CTA's
+// runs (more CTAs than SMs); sms = multiprocessors of the device.  Returns a
+// cudaError_t value (0 on success).
+int fused_setup(const Geo& g, int ty_req, int tz_req, int sms, FusedShape& fs);
+void launch_sor_fused(const Geo& g, const Scal& sc, const FusedShape& fs, const float* const eps[2],
+                      const float* const r[2], const float* const ea[2], float* const eb[2],
+                      unsigned long long* err, unsigned long long* flags, const int* skip, cudaStream_t st);
 void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cudaStream_t st);
 // Force-log sums: scratch holds 6 doubles per block of 256 cells; out[0..2]
 // pressure part, out[3..5] friction part (device).  Returns the block count.

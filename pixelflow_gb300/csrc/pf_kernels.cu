@@ -20,6 +20,8 @@
 // the SOR iteration count are the reference's exactly.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pf_internal.cuh"
 #include "pf_cells.cuh"
 
@@ -32,11 +34,12 @@ namespace {
 // tail of the current one; CUDA graph capture keeps these as programmatic
 // edges.
 template <typename... KArgs, typename... Args>
-void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+void launch_pdl_smem(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -44,6 +47,10 @@ void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  launch_pdl_smem(kernel, grid, block, 0, st, args...);
 }
 
 inline dim3 grid_interior(const Geo& g) {
@@ -509,6 +516,38 @@ __device__ __forceinline__ VecF<V> ldv(const float* p) {
   return *reinterpret_cast<const VecF<V>*>(p);
 }
 
+// The V cells of one chunk from its loaded operand rows: own correction EC,
+// residual R and porosity PC; the other colour's correction XO and porosity
+// PO at the same slots plus the one slot before (s = 0) or after (s = 1)
+// them (xx, px); the other colour's rows north/south/top/bottom.  Lanes
+// outside 1 <= i <= m keep their old value.  Every chunked form of the sweep
+// calls this, so they agree bit for bit.
+template <int DIM, bool TRACK, int V>
+__device__ __forceinline__ VecF<V> dc_chunk(const Geo& g, const DCConst& K, int h0, int s, const VecF<V>& EC,
+                                            const VecF<V>& R, const VecF<V>& PC, const VecF<V>& XO,
+                                            const VecF<V>& PO, float xx, float px, const VecF<V>& XN,
+                                            const VecF<V>& XS, const VecF<V>& PN, const VecF<V>& PS,
+                                            const VecF<V>& XT, const VecF<V>& XB, const VecF<V>& PT,
+                                            const VecF<V>& PB, unsigned& e) {
+  VecF<V> out;
+#pragma unroll
+  for (int u = 0; u < V; u++) {
+    const int i = 2 * (h0 + u) + s;
+    const float eold = EC.a[u];
+    // east = other colour at h + s, west at h - 1 + s
+    const float xe = s ? (u < V - 1 ? XO.a[u + 1] : xx) : XO.a[u];
+    const float xw = s ? XO.a[u] : (u > 0 ? XO.a[u - 1] : xx);
+    const float pe = s ? (u < V - 1 ? PO.a[u + 1] : px) : PO.a[u];
+    const float pw = s ? PO.a[u] : (u > 0 ? PO.a[u - 1] : px);
+    const float v = dc_cell<DIM>(K, PC.a[u], pe, pw, PN.a[u], PS.a[u], PT.a[u], PB.a[u], xe, xw, XN.a[u], XS.a[u],
+                                 XT.a[u], XB.a[u], R.a[u], eold, i == 1, i == g.m);
+    const bool in = i >= 1 && i <= g.m;
+    out.a[u] = in ? v : eold;
+    if (TRACK && in) e = max(e, abs_bits(v - eold));
+  }
+  return out;
+}
+
 template <int DIM, bool TRACK, int V>
 __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const float* __restrict__ epsc,
                                                          const float* __restrict__ epso,
@@ -545,25 +584,320 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
       PT = ldv<V>(epso + q + HY);
       PB = ldv<V>(epso + q - HY);
     }
-    VecF<V> out;
-#pragma unroll
-    for (int u = 0; u < V; u++) {
-      const int i = 2 * (h0 + u) + s;
-      const float eold = EC.a[u];
-      // east = other colour at h + s, west at h - 1 + s
-      const float xe = s ? (u < V - 1 ? XO.a[u + 1] : xx) : XO.a[u];
-      const float xw = s ? XO.a[u] : (u > 0 ? XO.a[u - 1] : xx);
-      const float pe = s ? (u < V - 1 ? PO.a[u + 1] : px) : PO.a[u];
-      const float pw = s ? PO.a[u] : (u > 0 ? PO.a[u - 1] : px);
-      const float v = dc_cell<DIM>(K, PC.a[u], pe, pw, PN.a[u], PS.a[u], PT.a[u], PB.a[u], xe, xw, XN.a[u],
-                                   XS.a[u], XT.a[u], XB.a[u], R.a[u], eold, i == 1, i == g.m);
-      const bool in = i >= 1 && i <= g.m;
-      out.a[u] = in ? v : eold;
-      if (TRACK && in) e = max(e, abs_bits(v - eold));
-    }
-    *reinterpret_cast<VecF<V>*>(ec + q) = out;
+    *reinterpret_cast<VecF<V>*>(ec + q) =
+        dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, PC, XO, PO, xx, px, XN, XS, PN, PS, XT, XB, PT, PB, e);
   }
   if (TRACK) block_max_atomic(e, err);
+}
+
+// Fused full correction sweep, 3D with even n and l (the periodic y/z edges
+// then read the opposite interior rows, which have the other colour): both
+// colours of one sweep in one launch, each operand row streamed from HBM
+// once per sweep by the bulk-copy (TMA) engine.
+//
+// Work: tiles of ty rows over the whole x extent, walked in z.  The
+// (tile, plane) pairs are dealt out to one persistent CTA per SM in
+// contiguous runs; a run that crosses a tile boundary is two segments.
+// Within a segment [k0, k1) of tile j0 .. j0+ny-1, step `it` (k = k0-1+it)
+// updates colour 0 of plane k on rows j0-1 .. j0+ny, then colour 1 of plane
+// k-1.  Each thread owns one chunk of V slots of one of those rows for the
+// whole segment and walks it in z, so the z neighbours and its own colour-0
+// results of the planes before stay in registers; only the other rows'
+// values go through shared memory (a three-plane ring of colour-0 results).
+// Halo rows and planes beyond a periodic edge are the opposite interior rows
+// and planes.  Colour 0 of the halo rows and of planes k0-1 and k1 is
+// recomputed here from the same operands, so every value equals the
+// two-launch sweep's bit for bit.  The correction is read from ea (its state
+// before the sweep) and written to eb, so a neighbouring CTA's halo
+// computation sees old values.
+//
+// Staging: one thread issues, per step, the cp.async.bulk copies (one per
+// run of rows contiguous in memory) of what the step after next needs:
+// colour-1 correction and porosity of plane k+1 with two rows of halo,
+// colour-0 porosity, correction and residual of plane k, colour-1 residual of
+// plane k-1, into shared-memory rings, and arms an mbarrier with their byte
+// count; the consumers wait on it (bounded: after FUSED_WAIT_NS the CTA
+// drains its copies in flight, raises PF_FLAG_FUSED_TIMEOUT and leaves).  A
+// stage overwrites only ring slots whose last reader finished before the
+// step's barrier.
+constexpr int FUSED_MAX_THREADS = 512;
+constexpr int FUSED_V = 4;
+constexpr int FZE = 4;       // ring depth of E1, P1: planes k, k+1 read, two ahead
+constexpr int FZP = 4;       // ring depth of P0: planes k-1, k read, two ahead
+constexpr int FZ1 = 3;       // ring depth of E0, R0, R1: one plane read, two ahead
+constexpr int FZR = 3;       // colour-0 result ring: plane k-1 read while plane k is written
+constexpr int FSTAGES = 3;   // mbarriers: the stage being read and two in flight
+constexpr unsigned long long FUSED_WAIT_NS = 200000000ULL;  // 0.2 s; a stage lands in microseconds
+constexpr int FUSED_WAIT_POLLS = 1 << 20;                    // backstop on the number of polls
+constexpr size_t FUSED_SMEM_MAX = 232448;  // dynamic shared memory per CTA on sm_100-class parts
+
+struct FusedArgs {
+  const float* eps[2];  // packed FP32 porosity of colour 0, 1
+  const float* r[2];    // packed FP32 residual
+  const float* ea[2];   // correction before the sweep
+  float* eb[2];         // correction after the sweep
+  unsigned long long* err;
+  unsigned long long* flags;
+  const int* skip;
+  int drop_stage;  // testing: a stage index never issued (its wait runs out), -1 otherwise
+};
+
+// Shared-memory layout in floats: mbarriers, then the rings, each region
+// followed by one pad vector (reads one slot before a row's start or up to
+// three past its end, by lanes whose results are discarded, stay inside).
+struct FusedLayout {
+  int e1, p1, p0, e0, r0, r1, red, total;
+};
+__host__ __device__ inline FusedLayout fused_layout(int ty, int H, int chunks) {
+  FusedLayout L;
+  const int rows1 = ty + 4, rows0 = ty + 2;
+  int o = 16 + FUSED_V;
+  L.e1 = o;
+  o += FZE * rows1 * H + FUSED_V;
+  L.p1 = o;
+  o += FZE * rows1 * H + FUSED_V;
+  L.p0 = o;
+  o += FZP * rows0 * H + FUSED_V;
+  L.e0 = o;
+  o += FZ1 * rows0 * H + FUSED_V;
+  L.r0 = o;
+  o += FZ1 * rows0 * H + FUSED_V;
+  L.r1 = o;
+  o += FZ1 * ty * H + FUSED_V;
+  L.red = o;
+  o += FZR * rows0 * (chunks * FUSED_V + 2 * FUSED_V) + FUSED_V;
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+// One test of an mbarrier phase; a thread whose phase is not complete may be
+// suspended for up to FUSED_SUSPEND_NS (woken early when the phase
+// completes), so waiting warps do not spin on the issue slots.
+constexpr unsigned FUSED_SUSPEND_NS = 20000;
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(FUSED_SUSPEND_NS)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for a phase of an mbarrier, giving up after FUSED_WAIT_NS.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (int i = 1; i < FUSED_WAIT_POLLS; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 0 && global_ns() - t0 > FUSED_WAIT_NS) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_copy(float* dst, const float* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+template <bool TRACK>
+__global__ void __launch_bounds__(FUSED_MAX_THREADS)
+    k_sor_fused3(Geo g, DCConst K, FusedArgs A, int chunks, int ty, int ntiles, int per_cta) {
+  constexpr int V = FUSED_V;
+  extern __shared__ __align__(128) float sm[];
+  __shared__ int abort_flag;
+  pdl_begin();
+  if (A.skip && *A.skip) return;
+  const int H = g.H;
+  const FusedLayout L = fused_layout(ty, H, chunks);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm);
+  const int P = chunks * V + 2 * V;  // result ring row pitch: slot h at V + h
+  const int plane1 = (ty + 4) * H, plane0 = (ty + 2) * H, planeR1 = ty * H, planeRed = (ty + 2) * P;
+  const unsigned rowb = (unsigned)H * sizeof(float);
+  const long long total = (long long)ntiles * g.l;
+  const long long lo = (long long)blockIdx.x * per_cta;
+  const long long hi = lo + per_cta < total ? lo + per_cta : total;
+  // the producer: lane 0 of the last warp, whose threads own the top halo row
+  // (colour 0 only) or nothing
+  const int producer = (blockDim.x - 1) & ~31;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < FSTAGES; b++) mbar_init(&bar[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  for (int x = threadIdx.x; x < FZR * planeRed; x += blockDim.x) sm[L.red + x] = 0.f;
+  __syncthreads();
+  auto wrapy = [&](int j) { return j < 1 ? j + g.n : (j > g.n ? j - g.n : j); };
+  auto wrapz = [&](int k) { return k < 1 ? k + g.l : (k > g.l ? k - g.l : k); };
+  // stage counters: mbarrier count % FSTAGES, parity (count / FSTAGES) & 1;
+  // `confirmed` stages are known (to the producer) to have landed
+  unsigned issued = 0, waited = 0, confirmed = 0, dropped = ~0u;
+  unsigned e = 0;
+  bool ok = true;
+  // this thread's chunk: row rl of the colour-0 rows j0-1 .. j0+ny, slots h0 ..
+  const int rl = threadIdx.x / chunks;
+  const int h0 = (threadIdx.x - rl * chunks) * V;
+  for (long long pos = lo; pos < hi && ok;) {
+    const int tile = (int)(pos / g.l);
+    const int k0 = (int)(pos - (long long)tile * g.l) + 1;
+    const int k1 = (int)(hi - pos < (long long)(g.l + 1 - k0) ? k0 + (hi - pos) : g.l + 1);
+    pos += k1 - k0;
+    const int j0 = 1 + tile * ty, ny = min(ty, g.n - j0 + 1);
+    const int nit = k1 - k0 + 2;  // steps: colour 0 of planes k0-1 .. k1
+    // stage `it`: the rows step `it` reads that no earlier stage brought
+    auto issue = [&](int it) {
+      if (it == A.drop_stage) {
+        dropped = issued++;
+        return;
+      }
+      const int k = k0 - 1 + it;
+      const unsigned rows = (unsigned)(2 * (ny + 4) * (it == 0 ? 3 : 1) + 3 * (ny + 2) + (it >= 2 ? ny : 0));
+      unsigned long long* b = &bar[issued % FSTAGES];
+      mbar_expect_tx(b, rows * rowb);
+      // rows jfirst .. jfirst+nrows-1 of plane kk (jfirst may lie up to two
+      // rows beyond a periodic edge) of up to three arrays into consecutive
+      // ring rows: one bulk copy per run of rows contiguous in memory
+      auto rows_copy = [&](int jfirst, int nrows, int kk, float* d0, const float* s0, float* d1, const float* s1,
+                           float* d2, const float* s2) {
+        for (int r = 0; r < nrows;) {
+          const int u = jfirst + r;
+          const int len = min(nrows - r, u < 1 ? 1 - u : (u <= g.n ? g.n + 1 - u : 2 * g.n + 1 - u));
+          const idx_t src = pk_idx(g, 0, wrapy(u), kk);
+          const unsigned bytes = (unsigned)len * rowb;
+          bulk_copy(d0 + r * H, s0 + src, bytes, b);
+          if (d1) bulk_copy(d1 + r * H, s1 + src, bytes, b);
+          if (d2) bulk_copy(d2 + r * H, s2 + src, bytes, b);
+          r += len;
+        }
+      };
+      for (int d = it == 0 ? -1 : 1; d <= 1; d++) {  // E1, P1 of plane k+d (plane index it+1+d)
+        const int slot = (it + 1 + d) % FZE;
+        rows_copy(j0 - 2, ny + 4, wrapz(k + d), sm + L.e1 + slot * plane1, A.ea[1], sm + L.p1 + slot * plane1,
+                  A.eps[1], nullptr, nullptr);
+      }
+      rows_copy(j0 - 1, ny + 2, wrapz(k), sm + L.p0 + (it % FZP) * plane0, A.eps[0],
+                sm + L.e0 + (it % FZ1) * plane0, A.ea[0], sm + L.r0 + (it % FZ1) * plane0, A.r[0]);
+      if (it >= 2)  // R1 of plane k-1 (interior: k0 <= k-1 < k1)
+        rows_copy(j0, ny, k - 1, sm + L.r1 + ((it - 1) % FZ1) * planeR1, A.r[1], nullptr, nullptr, nullptr,
+                  nullptr);
+      issued++;
+    };
+    if (threadIdx.x == producer) {
+      issue(0);
+      if (nit > 1) issue(1);
+    }
+    const bool red_item = rl < ny + 2;            // a colour-0 chunk of this tile
+    const bool black_item = rl >= 1 && rl <= ny;  // ... whose row is the tile's own
+    const int jw = wrapy(j0 - 1 + rl);
+    // z queues of this chunk: colour-1 correction and porosity of its row at
+    // planes k-1, k, k+1 (+ the side slot of planes k, k+1), colour-0
+    // porosity and results at planes k-2, k-1, k
+    VecF<V> qE0{}, qE1{}, qE2{}, qP0{}, qP1{}, qP2{}, c0{}, c1{}, c2{}, o0{}, o1{}, o2{};
+    float sE1 = 0.f, sE2 = 0.f, sP1 = 0.f, sP2 = 0.f;
+    for (int it = 0; it < nit; it++) {
+      const int k = k0 - 1 + it, kw = wrapz(k);
+      if (mbar_wait_bounded(&bar[waited % FSTAGES], (waited / FSTAGES) & 1))
+        confirmed = waited + 1;
+      else
+        abort_flag = 1;
+      waited++;
+      if (red_item) {  // colour 0 of plane k
+        const int s = (jw + kw) & 1;
+        const float* E1c = sm + L.e1 + ((it + 1) % FZE) * plane1 + (rl + 1) * H + h0;  // row jw, plane k
+        const float* E1p = sm + L.e1 + ((it + 2) % FZE) * plane1 + (rl + 1) * H + h0;  // plane k+1
+        const float* P1c = sm + L.p1 + ((it + 1) % FZE) * plane1 + (rl + 1) * H + h0;
+        const float* P1p = sm + L.p1 + ((it + 2) % FZE) * plane1 + (rl + 1) * H + h0;
+        const int o = rl * H + h0;
+        if (it == 0) {
+          const float* E1m = sm + L.e1 + (it % FZE) * plane1 + (rl + 1) * H + h0;
+          const float* P1m = sm + L.p1 + (it % FZE) * plane1 + (rl + 1) * H + h0;
+          qE1 = ldv<V>(E1c);
+          qP1 = ldv<V>(P1c);
+          qE2 = ldv<V>(E1m);  // shifted into qE0 below
+          qP2 = ldv<V>(P1m);
+          sE2 = s ? E1c[V] : E1c[-1];
+          sP2 = s ? P1c[V] : P1c[-1];
+          qE0 = qE2;
+          qP0 = qP2;
+          sE1 = sE2;
+          sP1 = sP2;
+        } else {
+          qE0 = qE1;
+          qE1 = qE2;
+          qP0 = qP1;
+          qP1 = qP2;
+          sE1 = sE2;
+          sP1 = sP2;
+        }
+        qE2 = ldv<V>(E1p);
+        qP2 = ldv<V>(P1p);
+        sE2 = s ? E1p[-1] : E1p[V];  // plane k+1 has the other parity
+        sP2 = s ? P1p[-1] : P1p[V];
+        c0 = c1;
+        c1 = c2;
+        c2 = ldv<V>(sm + L.p0 + (it % FZP) * plane0 + o);
+        const VecF<V> EC = ldv<V>(sm + L.e0 + (it % FZ1) * plane0 + o);
+        const VecF<V> R = ldv<V>(sm + L.r0 + (it % FZ1) * plane0 + o);
+        const VecF<V> XN = ldv<V>(E1c + H), XS = ldv<V>(E1c - H), PN = ldv<V>(P1c + H), PS = ldv<V>(P1c - H);
+        unsigned unused = 0;
+        o0 = o1;
+        o1 = o2;
+        o2 = dc_chunk<3, false, V>(g, K, h0, s, EC, R, c2, qE1, qP1, sE1, sP1, XN, XS, PN, PS, qE2, qE0, qP2, qP0,
+                                   unused);
+        *reinterpret_cast<VecF<V>*>(sm + L.red + (it % FZR) * planeRed + rl * P + V + h0) = o2;
+        if (black_item && k >= k0 && k < k1)
+          *reinterpret_cast<VecF<V>*>(A.eb[0] + pk_idx(g, h0, jw, kw)) = o2;
+      }
+      __syncthreads();
+      if (abort_flag) {  // uniform after the barrier
+        ok = false;
+        break;
+      }
+      if (threadIdx.x == producer && it + 2 < nit) {
+        // the slots this stage overwrites were last read before the barrier
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(it + 2);
+      }
+      if (it >= 2 && black_item) {  // colour 1 of plane kb = k-1, row jw
+        const int kb = k - 1;
+        const int s = (1 + jw + kb) & 1;
+        const float* P0b = sm + L.p0 + ((it - 1) % FZP) * plane0 + rl * H + h0;
+        const float* Rb = sm + L.red + ((it - 1) % FZR) * planeRed + rl * P + V + h0;
+        const VecF<V> R = ldv<V>(sm + L.r1 + ((it - 1) % FZ1) * planeR1 + (rl - 1) * H + h0);
+        const float px = s ? P0b[V] : P0b[-1];
+        const float xx = s ? Rb[V] : Rb[-1];
+        const VecF<V> PN = ldv<V>(P0b + H), PS = ldv<V>(P0b - H);
+        const VecF<V> XN = ldv<V>(Rb + P), XS = ldv<V>(Rb - P);
+        *reinterpret_cast<VecF<V>*>(A.eb[1] + pk_idx(g, h0, jw, kb)) =
+            dc_chunk<3, TRACK, V>(g, K, h0, s, qE0, R, qP0, o1, c1, xx, px, XN, XS, PN, PS, o2, o0, c2, c0, e);
+      }
+    }
+    __syncthreads();  // the next segment's first stages overwrite the rings
+  }
+  if (!ok) {
+    // leave no copy in flight into this CTA's shared memory: wait (bounded)
+    // for every stage issued and not seen to land, the one that ran out too
+    if (threadIdx.x == producer) {
+      for (unsigned sg = confirmed; sg < issued; sg++)
+        if (sg != dropped) mbar_wait_bounded(&bar[sg % FSTAGES], (sg / FSTAGES) & 1);
+      atomicOr(A.flags, (unsigned long long)PF_FLAG_FUSED_TIMEOUT);
+    }
+    return;
+  }
+  if (TRACK) block_max_atomic(e, A.err);
 }
 
 // FP32 porosity packed by colour (all positions, ghosts included).
@@ -747,15 +1081,13 @@ void launch_residual(const Geo& g, const Coef<double>& C, const double* pc, cons
     launch_pdl(k_residual<2>, grid, SWEEP_THREADS, st, g, C, pc, po, omega, colour, rf, ec, rmax, skip);
 }
 
+static DCConst dc_const(const Geo& g, const Scal& sc) {
+  return make_dc_const(sc.dt, sc.dx, sc.dy, sc.dz, g.dim, sc.omega);
+}
+
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st) {
-  DCConst K;
-  K.kx = (float)(sc.dt / sc.dx / sc.dx);
-  K.ky = (float)(sc.dt / sc.dy / sc.dy);
-  K.kz = g.dim == 3 ? (float)(sc.dt / sc.dz / sc.dz) : 0.f;
-  K.small = 1.e-6f;
-  K.omega = (float)sc.omega;
-  K.omw = (float)(1.0 - sc.omega);
+  const DCConst K = dc_const(g, sc);
   // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
   // 4 beat 2 per thread at 256^3 (1511 vs 1336 Mcell-steps/s for the step):
   // the extra occupancy of narrower chunks does not pay for their extra
@@ -779,6 +1111,77 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
       PF_DC(2, false);
   }
 #undef PF_DC
+}
+
+static int fused_chunks(const Geo& g) { return (g.m >> 1) / FUSED_V + 1; }
+static size_t fused_smem(const Geo& g, int ty) {
+  return (size_t)fused_layout(ty, g.H, fused_chunks(g)).total * sizeof(float);
+}
+
+bool fused_eligible(const Geo& g) {
+  return g.dim == 3 && !g.wall && g.n % 2 == 0 && g.l % 2 == 0 && fused_smem(g, 2) <= FUSED_SMEM_MAX &&
+         4 * fused_chunks(g) <= FUSED_MAX_THREADS;
+}
+
+int fused_setup(const Geo& g, int ty_req, int tz_req, int sms, FusedShape& fs) {
+  const int chunks = fused_chunks(g);
+  // tile height: the largest whose rings fit and whose chunks fit one CTA.
+  // A CTA's step is latency-bound, so more rows per step (more threads, fewer
+  // steps per CTA) wins although the halo rows are updated twice: at 256^3
+  // the sweep took 114, 105, 102 and 99 us with 8, 10, 11 and 12 rows.
+  int ty = 0;
+  for (int t = 1; t <= std::min(16, g.n); t++) {
+    if (ty_req > 0 ? t != std::min(ty_req, g.n) : t < 2) continue;
+    if (fused_smem(g, t) > FUSED_SMEM_MAX || (t + 2) * chunks > FUSED_MAX_THREADS) continue;
+    ty = t;
+  }
+  if (ty == 0) return (int)cudaErrorInvalidValue;
+  const size_t smem = fused_smem(g, ty);
+  const int threads = ((ty + 2) * chunks + 31) / 32 * 32;  // one chunk per thread
+  for (void* k : {(void*)k_sor_fused3<false>, (void*)k_sor_fused3<true>}) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sor_fused3<true>, threads, smem);
+  if (e != cudaSuccess) return (int)e;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  const int ntiles = (g.n + ty - 1) / ty;
+  const long long pairs = (long long)ntiles * g.l;
+  // one wave of persistent CTAs, each a contiguous run of (tile, plane) pairs
+  long long per_cta = (pairs + (long long)sms * per_sm - 1) / ((long long)sms * per_sm);
+  if (tz_req > 0) per_cta = std::min<long long>(per_cta, tz_req);
+  fs.ty = ty;
+  fs.per_cta = (int)per_cta;
+  fs.threads = threads;
+  fs.chunks = chunks;
+  fs.ntiles = ntiles;
+  fs.grid = (int)((pairs + per_cta - 1) / per_cta);
+  fs.smem = smem;
+  return 0;
+}
+
+void launch_sor_fused(const Geo& g, const Scal& sc, const FusedShape& fs, const float* const eps[2],
+                      const float* const r[2], const float* const ea[2], float* const eb[2],
+                      unsigned long long* err, unsigned long long* flags, const int* skip, cudaStream_t st) {
+  FusedArgs A;
+  for (int c = 0; c < 2; c++) {
+    A.eps[c] = eps[c];
+    A.r[c] = r[c];
+    A.ea[c] = ea[c];
+    A.eb[c] = eb[c];
+  }
+  A.err = err;
+  A.flags = flags;
+  A.skip = skip;
+  A.drop_stage = fs.drop_stage;
+  const DCConst K = dc_const(g, sc);
+  if (err)
+    launch_pdl_smem(k_sor_fused3<true>, dim3(fs.grid), dim3(fs.threads), fs.smem, st, g, K, A, fs.chunks, fs.ty,
+                    fs.ntiles, fs.per_cta);
+  else
+    launch_pdl_smem(k_sor_fused3<false>, dim3(fs.grid), dim3(fs.threads), fs.smem, st, g, K, A, fs.chunks, fs.ty,
+                    fs.ntiles, fs.per_cta);
 }
 
 int launch_forces(const Geo& g, const Scal& s, const double* poro, const double* p0, const double* p1,

@@ -21,6 +21,10 @@
 
 namespace pf {
 
+bool mixed_fused(const Geo& g, const pf_options& opt) {
+  return opt.precision == PF_PREC_MIXED && opt.sweep_form == PF_SWEEP_AUTO && fused_eligible(g);
+}
+
 int mixed_alloc(pf_case* c) {
   const Geo& g = c->g;
   const size_t nat = (size_t)g.nat * sizeof(float), pk = (size_t)g.pk * sizeof(float);
@@ -40,10 +44,19 @@ int mixed_alloc(pf_case* c) {
   req[nr++] = {&c->gzf, three ? nat : 0};
   req[nr++] = {&c->rinvf, nat};
   req[nr++] = {&c->dampf, nat};
+  const bool fused = mixed_fused(c->g, c->opt);
   for (int col = 0; col < 2; col++) {
     req[nr++] = {&c->e[col], pk};
     req[nr++] = {&c->rf[col], pk};
     req[nr++] = {&c->epsf[col], pk};
+    req[nr++] = {&c->e2[col], fused ? pk : 0};
+  }
+  if (fused) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int fe = fused_setup(c->g, c->opt.fused_rows, c->opt.fused_planes, sms, c->fused);
+    if (fe) return cuda_fail((cudaError_t)fe, "fused sweep set-up");
   }
   size_t total = 256;  // flag
   for (int r = 0; r < nr; r++) total += (req[r].bytes + 255) / 256 * 256;
@@ -105,28 +118,46 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);
+  const bool fused = c->e2[0] != nullptr;
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
     launch_zero_u64(&c->red[RED_RMAX], RED_SLOTS, st);
     for (int col = 0; col < 2; col++)
       launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col],
                       &c->red[RED_RMAX], skip, st);
     if (early) launch_dc_check(&c->red[RED_RMAX], c->opt.dc_tol * s.omega, c->skip, st);
-    for (int it = 0; it < c->opt.inner_sweeps; it++) {
-      for (int col = 0; col < 2; col++) {
-        if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
-        unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
-        launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err, skip,
-                      st);
+    const float* efin[2] = {c->e[0], c->e[1]};
+    if (fused) {
+      // e (zeroed by the residual) -> e2 -> e -> ...: the result of an odd
+      // number of sweeps is in e2
+      for (int it = 0; it < c->opt.inner_sweeps; it++) {
+        const float* ea[2] = {it & 1 ? c->e2[0] : c->e[0], it & 1 ? c->e2[1] : c->e[1]};
+        float* eb[2] = {it & 1 ? c->e[0] : c->e2[0], it & 1 ? c->e[1] : c->e2[1]};
+        launch_sor_fused(g, s, c->fused, c->epsf, c->rf, ea, eb, track ? &c->red[RED_ERRF] : nullptr,
+                         &c->red[RED_FLAGS], skip, st);
+      }
+      if (c->opt.inner_sweeps & 1) {
+        efin[0] = c->e2[0];
+        efin[1] = c->e2[1];
+      }
+    } else {
+      for (int it = 0; it < c->opt.inner_sweeps; it++) {
+        for (int col = 0; col < 2; col++) {
+          if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
+          unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
+          launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err,
+                        skip, st);
+        }
       }
     }
-    launch_accumulate(g, c->p[0], c->p[1], c->e[0], c->e[1], skip, st);
+    launch_accumulate(g, c->p[0], c->p[1], efin[0], efin[1], skip, st);
     if (halo) launch_p_halo<double>(g, c->p[0], c->p[1], skip, st);
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
   launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
+  const int64_t per_sweep = fused ? 1 : 2 * (halo ? 2 : 1);
   c->launches += 4 + (track ? 1 : 0) + (early ? 1 : 0) +
                  (int64_t)c->opt.outer_max *
-                     (4 + (early ? 1 : 0) + (halo ? 1 : 0) + (int64_t)c->opt.inner_sweeps * 2 * (halo ? 2 : 1));
+                     (4 + (early ? 1 : 0) + (halo ? 1 : 0) + (int64_t)c->opt.inner_sweeps * per_sweep);
   c->cur = nw;
 }
 

@@ -9,6 +9,7 @@ module pixelflow_gpu
 
   integer(c_int), parameter :: PF_OK = 0
   integer(c_int), parameter :: PF_PREC_FP64 = 0, PF_PREC_MIXED = 1
+  integer(c_int), parameter :: PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1
 
   type, bind(C) :: pf_params
     integer(c_int32_t) :: dim, m, n, l
@@ -24,7 +25,10 @@ module pixelflow_gpu
     integer(c_int32_t) :: precision, outer_max, inner_sweeps, track_sor_error
     real(c_double) :: dc_tol
     integer(c_int32_t) :: use_graph
-    integer(c_int32_t) :: reserved(5)
+    integer(c_int32_t) :: sweep_form
+    integer(c_int32_t) :: fused_rows
+    integer(c_int32_t) :: fused_planes
+    integer(c_int32_t) :: reserved(2)
   end type pf_options
 
   interface

@@ -23,6 +23,7 @@ from .config import Settings, read_porosity_csv, read_settings
 from ._lib import PfOptions, PfParams, check
 
 PRECISIONS = {"fp64": _lib.PF_PREC_FP64, "plain": _lib.PF_PREC_FP64, "mixed": _lib.PF_PREC_MIXED}
+SWEEP_FORMS = {"auto": _lib.PF_SWEEP_AUTO, "split": _lib.PF_SWEEP_SPLIT}
 
 
 def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
@@ -49,6 +50,12 @@ def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
     o.dc_tol = float(s.dc_tol)
     o.track_sor_error = 1 if s.track_sor_error else 0
     o.use_graph = 1 if use_graph else 0
+    form = str(s.sweep_form).lower()
+    if form not in SWEEP_FORMS:
+        raise ValueError(f"unknown sweep_form {s.sweep_form!r}")
+    o.sweep_form = SWEEP_FORMS[form]
+    o.fused_rows = int(s.fused_rows)
+    o.fused_planes = int(s.fused_planes)
     return o
 
 
