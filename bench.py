@@ -2,6 +2,7 @@
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                 [--workload spheres3d_256|spheres3d_384|cylinder2d] [--precision fp64|mixed]
+                [--sweep-form auto|split|fused]
 
 One step = one time step of the whole case (snapshot, predictor, RHS,
 iter_max red-black SOR iterations, projection, boundary).  Default workload:
@@ -365,6 +366,8 @@ def run_ours(args):
     from pixelflow_gb300.solver import Case, host_register, host_unregister
     _lib.check(_lib.load().pf_set_device(local))
     s, shape, vals, desc = workload(args.workload, args.precision)
+    if args.precision == "mixed":
+        s = s.replace(sweep_form=args.sweep_form)
     cells = int(np.prod(shape))
     case = Case(s, shape, vals)
     case.initial_conditions()
@@ -467,6 +470,7 @@ def run_ours(args):
         mp = mc.profile_end()
         mdiv, _ = mc.norms()
         mstate = mc.get_state()
+        msweep = mc.sweep_info()
         mc.close()
         # relative L2 of the precision form against the plain FP64 run after the
         # same number of steps from the same initial state (interior cells)
@@ -479,7 +483,8 @@ def run_ours(args):
         line["forms"] = {"mixed_same_case": {"value": mval, "unit": UNIT, "max_div": mdiv,
                                              "speedup_vs_plain_fp64": mval / value,
                                              "rel_l2_vs_fp64": err, "after_steps": args.warmup + args.steps,
-                                             "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation"}}
+                                             "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation",
+                                             "sweep": msweep}}
         if not args.no_batch:
             line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
             line["forms"]["serving"] = bench_serving(policy="srpt")
@@ -499,6 +504,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="spheres3d_256")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--sweep-form", default="auto", choices=["auto", "split", "fused"],
+                    help="precision form: the FP32 sweep's form (auto: timed on the case at creation)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", type=int, default=1, help="also measure the precision and batched forms")
     ap.add_argument("--no-batch", action="store_true")

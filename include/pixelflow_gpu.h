@@ -76,16 +76,19 @@ typedef struct pf_options {
   int32_t track_sor_error; /* 1: compute the reference's SOR max-change */
   double dc_tol;           /* mixed: stop passes once max|r| <= dc_tol */
   int32_t use_graph;       /* 1: replay each step from a CUDA graph */
-  int32_t sweep_form;      /* mixed: PF_SWEEP_AUTO fuses both colours of an
-                              FP32 sweep into one launch where the case allows
-                              it (3D, even n and l); PF_SWEEP_SPLIT launches
-                              one kernel per colour.  Same results bit for bit */
-  int32_t fused_rows;      /* mixed, fused sweep: y rows per CTA (0: auto) */
-  int32_t fused_planes;    /* mixed, fused sweep: z planes per CTA (0: auto) */
+  int32_t sweep_form;      /* mixed, FP32 sweeps: PF_SWEEP_SPLIT one launch
+                              per colour; PF_SWEEP_FUSED both colours in one
+                              launch where the case allows it (3D, even n and
+                              l; split otherwise); PF_SWEEP_AUTO times both
+                              on the case at creation and keeps the faster.
+                              Same results bit for bit */
+  int32_t fused_rows;      /* mixed, fused sweep: y rows per tile (0: auto) */
+  int32_t fused_planes;    /* mixed, fused sweep: cap on the (tile, plane)
+                              pairs of one CTA (0: one wave of CTAs) */
   int32_t reserved[2];
 } pf_options;
 
-enum { PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1 };
+enum { PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1, PF_SWEEP_FUSED = 2 };
 
 typedef struct pf_case pf_case;
 
@@ -270,6 +273,12 @@ int pf_batch_last_ms(pf_batch *b, double *ms);
 #define PF_NOALLOC_MAX_ROWS 262144
 int pf_max_div_noalloc(const pf_params *prm, const double *u, const double *v, const double *w,
                        const double *porosity, int ld1, int ld2, double *max_div, void *stream);
+
+/* The precision form's FP32 sweep: *fused = 1 when the case runs both
+ * colours in one launch; split_ms / fused_ms (either may be NULL) = the
+ * time per sweep of each form measured at creation under PF_SWEEP_AUTO
+ * (0 when not measured). */
+int pf_sweep_info(pf_case *c, int *fused, float *split_ms, float *fused_ms);
 
 /* Testing of the failure path of the fused correction sweep (no reference
  * counterpart): from the next step on, the sweep's producer skips staging

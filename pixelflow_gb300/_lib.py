@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "libpixelflow_gb300.so")
 PF_OK = 0
 PF_PREC_FP64 = 0
 PF_PREC_MIXED = 1
-PF_SWEEP_AUTO, PF_SWEEP_SPLIT = 0, 1
+PF_SWEEP_AUTO, PF_SWEEP_SPLIT, PF_SWEEP_FUSED = 0, 1, 2
 ERRORS = {
     -1: "PF_E_INVALID", -2: "PF_E_CUDA", -3: "PF_E_NOMEM", -4: "PF_E_NONFINITE",
     -5: "PF_E_TIMEOUT", -6: "PF_E_STATE", -7: "PF_E_BUSY",
@@ -105,6 +105,7 @@ _PROTOS = {
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     "pf_debug_fused_drop_stage": (_I, [_VP, _I]),
+    "pf_sweep_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
     "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfBatchOptions), ctypes.POINTER(_VP)]),

@@ -67,10 +67,12 @@ class Settings:
     inner_sweeps: int = 25           # mixed: FP32 SOR iterations per pass
     dc_tol: float = 0.0              # mixed: stop the passes once max|r| <= dc_tol (0: run all)
     track_sor_error: bool = True     # keep the reference's SOR max-change diagnostic
-    # mixed: "auto" runs both colours of an FP32 sweep in one launch where the
-    # case allows it (3D, even n and l), "split" one launch per colour; the
-    # results are the same bit for bit.  fused_rows / fused_planes: the fused
-    # sweep's rows and planes per CTA (0: chosen from the grid and the device)
+    # mixed: "split" runs one launch per colour of an FP32 sweep, "fused" both
+    # colours in one launch where the case allows it (3D, even n and l),
+    # "auto" times both on the case when it is created and keeps the faster;
+    # the results are the same bit for bit.  fused_rows / fused_planes: the
+    # fused sweep's rows per tile and cap on (tile, plane) pairs per CTA (0:
+    # chosen from the grid and the device)
     sweep_form: str = "auto"
     fused_rows: int = 0
     fused_planes: int = 0

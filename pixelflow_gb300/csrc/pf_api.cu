@@ -416,7 +416,8 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "outer_max and inner_sweeps must be >= 0");
   if (rc == PF_OK && c->g.wall && c->opt.precision != PF_PREC_FP64)
     rc = fail(PF_E_INVALID, "wall_mode: the air-condition program runs in the plain FP64 form only");
-  if (rc == PF_OK && c->opt.sweep_form != PF_SWEEP_AUTO && c->opt.sweep_form != PF_SWEEP_SPLIT)
+  if (rc == PF_OK && c->opt.sweep_form != PF_SWEEP_AUTO && c->opt.sweep_form != PF_SWEEP_SPLIT &&
+      c->opt.sweep_form != PF_SWEEP_FUSED)
     rc = fail(PF_E_INVALID, "unknown sweep_form");
   if (rc == PF_OK && (c->opt.fused_rows < 0 || c->opt.fused_planes < 0))
     rc = fail(PF_E_INVALID, "fused_rows and fused_planes must be >= 0");
@@ -456,6 +457,7 @@ static int finish_setup(pf_case* c) {
   int rc = check_launch("case set-up kernels");
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st));
+  if (c->opt.precision == PF_PREC_MIXED) return mixed_choose_sweep(c);
   return PF_OK;
 }
 
@@ -880,9 +882,17 @@ int pf_kernel_launches(pf_case* c, int64_t* count) {
   return PF_OK;
 }
 
+int pf_sweep_info(pf_case* c, int* fused, float* split_ms, float* fused_ms) {
+  if (!c || !fused) return fail(PF_E_INVALID, "null argument");
+  *fused = c->use_fused ? 1 : 0;
+  if (split_ms) *split_ms = c->sweep_ms[0];
+  if (fused_ms) *fused_ms = c->sweep_ms[1];
+  return PF_OK;
+}
+
 int pf_debug_fused_drop_stage(pf_case* c, int stage) {
   if (!c) return fail(PF_E_INVALID, "null handle");
-  if (!c->e2[0]) return fail(PF_E_STATE, "the case does not run the fused correction sweep");
+  if (!c->use_fused) return fail(PF_E_STATE, "the case does not run the fused correction sweep");
   c->fused.drop_stage = stage < 0 ? -1 : stage;
   for (int b = 0; b < 2; b++)  // captured launches hold the old value
     if (c->gexec[b]) {

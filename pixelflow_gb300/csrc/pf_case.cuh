@@ -51,15 +51,17 @@ struct pf_case {
   float *gxf = nullptr, *gyf = nullptr, *gzf = nullptr, *rinvf = nullptr, *dampf = nullptr;
   float* e[2] = {nullptr, nullptr};     // packed FP32 correction
   // fused sweep (both colours per launch): the correction ping-pongs between
-  // e and e2 within a pass; null when the case uses one launch per colour
+  // e and e2 within a pass; e2 is allocated when the case may run it
   float* e2[2] = {nullptr, nullptr};
   pf::FusedShape fused;
+  bool use_fused = false;
+  float sweep_ms[2] = {0.f, 0.f};  // PF_SWEEP_AUTO: ms per sweep measured at creation (split, fused)
   float* rf[2] = {nullptr, nullptr};    // packed FP32 normalised residual (RHS of the sweeps)
   float* epsf[2] = {nullptr, nullptr};  // packed FP32 porosity (operator rebuilt on the fly)
   int* skip = nullptr;                  // device flag: defect correction converged
 
   int64_t sor_launches_per_step() const {
-    if (opt.precision == PF_PREC_MIXED) return (e2[0] ? 1LL : 2LL) * opt.outer_max * opt.inner_sweeps;
+    if (opt.precision == PF_PREC_MIXED) return (use_fused ? 1LL : 2LL) * opt.outer_max * opt.inner_sweeps;
     return 2LL * prm.iter_max;
   }
 };
@@ -68,6 +70,8 @@ namespace pf {
 // The precision form with the fused sweep (both colours per launch).
 bool mixed_fused(const Geo& g, const pf_options& opt);
 int mixed_alloc(pf_case* c);
+// After set-up: the sweep form (PF_SWEEP_AUTO times both forms on the case).
+int mixed_choose_sweep(pf_case* c);
 void mixed_free(pf_case* c);
 void mixed_setup(pf_case* c);
 void mixed_sync_from_fp64(pf_case* c);

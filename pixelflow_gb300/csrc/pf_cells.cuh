@@ -601,22 +601,19 @@ __host__ __device__ inline DCConst make_dc_const(double dt, double dx, double dy
   return K;
 }
 
-// One cell of the correction sweep from its loaded operands.  Every form of
-// the sweep (the vectorised single-case kernel, the persistent batch kernel's
-// global and shared-memory passes) calls this, so they agree bit for bit.
+// A face coefficient of the correction sweep's operator from the porosity of
+// the two cells sharing the face: the same float for both cells (the sum is
+// commutative), so a kernel may compute a face once for the two updates.
+__device__ __forceinline__ float dc_face(float h, const DCConst& K, float pa, float pb) {
+  return h * fmaxf(K.small2, pa + pb);
+}
+
+// One cell of the correction sweep from its face coefficients and the other
+// colour's neighbour corrections.
 template <int DIM>
-__device__ __forceinline__ float dc_cell(const DCConst& K, float pc, float pe, float pw, float pn, float ps,
-                                         float pt, float pb, float xe, float xw, float xn, float xs, float xt,
-                                         float xb, float rr, float eold, bool inlet, bool outlet) {
-  float ae = K.hx * fmaxf(K.small2, pe + pc);
-  float aw = K.hx * fmaxf(K.small2, pc + pw);
-  const float an = K.hy * fmaxf(K.small2, pn + pc);
-  const float as = K.hy * fmaxf(K.small2, pc + ps);
-  float at = 0.f, ab = 0.f;
-  if (DIM == 3) {
-    at = K.hz * fmaxf(K.small2, pt + pc);
-    ab = K.hz * fmaxf(K.small2, pc + pb);
-  }
+__device__ __forceinline__ float dc_cell_faces(const DCConst& K, float ae, float aw, float an, float as, float at,
+                                               float ab, float xe, float xw, float xn, float xs, float xt,
+                                               float xb, float rr, float eold, bool inlet, bool outlet) {
   const float ap = -ae - aw - an - as - at - ab;
   float enew = fmaf(K.omw, eold, rr);
   if (!outlet) {
@@ -635,6 +632,20 @@ __device__ __forceinline__ float dc_cell(const DCConst& K, float pc, float pe, f
     enew = fmaf(-__fdividef(K.omega, ap), t, enew);
   }
   return enew;
+}
+
+// One cell of the correction sweep from its loaded operands.  Every form of
+// the sweep (the vectorised single-case kernel, the fused kernel, the
+// persistent batch kernel's global and shared-memory passes) reaches
+// dc_cell_faces with faces from dc_face, so they agree bit for bit.
+template <int DIM>
+__device__ __forceinline__ float dc_cell(const DCConst& K, float pc, float pe, float pw, float pn, float ps,
+                                         float pt, float pb, float xe, float xw, float xn, float xs, float xt,
+                                         float xb, float rr, float eold, bool inlet, bool outlet) {
+  const float at = DIM == 3 ? dc_face(K.hz, K, pt, pc) : 0.f;
+  const float ab = DIM == 3 ? dc_face(K.hz, K, pc, pb) : 0.f;
+  return dc_cell_faces<DIM>(K, dc_face(K.hx, K, pe, pc), dc_face(K.hx, K, pc, pw), dc_face(K.hy, K, pn, pc),
+                            dc_face(K.hy, K, pc, ps), at, ab, xe, xw, xn, xs, xt, xb, rr, eold, inlet, outlet);
 }
 
 template <int DIM>

@@ -590,6 +590,39 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
   if (TRACK) block_max_atomic(e, err);
 }
 
+// The fused kernel's chunk: dc_chunk (3D, colour side S) with the top faces
+// either computed or given (ATIN: colour 1 takes them from the colour-0
+// update of the plane above, whose bottom faces they are).  The bottom faces
+// are returned in AB.
+template <bool TRACK, bool ATIN>
+__device__ __forceinline__ VecF<4> dc_chunk_f(const Geo& g, const DCConst& K, int h0, int S, const VecF<4>& EC,
+                                              const VecF<4>& R, const VecF<4>& PC, const VecF<4>& XO,
+                                              const VecF<4>& PO, float xx, float px, const VecF<4>& XN,
+                                              const VecF<4>& XS, const VecF<4>& PN, const VecF<4>& PS,
+                                              const VecF<4>& XT, const VecF<4>& XB, const VecF<4>& PT,
+                                              const VecF<4>& PB, const VecF<4>& ATin, VecF<4>& AB, unsigned& e) {
+  VecF<4> out;
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const int i = 2 * (h0 + u) + S;
+    const float eold = EC.a[u];
+    const float xe = S ? (u < 3 ? XO.a[u + 1] : xx) : XO.a[u];
+    const float xw = S ? XO.a[u] : (u > 0 ? XO.a[u - 1] : xx);
+    const float pe = S ? (u < 3 ? PO.a[u + 1] : px) : PO.a[u];
+    const float pw = S ? PO.a[u] : (u > 0 ? PO.a[u - 1] : px);
+    const float pc = PC.a[u];
+    const float at = ATIN ? ATin.a[u] : dc_face(K.hz, K, PT.a[u], pc);
+    AB.a[u] = dc_face(K.hz, K, pc, PB.a[u]);
+    const float v = dc_cell_faces<3>(K, dc_face(K.hx, K, pe, pc), dc_face(K.hx, K, pc, pw),
+                                     dc_face(K.hy, K, PN.a[u], pc), dc_face(K.hy, K, pc, PS.a[u]), at, AB.a[u], xe,
+                                     xw, XN.a[u], XS.a[u], XT.a[u], XB.a[u], R.a[u], eold, i == 1, i == g.m);
+    const bool in = i >= 1 && i <= g.m;
+    out.a[u] = in ? v : eold;
+    if (TRACK && in) e = max(e, abs_bits(v - eold));
+  }
+  return out;
+}
+
 // Fused full correction sweep, 3D with even n and l (the periodic y/z edges
 // then read the opposite interior rows, which have the other colour): both
 // colours of one sweep in one launch, each operand row streamed from HBM
@@ -806,6 +839,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
     // planes k-1, k, k+1 (+ the side slot of planes k, k+1), colour-0
     // porosity and results at planes k-2, k-1, k
     VecF<V> qE0{}, qE1{}, qE2{}, qP0{}, qP1{}, qP2{}, c0{}, c1{}, c2{}, o0{}, o1{}, o2{};
+    VecF<V> ab{};  // bottom faces of the colour-0 update of plane k (the top faces of colour 1, plane k-1)
     float sE1 = 0.f, sE2 = 0.f, sP1 = 0.f, sP2 = 0.f;
     for (int it = 0; it < nit; it++) {
       const int k = k0 - 1 + it, kw = wrapz(k);
@@ -855,8 +889,8 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
         unsigned unused = 0;
         o0 = o1;
         o1 = o2;
-        o2 = dc_chunk<3, false, V>(g, K, h0, s, EC, R, c2, qE1, qP1, sE1, sP1, XN, XS, PN, PS, qE2, qE0, qP2, qP0,
-                                   unused);
+        o2 = dc_chunk_f<false, false>(g, K, h0, s, EC, R, c2, qE1, qP1, sE1, sP1, XN, XS, PN, PS, qE2, qE0, qP2,
+                                      qP0, ab, ab, unused);
         *reinterpret_cast<VecF<V>*>(sm + L.red + (it % FZR) * planeRed + rl * P + V + h0) = o2;
         if (black_item && k >= k0 && k < k1)
           *reinterpret_cast<VecF<V>*>(A.eb[0] + pk_idx(g, h0, jw, kw)) = o2;
@@ -881,8 +915,11 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
         const float xx = s ? Rb[V] : Rb[-1];
         const VecF<V> PN = ldv<V>(P0b + H), PS = ldv<V>(P0b - H);
         const VecF<V> XN = ldv<V>(Rb + P), XS = ldv<V>(Rb - P);
-        *reinterpret_cast<VecF<V>*>(A.eb[1] + pk_idx(g, h0, jw, kb)) =
-            dc_chunk<3, TRACK, V>(g, K, h0, s, qE0, R, qP0, o1, c1, xx, px, XN, XS, PN, PS, o2, o0, c2, c0, e);
+        // top faces: the bottom faces of this chunk's colour-0 update of plane k
+        VecF<V> abb;
+        const VecF<V> out = dc_chunk_f<TRACK, true>(g, K, h0, s, qE0, R, qP0, o1, c1, xx, px, XN, XS, PN, PS, o2,
+                                                    o0, c2, c0, ab, abb, e);
+        *reinterpret_cast<VecF<V>*>(A.eb[1] + pk_idx(g, h0, jw, kb)) = out;
       }
     }
     __syncthreads();  // the next segment's first stages overwrite the rings

@@ -16,13 +16,66 @@
 // max|r|/omega <= dc_tol (a device flag, so the step stays one graph).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pf_case.cuh"
 #include "pf_internal.cuh"
 
 namespace pf {
 
 bool mixed_fused(const Geo& g, const pf_options& opt) {
-  return opt.precision == PF_PREC_MIXED && opt.sweep_form == PF_SWEEP_AUTO && fused_eligible(g);
+  return opt.precision == PF_PREC_MIXED && opt.sweep_form != PF_SWEEP_SPLIT && fused_eligible(g);
+}
+
+// The sweep form of the case.  PF_SWEEP_AUTO runs a few sweeps of each form
+// on the case's own arrays while the residual and the correction are still
+// zero (so they stay zero: the state is untouched) and keeps the faster; the
+// forms' speeds depend on the grid's shape in ways no simple rule captures
+// (measured: the fused sweep is 5 % faster at 384^3, 6 % at 320^3, 1 % slower
+// at 256^3, 11 % slower at 512 x 256 x 256, 39 % slower at 128^3).
+int mixed_choose_sweep(pf_case* c) {
+  c->use_fused = c->e2[0] != nullptr;
+  if (!c->use_fused || c->opt.sweep_form != PF_SWEEP_AUTO) return PF_OK;
+  const Geo& g = c->g;
+  const Scal& s = c->s;
+  cudaStream_t st = c->st;
+  cudaEvent_t ev[3];
+  for (auto& e : ev) PF_CUDA(cudaEventCreate(&e));
+  constexpr int SWEEPS = 4, REPEATS = 3;
+  // the launches of a step: with error tracking, colour 1 of each split sweep
+  // and every fused sweep track (a change of 0 here; the slots are zeroed at
+  // the start of each step)
+  unsigned long long* err = c->opt.track_sor_error ? &c->red[RED_ERRF] : nullptr;
+  float best[2] = {1e30f, 1e30f};
+  for (int rep = 0; rep < REPEATS; rep++) {
+    cudaEventRecord(ev[0], st);
+    for (int it = 0; it < SWEEPS; it++)
+      for (int col = 0; col < 2; col++)
+        launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
+                      col == 1 ? err : nullptr, nullptr, st);
+    cudaEventRecord(ev[1], st);
+    for (int it = 0; it < SWEEPS; it++) {
+      const float* ea[2] = {it & 1 ? c->e2[0] : c->e[0], it & 1 ? c->e2[1] : c->e[1]};
+      float* eb[2] = {it & 1 ? c->e[0] : c->e2[0], it & 1 ? c->e[1] : c->e2[1]};
+      launch_sor_fused(g, s, c->fused, c->epsf, c->rf, ea, eb, err, &c->red[RED_FLAGS], nullptr, st);
+    }
+    cudaEventRecord(ev[2], st);
+    cudaError_t e = cudaEventSynchronize(ev[2]);
+    float ms[2] = {0.f, 0.f};
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+    if (e != cudaSuccess) {
+      for (auto& x : ev) cudaEventDestroy(x);
+      return cuda_fail(e, "sweep form timing");
+    }
+    for (int f = 0; f < 2; f++) best[f] = std::min(best[f], ms[f] / SWEEPS);
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  c->launches += (int64_t)REPEATS * SWEEPS * 3;
+  c->sweep_ms[0] = best[0];
+  c->sweep_ms[1] = best[1];
+  c->use_fused = best[1] < best[0];
+  return PF_OK;
 }
 
 int mixed_alloc(pf_case* c) {
@@ -118,7 +171,7 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);
-  const bool fused = c->e2[0] != nullptr;
+  const bool fused = c->use_fused;
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
     launch_zero_u64(&c->red[RED_RMAX], RED_SLOTS, st);
     for (int col = 0; col < 2; col++)

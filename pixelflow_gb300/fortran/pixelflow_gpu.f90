@@ -9,7 +9,7 @@ module pixelflow_gpu
 
   integer(c_int), parameter :: PF_OK = 0
   integer(c_int), parameter :: PF_PREC_FP64 = 0, PF_PREC_MIXED = 1
-  integer(c_int), parameter :: PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1
+  integer(c_int), parameter :: PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1, PF_SWEEP_FUSED = 2
 
   type, bind(C) :: pf_params
     integer(c_int32_t) :: dim, m, n, l
@@ -112,6 +112,13 @@ module pixelflow_gpu
       type(c_ptr), value :: h
       real(c_double), intent(out) :: u(*), v(*), w(*), p(*)
       integer(c_int), value :: ld1, ld2
+    end function
+
+    integer(c_int) function pf_sweep_info(h, fused, split_ms, fused_ms) bind(C, name="pf_sweep_info")
+      import :: c_int, c_float, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), intent(out) :: fused
+      real(c_float), intent(out) :: split_ms, fused_ms
     end function
 
     type(c_ptr) function pf_last_error() bind(C, name="pf_last_error")

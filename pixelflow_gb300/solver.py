@@ -23,7 +23,7 @@ from .config import Settings, read_porosity_csv, read_settings
 from ._lib import PfOptions, PfParams, check
 
 PRECISIONS = {"fp64": _lib.PF_PREC_FP64, "plain": _lib.PF_PREC_FP64, "mixed": _lib.PF_PREC_MIXED}
-SWEEP_FORMS = {"auto": _lib.PF_SWEEP_AUTO, "split": _lib.PF_SWEEP_SPLIT}
+SWEEP_FORMS = {"auto": _lib.PF_SWEEP_AUTO, "split": _lib.PF_SWEEP_SPLIT, "fused": _lib.PF_SWEEP_FUSED}
 
 
 def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
@@ -267,6 +267,14 @@ class Case:
         buf = np.zeros(max_steps)
         check(self.L.pf_profile_step_times(self.h, _ptr(buf), max_steps, ctypes.byref(n)))
         return buf[: n.value].copy()
+
+    def sweep_info(self) -> Dict[str, object]:
+        """The precision form's FP32 sweep: {"form": "fused" | "split",
+        "split_ms", "fused_ms"} (per sweep, measured at creation when the form
+        was chosen automatically, else 0)."""
+        f, a, b = ctypes.c_int(), ctypes.c_float(), ctypes.c_float()
+        check(self.L.pf_sweep_info(self.h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)))
+        return {"form": "fused" if f.value else "split", "split_ms": a.value, "fused_ms": b.value}
 
     def memory_bytes(self) -> int:
         b = ctypes.c_size_t()

@@ -41,7 +41,7 @@ def test_fused_sweep_matches_split_bit_for_bit(shape):
     s = G.settings_spheres_3d(precision="mixed", outer_max=2, inner_sweeps=5)
     vals = G.spheres_3d(*shape, count=6, seed=3)
     split, nsplit, lsplit, msplit = _run(s.replace(sweep_form="split"), shape, vals, 4)
-    fused, nfused, lfused, mfused = _run(s, shape, vals, 4)
+    fused, nfused, lfused, mfused = _run(s.replace(sweep_form="fused"), shape, vals, 4)
     assert _same(fused, split)
     assert nfused == nsplit  # max|div u| and the tracked SOR error
     # one launch per sweep instead of one per colour; two more packed FP32 arrays
@@ -55,7 +55,7 @@ def test_fused_tile_shapes_agree(rows, planes):
     s = G.settings_spheres_3d(precision="mixed", outer_max=2, inner_sweeps=4)
     vals = G.spheres_3d(*shape, count=5, seed=4)
     ref, nref, _, _ = _run(s.replace(sweep_form="split"), shape, vals, 3)
-    got, ngot, _, _ = _run(s.replace(fused_rows=rows, fused_planes=planes), shape, vals, 3)
+    got, ngot, _, _ = _run(s.replace(sweep_form="fused", fused_rows=rows, fused_planes=planes), shape, vals, 3)
     assert _same(got, ref)
     assert ngot == nref
 
@@ -67,7 +67,8 @@ def test_fused_eager_early_stop_and_untracked():
     shape = (30, 24, 26)
     vals = G.spheres_3d(*shape, count=4, seed=5)
     for kw in (dict(dc_tol=1e-3), dict(track_sor_error=False), dict(inner_sweeps=6)):
-        s = G.settings_spheres_3d(precision="mixed", outer_max=3, inner_sweeps=kw.pop("inner_sweeps", 5), **kw)
+        s = G.settings_spheres_3d(precision="mixed", sweep_form="fused", outer_max=3,
+                                  inner_sweeps=kw.pop("inner_sweeps", 5), **kw)
         ref = _run(s.replace(sweep_form="split"), shape, vals, 3, use_graph=False)[0]
         assert _same(_run(s, shape, vals, 3, use_graph=False)[0], ref), kw
         assert _same(_run(s, shape, vals, 3, use_graph=True)[0], ref), kw
@@ -77,7 +78,7 @@ def test_fused_not_used_for_odd_periodic_sizes():
     """Odd n or l needs the ghost-row refresh between colours: the case keeps
     the two-launch sweep (same memory and launches as asking for it)."""
     shape = (24, 21, 16)
-    s = G.settings_spheres_3d(precision="mixed", outer_max=1, inner_sweeps=3)
+    s = G.settings_spheres_3d(precision="mixed", sweep_form="fused", outer_max=1, inner_sweeps=3)
     vals = G.spheres_3d(*shape, count=3, seed=6)
     a = _run(s, shape, vals, 2)
     b = _run(s.replace(sweep_form="split"), shape, vals, 2)
@@ -92,7 +93,7 @@ def test_fused_case_bytes_match_allocation():
     s = G.settings_spheres_3d(precision="mixed")
     vals = G.spheres_3d(*shape, count=3, seed=7)
     L = _lib.load()
-    for form in ("auto", "split"):
+    for form in ("auto", "fused", "split"):
         ss = s.replace(sweep_form=form)
         need = ctypes.c_size_t()
         prm, opt = make_params(ss, shape), make_options(ss)
@@ -118,7 +119,7 @@ def test_fused_staging_timeout_reported_context_usable():
     from pixelflow_gb300 import _lib
     from pixelflow_gb300._lib import PfError
     shape = (32, 16, 16)
-    s = G.settings_spheres_3d(precision="mixed", outer_max=1, inner_sweeps=2)
+    s = G.settings_spheres_3d(precision="mixed", sweep_form="fused", outer_max=1, inner_sweeps=2)
     vals = G.spheres_3d(*shape, count=3, seed=8)
     L = _lib.load()
     with Case(s, shape, vals) as c:
@@ -139,3 +140,24 @@ def test_fused_staging_timeout_reported_context_usable():
     a = _run(s, shape, vals, 2)[0]
     b = _run(s.replace(sweep_form="split"), shape, vals, 2)[0]
     assert _same(a, b)
+
+
+@pytest.mark.parametrize("shape", [(40, 32, 24), (24, 21, 16)])
+def test_auto_sweep_form_choice(shape):
+    """PF_SWEEP_AUTO times both forms at creation on zero residual and
+    correction (the state is untouched: same bits as the split run from the
+    start) and keeps the faster; odd sizes measure nothing and keep split."""
+    s = G.settings_spheres_3d(precision="mixed", outer_max=2, inner_sweeps=3)
+    vals = G.spheres_3d(*shape, count=3, seed=9)
+    with Case(s, shape, vals) as c:
+        info = c.sweep_info()
+        c.initial_conditions()
+        c.step(2)
+        got = c.get_state()
+    if shape[1] % 2 == 0:
+        assert info["split_ms"] > 0 and info["fused_ms"] > 0
+        assert info["form"] == ("fused" if info["fused_ms"] < info["split_ms"] else "split")
+    else:
+        assert info == {"form": "split", "split_ms": 0.0, "fused_ms": 0.0}
+    ref = _run(s.replace(sweep_form="split"), shape, vals, 2)[0]
+    assert _same(got, ref)
