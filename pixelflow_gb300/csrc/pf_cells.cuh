@@ -25,9 +25,11 @@ __device__ __forceinline__ unsigned abs_bits(float x) { return __float_as_uint(x
 // normal with the same sign and exponent, a - b = (ma - mb) * 2^(E-1075) is
 // exact in 52 bits, so the result is assembled with integer operations;
 // otherwise (sign or exponent differ, zeros, subnormals, Inf, NaN, or a
-// subnormal result) the FP64 subtraction.  Same bits either way.  On GB300
-// the FP64 subtraction made a tracked SOR update 29 % slower (83.6 against
-// 64.9 us for 4.8 M updates); the integer form costs nothing measurable.
+// subnormal result) the FP64 subtraction.  Same bits either way.  Measured
+// on the 256^3 plain step (Mcell-steps/s): tracking by FP64 subtraction 590,
+// this form 641, no tracked value at all 663; a complete integer emulation
+// of the subtraction (every operand class, no FP64 instruction) 584 -- its
+// data-dependent branches split the warps.
 __device__ __forceinline__ unsigned long long abs_diff_bits(double a, double b) {
   const unsigned long long A = (unsigned long long)__double_as_longlong(a);
   const unsigned long long B = (unsigned long long)__double_as_longlong(b);
