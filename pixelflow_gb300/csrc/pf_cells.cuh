@@ -118,6 +118,16 @@ __device__ __forceinline__ void warp_max_atomic(unsigned long long v, unsigned l
   }
 }
 
+// Warp max of FP32 magnitudes (32-bit patterns) into the low 32 bits of the
+// spread slots, without a block barrier.
+__device__ __forceinline__ void warp_max_atomic(unsigned v, unsigned long long* out) {
+  const unsigned r = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && r) {
+    const unsigned wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    atomicMax(reinterpret_cast<unsigned*>(out + (wid & (RED_SLOTS - 1))), r);
+  }
+}
+
 // FP32 magnitudes: 32-bit patterns, max into the low 32 bits of *slot.
 __device__ __forceinline__ void block_max_atomic(unsigned v, unsigned long long* slot) {
   __shared__ unsigned red[32];

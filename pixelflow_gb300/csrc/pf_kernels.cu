@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_residual(Geo g, Coef<double> 
     packed_item<DIM>(g, t, h, j, k);
     r = c_residual<DIM>(g, C, pc, po, omega, colour, rf, ec, h, j, k);
   }
-  block_max_atomic(r, rmax);
+  warp_max_atomic(r, rmax);
 }
 
 // FP32 correction sweep, four consecutive cells of one packed row per
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
     *reinterpret_cast<VecF<V>*>(ec + q) =
         dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, PC, XO, PO, xx, px, XN, XS, PN, PS, XT, XB, PT, PB, e);
   }
-  if (TRACK) block_max_atomic(e, err);
+  if (TRACK) warp_max_atomic(e, err);
 }
 
 // The fused kernel's chunk: dc_chunk (3D, colour side S) with the top faces
