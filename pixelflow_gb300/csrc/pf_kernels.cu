@@ -1126,9 +1126,9 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
                    const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st) {
   const DCConst K = dc_const(g, sc);
   // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
-  // 4 beat 2 per thread at 256^3 (1511 vs 1336 Mcell-steps/s for the step):
-  // the extra occupancy of narrower chunks does not pay for their extra
-  // instructions
+  // 4 beat 2 and 8 per thread at 256^3 (1547 vs 1336 and 1508 Mcell-steps/s
+  // for the step): the extra occupancy of narrower chunks does not pay for
+  // their extra instructions, and 8 slots take 126 registers (two CTAs per SM)
   constexpr int V = 4;
   const int chunks = (g.m >> 1) / V + 1;
   const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
