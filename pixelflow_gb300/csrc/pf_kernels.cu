@@ -655,11 +655,16 @@ __device__ __forceinline__ VecF<4> dc_chunk_f(const Geo& g, const DCConst& K, in
 // step's barrier.
 constexpr int FUSED_MAX_THREADS = 512;
 constexpr int FUSED_V = 4;
-constexpr int FZE = 4;       // ring depth of E1, P1: planes k, k+1 read, two ahead
-constexpr int FZP = 4;       // ring depth of P0: planes k-1, k read, two ahead
-constexpr int FZ1 = 3;       // ring depth of E0, R0, R1: one plane read, two ahead
-constexpr int FZR = 3;       // colour-0 result ring: plane k-1 read while plane k is written
-constexpr int FSTAGES = 3;   // mbarriers: the stage being read and two in flight
+// stages in flight ahead of the one being read: 2 (whole precision-form step
+// at 256^3 with the fused sweep: 1196, 1507, 1399 Mcell-steps/s for 1, 2, 3;
+// one leaves the staging latency exposed, three makes the rings too deep for
+// tall tiles)
+constexpr int FPRE = 2;
+constexpr int FZE = 2 + FPRE;    // ring depth of E1, P1: planes k, k+1 read, FPRE ahead
+constexpr int FZP = 2 + FPRE;    // ring depth of P0: planes k-1, k read, FPRE ahead
+constexpr int FZ1 = 1 + FPRE;    // ring depth of E0, R0, R1: one plane read, FPRE ahead
+constexpr int FZR = 3;           // colour-0 result ring: plane k-1 read while plane k is written
+constexpr int FSTAGES = 1 + FPRE;  // mbarriers: the stage being read and FPRE in flight
 constexpr unsigned long long FUSED_WAIT_NS = 200000000ULL;  // 0.2 s; a stage lands in microseconds
 constexpr int FUSED_WAIT_POLLS = 1 << 20;                    // backstop on the number of polls
 constexpr size_t FUSED_SMEM_MAX = 232448;  // dynamic shared memory per CTA on sm_100-class parts
@@ -828,10 +833,8 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
                   nullptr);
       issued++;
     };
-    if (threadIdx.x == producer) {
-      issue(0);
-      if (nit > 1) issue(1);
-    }
+    if (threadIdx.x == producer)
+      for (int i = 0; i < FPRE && i < nit; i++) issue(i);
     const bool red_item = rl < ny + 2;            // a colour-0 chunk of this tile
     const bool black_item = rl >= 1 && rl <= ny;  // ... whose row is the tile's own
     const int jw = wrapy(j0 - 1 + rl);
@@ -900,10 +903,10 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
         ok = false;
         break;
       }
-      if (threadIdx.x == producer && it + 2 < nit) {
+      if (threadIdx.x == producer && it + FPRE < nit) {
         // the slots this stage overwrites were last read before the barrier
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(it + 2);
+        issue(it + FPRE);
       }
       if (it >= 2 && black_item) {  // colour 1 of plane kb = k-1, row jw
         const int kb = k - 1;
