@@ -645,10 +645,11 @@ __device__ __forceinline__ VecF<4> dc_chunk_f(const Geo& g, const DCConst& K, in
 // computation sees old values.
 //
 // Staging: one thread issues, per step, the cp.async.bulk copies (one per
-// run of rows contiguous in memory) of what the step after next needs:
-// colour-1 correction and porosity of plane k+1 with two rows of halo,
+// run of rows contiguous in memory) of what the step FPRE steps ahead needs
+// (for step it: colour-1 correction and porosity of plane k+1 with two rows
+// of halo,
 // colour-0 porosity, correction and residual of plane k, colour-1 residual of
-// plane k-1, into shared-memory rings, and arms an mbarrier with their byte
+// plane k-1) into shared-memory rings, and arms an mbarrier with their byte
 // count; the consumers wait on it (bounded: after FUSED_WAIT_NS the CTA
 // drains its copies in flight, raises PF_FLAG_FUSED_TIMEOUT and leaves).  A
 // stage overwrites only ring slots whose last reader finished before the
