@@ -25,13 +25,18 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
-def case_bytes(settings: Settings, shape: Sequence[int]) -> int:
-    """Device bytes one case of this shape needs in a batch."""
+def case_bytes(settings: Settings, shape: Sequence[int], large_cells: int = 300000) -> int:
+    """Device bytes one case of this shape takes in a batch: the allocation
+    pf_batch_add makes (precision form; a case the persistent kernel steps,
+    at most `large_cells` cells, uses the split FP32 sweep)."""
     L = _lib.load()
     b = ctypes.c_size_t()
+    cells = int(np.prod(shape))
     s = settings.replace(precision="mixed")
-    check(L.pf_case_bytes(ctypes.byref(make_params(s, shape)), ctypes.byref(make_options(s, use_graph=False)),
-                          ctypes.byref(b)))
+    if cells <= large_cells:
+        s = s.replace(sweep_form="split")
+    check(L.pf_case_bytes(ctypes.byref(make_params(s, shape)),
+                          ctypes.byref(make_options(s, use_graph=cells > large_cells)), ctypes.byref(b)))
     return b.value
 
 

@@ -524,6 +524,9 @@ static int batch_add_impl(pf_batch* b, const pf_params* prm, const pf_options* o
   // their own stream, concurrently with the persistent kernel
   const long long cells = (long long)prm->m * prm->n * (prm->dim == 3 ? prm->l : 1);
   o.use_graph = cells > b->opt.large_cells ? 1 : 0;
+  // a case the persistent kernel steps never runs the single-case FP32 sweep:
+  // no second correction array, no sweep-form timing at creation
+  if (!o.use_graph) o.sweep_form = PF_SWEEP_SPLIT;
   size_t need = 0;
   int rc = pf_case_bytes(prm, &o, &need);
   if (rc) return rc;

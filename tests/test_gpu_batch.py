@@ -121,7 +121,11 @@ def test_batch_launch_is_persistent_one_per_dimension():
 
 
 def test_admission_bytes_equal_the_allocation():
-    """The admission estimate (pf_case_bytes) is the case's real allocation."""
+    """The admission estimate (pf_case_bytes through case_bytes) is the
+    allocation a batch makes for the case, for small cases (stepped by the
+    persistent kernel, split sweep) and large ones (own step graphs)."""
     for (s, shape, vals) in _cases():
-        with Case(s.replace(precision="mixed"), shape, vals) as c:
-            assert c.memory_bytes() == case_bytes(s, shape), shape
+        for large in (300000, 100):
+            with Batch(max_cases=2, large_cells=large) as b:
+                b.add(s, shape, vals)
+                assert b.memory()[0] == case_bytes(s, shape, large_cells=large), (shape, large)
