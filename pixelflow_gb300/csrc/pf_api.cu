@@ -285,7 +285,10 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
       if (halo) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
       // 2D tracks both half-sweeps (ibm_2d:351,385); 3D only the second (ibm_3d:575-583)
       unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERR] : nullptr;
-      launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, st);
+      // the operator loads may precede the dependency wait unless the previous
+      // kernel is the RHS, which writes bbn
+      const bool early = it > 0 || col > 0 || halo;
+      launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, early, st);
     }
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);

@@ -380,43 +380,6 @@ __device__ __forceinline__ void c_initial(Geo g, Scal s, T* u, T* v, T* w, doubl
   pref(g, p0, p1, i, j, k) = s.outlet_pressure;
 }
 
-// One red-black half-sweep update of cell (2h+s, j, k) of colour `colour`,
-// in place:  p = (1-omega) p + bbn - sum_nb a_nb p_nb  (all neighbours have
-// the other colour), which is the reference's
-//   p = (bb - sum a_nb p_old_nb)/ap*omega + p_old*(1-omega)
-// because no neighbour of a cell changes during its own colour's sweep.
-// Returns |p_new - p_old| as bits when TRACK (0 for cells outside the grid).
-template <typename T, int DIM, bool TRACK>
-__device__ __forceinline__ decltype(abs_bits(T(0))) c_sor_half(const Geo& g, const Coef<T>& C, T* __restrict__ pc,
-                                                              const T* __restrict__ po, T omw, int colour, int h,
-                                                              int j, int k) {
-  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  const int i = 2 * h + s;
-  decltype(abs_bits(T(0))) e = 0;
-  if (j <= g.n && i >= 1 && i <= g.m) {
-    const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
-    const idx_t q = pk_idx(g, h, j, k);
-    const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
-    const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-    const T pold = pc[q];
-    T t = C.bbn[q];
-    t = fma(-C.a[0][q], po[q + s], t);
-    t = fma(-C.a[1][q], po[q - 1 + s], t);
-    t = fma(-C.a[2][q], po[qn], t);
-    t = fma(-C.a[3][q], po[qs], t);
-    if (DIM == 3) {
-      const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
-      const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
-      t = fma(-C.a[4][q], po[qt], t);
-      t = fma(-C.a[5][q], po[qb], t);
-    }
-    const T pnew = fma(omw, pold, t);
-    pc[q] = pnew;
-    if (TRACK) e = abs_diff_bits(pnew, pold);
-  }
-  return e;
-}
-
 // FP64 residual of one cell, r = bbn - w p - sum a p_nb (normalised by w/ap).
 // Returns false for positions outside the grid.
 template <int DIM>

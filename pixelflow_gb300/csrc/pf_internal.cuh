@@ -134,7 +134,7 @@ void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV*
                 cudaStream_t st);
 template <typename T>
 void launch_sor_half(const Geo& g, const Coef<T>& cc, T* pc, const T* po, T one_minus_omega, int colour,
-                     unsigned long long* err, const int* skip, cudaStream_t st);
+                     unsigned long long* err, const int* skip, bool early, cudaStream_t st);
 template <typename T>
 void launch_p_halo(const Geo& g, T* p0, T* p1, const int* skip, cudaStream_t st);
 template <typename TV>

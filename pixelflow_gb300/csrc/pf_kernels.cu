@@ -225,19 +225,69 @@ __global__ void k_rhs(Geo g, Scal s, const T* __restrict__ u, const T* __restric
 // With TRACK the block max of |p_new - p_old| goes to *err.
 constexpr int SWEEP_THREADS = 256;
 
-template <typename T, int DIM, bool TRACK>
+// One red-black half-sweep of colour `colour`, in place: for each cell
+// (2h+s, j, k) of that colour,  p = (1-omega) p + bbn - sum_nb a_nb p_nb
+// (all neighbours have the other colour), which is the reference's
+//   p = (bb - sum a_nb p_old_nb)/ap*omega + p_old*(1-omega)
+// because no neighbour of a cell changes during its own colour's sweep.
+// With TRACK the max of |p_new - p_old| goes to err.
+//
+// EARLY: the cell's operator (bbn and the face coefficients) is loaded
+// before griddepcontrol.wait.  Under programmatic dependent launch the
+// grid's CTAs are resident before the previous half-sweep has finished; the
+// operator was written by kernels that finished before that one could
+// launch, so only the loads of p stay behind the wait, which shortens each
+// half-sweep of the launch-bound small grids.  Not for the first half-sweep
+// of a step, whose predecessor writes bbn.
+template <typename T, int DIM, bool TRACK, bool EARLY>
 __global__ void __launch_bounds__(SWEEP_THREADS) k_sor_half(Geo g, Coef<T> C, T* __restrict__ pc,
                                                             const T* __restrict__ po, T omw, int colour,
                                                             unsigned long long* __restrict__ err,
                                                             const int* __restrict__ skip) {
+  const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
+  int h = 0, j = 1, k = 1;
+  bool act = t < packed_items(g);
+  if (act) packed_item<DIM>(g, t, h, j, k);
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const int i = 2 * h + s;
+  act = act && j <= g.n && i >= 1 && i <= g.m;
+  const idx_t q = pk_idx(g, h, j, k);
+  T cb = T(0), c0 = T(0), c1 = T(0), c2 = T(0), c3 = T(0), c4 = T(0), c5 = T(0);
+  auto load_operator = [&]() {
+    cb = C.bbn[q];
+    c0 = C.a[0][q];
+    c1 = C.a[1][q];
+    c2 = C.a[2][q];
+    c3 = C.a[3][q];
+    if (DIM == 3) {
+      c4 = C.a[4][q];
+      c5 = C.a[5][q];
+    }
+  };
+  if (EARLY && act) load_operator();
   pdl_begin();
   if (skip && *skip) return;  // uniform over the grid: defect correction converged
-  const int t = blockIdx.x * SWEEP_THREADS + threadIdx.x;
+  if (!EARLY && act) load_operator();
   decltype(abs_bits(T(0))) e = 0;
-  if (t < packed_items(g)) {
-    int h, j, k;
-    packed_item<DIM>(g, t, h, j, k);
-    e = c_sor_half<T, DIM, TRACK>(g, C, pc, po, omw, colour, h, j, k);
+  if (act) {
+    const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+    const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
+    const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
+    const T pold = pc[q];
+    T tt = cb;
+    tt = fma(-c0, po[q + s], tt);
+    tt = fma(-c1, po[q - 1 + s], tt);
+    tt = fma(-c2, po[qn], tt);
+    tt = fma(-c3, po[qs], tt);
+    if (DIM == 3) {
+      const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
+      const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
+      tt = fma(-c4, po[qt], tt);
+      tt = fma(-c5, po[qb], tt);
+    }
+    const T pnew = fma(omw, pold, tt);
+    pc[q] = pnew;
+    if (TRACK) e = abs_diff_bits(pnew, pold);
   }
   if (TRACK) warp_max_atomic(e, err);
 }
@@ -1050,19 +1100,22 @@ static dim3 grid_packed(const Geo& g) {
 
 template <typename T>
 void launch_sor_half(const Geo& g, const Coef<T>& cc, T* pc, const T* po, T one_minus_omega, int colour,
-                     unsigned long long* err, const int* skip, cudaStream_t st) {
+                     unsigned long long* err, const int* skip, bool early, cudaStream_t st) {
   const unsigned grid = (unsigned)((packed_items(g) + SWEEP_THREADS - 1) / SWEEP_THREADS);
+#define PF_SH(D, TR, EA) \
+  launch_pdl(k_sor_half<T, D, TR, EA>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip)
   if (g.dim == 3) {
     if (err)
-      launch_pdl(k_sor_half<T, 3, true>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
+      early ? PF_SH(3, true, true) : PF_SH(3, true, false);
     else
-      launch_pdl(k_sor_half<T, 3, false>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
+      early ? PF_SH(3, false, true) : PF_SH(3, false, false);
   } else {
     if (err)
-      launch_pdl(k_sor_half<T, 2, true>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
+      early ? PF_SH(2, true, true) : PF_SH(2, true, false);
     else
-      launch_pdl(k_sor_half<T, 2, false>, grid, SWEEP_THREADS, st, g, cc, pc, po, one_minus_omega, colour, err, skip);
+      early ? PF_SH(2, false, true) : PF_SH(2, false, false);
   }
+#undef PF_SH
 }
 
 template <typename T>
@@ -1296,7 +1349,7 @@ void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* 
                                     const double*, const double*, const double*, unsigned long long*,       \
                                     cudaStream_t);                                                           \
   template void launch_sor_half<TV>(const Geo&, const Coef<TV>&, TV*, const TV*, TV, int,                   \
-                                    unsigned long long*, const int*, cudaStream_t);                          \
+                                    unsigned long long*, const int*, bool, cudaStream_t);                    \
   template void launch_p_halo<TV>(const Geo&, TV*, TV*, const int*, cudaStream_t);
 PF_INST_V(double)
 PF_INST_V(float)
