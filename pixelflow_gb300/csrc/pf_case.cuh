@@ -55,6 +55,7 @@ struct pf_case {
   float* e2[2] = {nullptr, nullptr};
   pf::FusedShape fused;
   bool use_fused = false;
+  bool dc_early = false;  // the split FP32 sweep's grid fits one wave: early operand loads
   float sweep_ms[2] = {0.f, 0.f};  // PF_SWEEP_AUTO: ms per sweep measured at creation (split, fused)
   float* rf[2] = {nullptr, nullptr};    // packed FP32 normalised residual (RHS of the sweeps)
   float* epsf[2] = {nullptr, nullptr};  // packed FP32 porosity (operator rebuilt on the fly)

@@ -159,8 +159,12 @@ void launch_accumulate(const Geo& g, double* p0, double* p1, const float* e0, co
 void launch_zero_u64(unsigned long long* p, int n, cudaStream_t st);
 void launch_zero_int(int* p, cudaStream_t st);
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
+// The FP32 split sweep (one colour); early: its grid fits one wave (see
+// dc_one_wave), so its fixed operands load before the dependency wait.
+bool dc_one_wave(const Geo& g, int sms);
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
-                   const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st);
+                   const float* eo, int colour, unsigned long long* err, const int* skip, bool early,
+                   cudaStream_t st);
 // Fused full correction sweep (both colours in one launch, 3D with even n
 // and l): launch shape chosen once per case.
 struct FusedShape {

@@ -640,6 +640,66 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const
   if (TRACK) warp_max_atomic(e, err);
 }
 
+// The same sweep for grids of one wave, where a launch's latency dominates:
+// porosity (set-up time) and the residual r (written by the residual kernel
+// of this colour, which finished before the kernel preceding this one could
+// let it launch) are loaded before griddepcontrol.wait, the correction,
+// which the preceding kernel may write, after it.  (On larger grids this
+// order of the loads costs more than it saves: 256^3 step 1553 -> 1414
+// Mcell-steps/s.)  The arithmetic is dc_chunk's, so the bits are k_sor_dc4's.
+template <int DIM, bool TRACK, int V>
+__global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4_early(Geo g, DCConst K, const float* __restrict__ epsc,
+                                                               const float* __restrict__ epso,
+                                                               const float* __restrict__ r, float* __restrict__ ec,
+                                                               const float* __restrict__ eo, int colour, int chunks,
+                                                               unsigned long long* __restrict__ err,
+                                                               const int* __restrict__ skip) {
+  const int t = blockIdx.x * DC4_THREADS + threadIdx.x;
+  const int rows = DIM == 3 ? g.n * g.l : g.n;
+  const bool act = t < chunks * rows;
+  const int row = act ? t / chunks : 0;
+  const int h0 = (t - row * chunks) * V;
+  const int k = DIM == 3 ? row / g.n + 1 : 0;
+  const int j = DIM == 3 ? row - (k - 1) * g.n + 1 : row + 1;
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
+  const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+  const idx_t q = pk_idx(g, h0, j, k);
+  VecF<V> R{}, PC{}, PO{}, PN{}, PS{}, PT{}, PB{};
+  float px = 0.f;
+  if (act) {
+    R = ldv<V>(r + q);
+    PC = ldv<V>(epsc + q);
+    PO = ldv<V>(epso + q);
+    px = s ? epso[q + V] : epso[q - 1];
+    PN = ldv<V>(epso + q + H);
+    PS = ldv<V>(epso + q - H);
+    if (DIM == 3) {
+      PT = ldv<V>(epso + q + HY);
+      PB = ldv<V>(epso + q - HY);
+    }
+  }
+  pdl_begin();
+  if (skip && *skip) return;
+  unsigned e = 0;
+  if (act) {
+    const idx_t qn = (j == g.n) ? pk_idx(g, h0, g.jn_n, k) : q + H;
+    const idx_t qs = (j == 1) ? pk_idx(g, h0, g.js_1, k) : q - H;
+    const VecF<V> EC = ldv<V>(ec + q), XO = ldv<V>(eo + q);
+    const float xx = s ? eo[q + V] : eo[q - 1];
+    const VecF<V> XN = ldv<V>(eo + qn), XS = ldv<V>(eo + qs);
+    VecF<V> XT{}, XB{};
+    if (DIM == 3) {
+      const idx_t qt = (k == g.l) ? pk_idx(g, h0, j, g.kt_l) : q + HY;
+      const idx_t qb = (k == 1) ? pk_idx(g, h0, j, g.kb_1) : q - HY;
+      XT = ldv<V>(eo + qt);
+      XB = ldv<V>(eo + qb);
+    }
+    *reinterpret_cast<VecF<V>*>(ec + q) =
+        dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, PC, XO, PO, xx, px, XN, XS, PN, PS, XT, XB, PT, PB, e);
+  }
+  if (TRACK) warp_max_atomic(e, err);
+}
+
 // The fused kernel's chunk: dc_chunk (3D, colour side S) with the top faces
 // either computed or given (ATIN: colour 1 takes them from the colour-0
 // update of the plane above, whose bottom faces they are).  The bottom faces
@@ -1179,8 +1239,23 @@ static DCConst dc_const(const Geo& g, const Scal& sc) {
   return make_dc_const(sc.dt, sc.dx, sc.dy, sc.dz, g.dim, sc.omega);
 }
 
+// Whether the FP32 split sweep's grid fits one wave of resident CTAs (its
+// fixed operands then load before the dependency wait).
+bool dc_one_wave(const Geo& g, int sms) {
+  const int chunks = (g.m >> 1) / 4 + 1;
+  const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
+  const long long blocks = (threads + DC4_THREADS - 1) / DC4_THREADS;
+  int per_sm = 0;
+  if (g.dim == 3)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sor_dc4_early<3, true, 4>, DC4_THREADS, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sor_dc4_early<2, true, 4>, DC4_THREADS, 0);
+  return blocks <= (long long)per_sm * sms;
+}
+
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
-                   const float* eo, int colour, unsigned long long* err, const int* skip, cudaStream_t st) {
+                   const float* eo, int colour, unsigned long long* err, const int* skip, bool early,
+                   cudaStream_t st) {
   const DCConst K = dc_const(g, sc);
   // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
   // 4 beat 2 and 8 per thread at 256^3 (1547 vs 1336 and 1508 Mcell-steps/s
@@ -1190,9 +1265,11 @@ void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float*
   const int chunks = (g.m >> 1) / V + 1;
   const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
   const unsigned blocks = (unsigned)((threads + DC4_THREADS - 1) / DC4_THREADS);
-#define PF_DC(DIMV, TR) \
-  launch_pdl(k_sor_dc4<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo, colour, \
-             chunks, err, skip)
+#define PF_DC(DIMV, TR)                                                                                          \
+  (early ? launch_pdl(k_sor_dc4_early<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo, \
+                      colour, chunks, err, skip)                                                                     \
+         : launch_pdl(k_sor_dc4<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo,       \
+                      colour, chunks, err, skip))
   if (g.dim == 3) {
     if (err)
       PF_DC(3, true);

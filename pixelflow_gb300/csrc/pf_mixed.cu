@@ -52,7 +52,7 @@ int mixed_choose_sweep(pf_case* c) {
     for (int it = 0; it < SWEEPS; it++)
       for (int col = 0; col < 2; col++)
         launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
-                      col == 1 ? err : nullptr, nullptr, st);
+                      col == 1 ? err : nullptr, nullptr, c->dc_early, st);
     cudaEventRecord(ev[1], st);
     for (int it = 0; it < SWEEPS; it++) {
       const float* ea[2] = {it & 1 ? c->e2[0] : c->e[0], it & 1 ? c->e2[1] : c->e[1]};
@@ -104,10 +104,11 @@ int mixed_alloc(pf_case* c) {
     req[nr++] = {&c->epsf[col], pk};
     req[nr++] = {&c->e2[col], fused ? pk : 0};
   }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  c->dc_early = dc_one_wave(c->g, sms);
   if (fused) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int fe = fused_setup(c->g, c->opt.fused_rows, c->opt.fused_planes, sms, c->fused);
     if (fe) return cuda_fail((cudaError_t)fe, "fused sweep set-up");
   }
@@ -198,7 +199,7 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
           if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
           unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
           launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err,
-                        skip, st);
+                        skip, c->dc_early, st);
         }
       }
     }
