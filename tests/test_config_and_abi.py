@@ -110,7 +110,8 @@ def test_reference_cylinder_fixture_parses(tmp_path):
 
 
 def _declared_symbols():
-    text = open(HEADER).read()
+    with open(HEADER) as f:
+        text = f.read()
     return sorted(set(re.findall(r"\b(pf_[a-z_0-9]+)\s*\(", text)))
 
 
