@@ -11,8 +11,10 @@ FP64, iter_max=100, omega=1.7 -- with synthetic (seeded) porosity.
 
 Prints one JSON line.  `value` is device time (CUDA events on the case's
 stream) with the fields resident in HBM; `e2e` is the same metric through the
-C ABI with pinned host buffers copied in (pf_set_state) and out
-(pf_get_state) every step.  With --gpus N > 1 (torchrun) every rank advances
+C ABI with pinned host buffers copied in and out every step: pf_step_host
+(one step from host fields to host fields, the input copies overlapped with
+the predictor), and under `three_calls` the same through pf_set_state +
+pf_step + pf_get_state.  With --gpus N > 1 (torchrun) every rank advances
 its own replica of the case (no exchange between ranks: the path shards by
 case), and `value` is the sum over ranks over the max-over-ranks time.
 
@@ -430,6 +432,15 @@ def run_ours(args):
     out = {k: np.empty_like(a) for k, a in host.items()}
     for a in out.values():
         host_register(a)
+    # pf_step_host: one step from host fields to host fields (input copies in
+    # slabs beside the predictor); the same through the three calls it
+    # stands for (set_state, step, get_state) for comparison
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        case.step_host(host, out)
+    t1 = time.perf_counter()
+    e2e_s = reduce_max(t1 - t0, world)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -437,12 +448,13 @@ def run_ours(args):
         case.step(1)
         case.get_state(out)
     t1 = time.perf_counter()
-    e2e_s = reduce_max(t1 - t0, world)
+    three_s = reduce_max(t1 - t0, world)
     for a in list(host.values()) + list(out.values()):
         host_unregister(a)
     nbytes = sum(a.nbytes for a in host.values())
     e2e = {"value": world * cells * args.steps / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-           "d2h_bytes_per_step": nbytes}
+           "d2h_bytes_per_step": nbytes, "call": "pf_step_host",
+           "three_calls": world * cells * args.steps / three_s / 1e6}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,

@@ -165,6 +165,18 @@ int pf_boundary(pf_case *c);
 int pf_step(pf_case *c, int nsteps);
 int pf_synchronize(pf_case *c);
 
+/* One pass of the step loop body (2D :80-125, 3D :81-132) from host arrays
+ * to host arrays, for a caller whose fields live on the host between steps:
+ * the result equals pf_set_state(u, v, w, p) + pf_step(c, 1) +
+ * pf_get_state(u_out, ...), bit for bit.  For 3D periodic plain-FP64 cases
+ * with ld1 = m+2 and ld2 = n+2 the input copies run in slabs of planes beside
+ * the divergence and the predictor of the planes already in place (the first
+ * use allocates three fields of device staging, counted by
+ * pf_memory_bytes); other cases make the three calls.  A null output field is
+ * not read back.  Waits for the result. */
+int pf_step_host(pf_case *c, const double *u, const double *v, const double *w, const double *p,
+                 double *u_out, double *v_out, double *w_out, double *p_out, int ld1, int ld2);
+
 /* max|div u| of the porosity-weighted divergence that output_divergent_2d/3d
  * writes (lib/output.f90:217-224, :929-941) on the current fields, and the
  * SOR `error` of the last solve_p (the value the reference prints at

@@ -93,6 +93,7 @@ _PROTOS = {
     "pf_projection": (_I, [_VP]),
     "pf_boundary": (_I, [_VP]),
     "pf_step": (_I, [_VP, _I]),
+    "pf_step_host": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _I]),
     "pf_synchronize": (_I, [_VP]),
     "pf_norms": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "pf_forces": (_I, [_VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),

@@ -30,6 +30,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 static int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
+// one field in the dense (m+2)(n+2)[(l+2)] host layout
+static size_t dense_bytes(const Geo& g) { return (size_t)(g.m + 2) * (g.n + 2) * g.Z * sizeof(double); }
+
 int make_geo(const pf_params& p, Geo& g) {
   if (p.dim != 2 && p.dim != 3) return fail(PF_E_INVALID, "dim must be 2 or 3");
   if (p.m < 3 || p.n < 3 || (p.dim == 3 && p.l < 3))
@@ -249,9 +252,13 @@ static int case_alloc(pf_case* c) {
 
 static void case_free(pf_case* c) {
   if (!c) return;
-  for (int b = 0; b < 2; b++)
-    if (c->gexec[b]) cudaGraphExecDestroy(c->gexec[b]);
+  for (auto& part : c->gexec)
+    for (auto& x : part)
+      if (x) cudaGraphExecDestroy(x);
   for (auto& e : c->events) cudaEventDestroy(e);
+  for (auto& e : c->ev_io) cudaEventDestroy(e);
+  if (c->iostage) cudaFree(c->iostage);
+  if (c->st_io) cudaStreamDestroy(c->st_io);
   if (c->base) cudaFree(c->base);
   mixed_free(c);
   if (c->hred) cudaFreeHost(c->hred);
@@ -266,16 +273,20 @@ static void case_free(pf_case* c) {
 
 // solve_p on the device: snapshot (buffer swap), divergence, predictor,
 // RHS, SOR.  Only stream-ordered launches, so it can be graph-captured.
-static void enqueue_solve_p(pf_case* c, bool prof) {
+// head = false leaves out the divergence and the predictor (pf_step_host
+// issues them plane range by plane range as the input planes arrive).
+static void enqueue_solve_p(pf_case* c, bool prof, bool head) {
   const Geo& g = c->g;
   const Scal& s = c->s;
   cudaStream_t st = c->st;
   const int o = c->cur, nw = 1 - c->cur;
   const bool track = c->opt.track_sor_error != 0;
   if (track) launch_zero_u64(&c->red[RED_ERR], RED_SLOTS, st);
-  launch_divergence<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, st);
-  launch_predictor<double, double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv,
-                                   c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
+  if (head) {
+    launch_divergence<double>(g, s, c->U[o], c->V[o], c->W[o], c->div, st);
+    launch_predictor<double, double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv,
+                                     c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
+  }
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);
@@ -293,7 +304,7 @@ static void enqueue_solve_p(pf_case* c, bool prof) {
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
   if (!g.wall) launch_p_halo<double>(g, c->p[0], c->p[1], nullptr, st);
-  c->launches += 3 + (track ? 1 : 0) + (g.wall ? 0 : 1) + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
+  c->launches += (head ? 3 : 1) + (track ? 1 : 0) + (g.wall ? 0 : 1) + (int64_t)c->prm.iter_max * 2 * (halo ? 2 : 1);
   c->cur = nw;
 }
 
@@ -309,13 +320,14 @@ static void enqueue_boundary(pf_case* c) {
   launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
 }
 
-static void enqueue_step(pf_case* c, bool prof) {
+// head = false: the step after the predictor (plain FP64 form only)
+static void enqueue_step(pf_case* c, bool prof, bool head = true) {
   if (c->opt.precision == PF_PREC_MIXED) {
     enqueue_solve_p_mixed(c, prof);
     enqueue_projection_mixed(c);
     enqueue_boundary_mixed(c);
   } else {
-    enqueue_solve_p(c, prof);
+    enqueue_solve_p(c, prof, head);
     enqueue_projection(c);
     enqueue_boundary(c);
   }
@@ -327,24 +339,27 @@ static int check_launch(const char* what) {
   return PF_OK;
 }
 
-static int step_graph(pf_case* c) {
-  const int b = c->cur;
-  if (!c->gexec[b]) {
+// Replays the captured step (head = false: the part after the predictor),
+// capturing it on first use for the current buffer.
+static int step_graph(pf_case* c, bool head = true) {
+  const int b = c->cur, part = head ? 0 : 1;
+  cudaGraphExec_t& x = c->gexec[part][b];
+  if (!x) {
     cudaGraph_t graph = nullptr;
     PF_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     const int64_t before = c->launches;
-    enqueue_step(c, false);
-    c->graph_kernels[b] = c->launches - before;
+    enqueue_step(c, false, head);
+    c->graph_kernels[part][b] = c->launches - before;
     c->launches = before;
     cudaError_t e = cudaStreamEndCapture(c->st, &graph);
     c->cur = b;  // capture only recorded the swap
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&c->gexec[b], graph, 0);
+    e = cudaGraphInstantiate(&x, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   }
-  PF_CUDA(cudaGraphLaunch(c->gexec[b], c->st));
-  c->launches += c->graph_kernels[b];
+  PF_CUDA(cudaGraphLaunch(x, c->st));
+  c->launches += c->graph_kernels[part][b];
   c->cur = 1 - b;
   return PF_OK;
 }
@@ -633,6 +648,145 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   return check_flags(c);
 }
 
+// ---- one step from host state to host state ------------------------------
+// pf_step_host = pf_set_state + pf_step(1) + pf_get_state with the copies
+// overlapped with the step's first stages.  A step's input and its result
+// are dependent, but the divergence and the predictor at plane k read the old
+// velocities of planes k-1 .. k+1 only (the periodic z-wrap of the
+// divergence aside).  So the input arrives on a second stream in slabs of
+// planes and the case's stream runs the divergence and the predictor over
+// each range of planes whose inputs are in place while the next slabs are in
+// flight; p (read first by the SOR) comes last.  Plane 1 of the predictor
+// reads the divergence of plane l through the wrap and runs after the last
+// slab.  Each cell's arithmetic is the step's own, so the results are those of
+// the three calls (tested bit for bit).  The readback overlaps the gathers of
+// the next fields with the copies of the previous ones.
+static constexpr int IO_SLABS = 16;  // slabs of the input (the first one is exposed)
+
+static bool step_host_overlaps(const pf_case* c, int ld1, int ld2) {
+  const Geo& g = c->g;
+  return g.dim == 3 && !g.wall && c->opt.precision == PF_PREC_FP64 && !c->profiling && ld1 == g.m + 2 &&
+         ld2 == g.n + 2;
+}
+
+static int io_setup(pf_case* c, size_t nevents) {
+  if (!c->iostage) {
+    cudaError_t e = cudaMalloc(&c->iostage, 3 * dense_bytes(c->g));
+    if (e != cudaSuccess) {
+      c->iostage = nullptr;
+      return cuda_fail(e, "cudaMalloc(host-step staging)");
+    }
+  }
+  if (!c->st_io) PF_CUDA(cudaStreamCreateWithFlags(&c->st_io, cudaStreamNonBlocking));
+  while (c->ev_io.size() < nevents) {
+    cudaEvent_t e;
+    PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->ev_io.push_back(e);
+  }
+  return PF_OK;
+}
+
+static int step_host_overlapped(pf_case* c, const double* const* in, double* const* out) {
+  const Geo& g = c->g;
+  const Scal& s = c->s;
+  const int Z = g.Z, l = g.l;
+  const int slab = std::max(2, (Z + IO_SLABS - 1) / IO_SLABS);
+  const int nslabs = (Z + slab - 1) / slab;
+  int rc = io_setup(c, (size_t)nslabs + 6);
+  if (rc) return rc;
+  cudaEvent_t* ev = c->ev_io.data();  // [0] start, [1..nslabs] slabs, then p in, 4 fields out
+  cudaEvent_t ev_p = ev[nslabs + 1];
+  const size_t plane = (size_t)(g.m + 2) * (g.n + 2), field = plane * Z;
+  const int o = c->cur, nw = 1 - o;
+  double* vel[3] = {c->U[o], c->V[o], c->W[o]};
+  // the staging and the old fields may still be in use by earlier calls
+  PF_CUDA(cudaEventRecord(ev[0], c->st));
+  PF_CUDA(cudaStreamWaitEvent(c->st_io, ev[0], 0));
+  for (int b = 0; b < nslabs; b++) {
+    const size_t k0 = (size_t)b * slab, nk = std::min<size_t>(slab, Z - k0);
+    for (int f = 0; f < 3; f++)
+      PF_CUDA(cudaMemcpyAsync(c->iostage + f * field + k0 * plane, in[f] + k0 * plane, nk * plane * sizeof(double),
+                              cudaMemcpyHostToDevice, c->st_io));
+    PF_CUDA(cudaEventRecord(ev[1 + b], c->st_io));
+  }
+  PF_CUDA(cudaMemcpyAsync(c->stage, in[3], field * sizeof(double), cudaMemcpyHostToDevice, c->st_io));
+  PF_CUDA(cudaEventRecord(ev_p, c->st_io));
+  // div_to / pred_to: the last plane done (the predictor starts at plane 2)
+  int div_to = 0, pred_to = 1;
+  for (int b = 0; b < nslabs; b++) {
+    const int k0 = b * slab, k1 = std::min(k0 + slab, Z) - 1;
+    PF_CUDA(cudaStreamWaitEvent(c->st, ev[1 + b], 0));
+    for (int f = 0; f < 3; f++) launch_scatter_nat_planes(g, c->iostage + f * field, vel[f], k0, k1, c->st);
+    c->launches += 3;
+    // the divergence at k reads planes k-1 .. k+1; the predictor at k reads
+    // them and the divergence at k-1 .. k+1 (plane l: at l-1, l and 1)
+    const int d = std::min(k1 - 1, l);
+    if (d > div_to) {
+      launch_divergence<double>(g, s, vel[0], vel[1], vel[2], c->div, c->st, div_to + 1, d);
+      c->launches += 1;
+      div_to = d;
+    }
+    const int pr = div_to == l ? l : div_to - 1;
+    if (pr > pred_to) {
+      launch_predictor<double, double>(g, s, vel[0], vel[1], vel[2], c->div, c->gx, c->gy, c->gz, c->rinv,
+                                       c->damp, vel[0], vel[1], vel[2], c->U[nw], c->V[nw], c->W[nw], c->st,
+                                       pred_to + 1, pr);
+      c->launches += 1;
+      pred_to = pr;
+    }
+  }
+  launch_predictor<double, double>(g, s, vel[0], vel[1], vel[2], c->div, c->gx, c->gy, c->gz, c->rinv, c->damp,
+                                   vel[0], vel[1], vel[2], c->U[nw], c->V[nw], c->W[nw], c->st, 1, 1);
+  PF_CUDA(cudaStreamWaitEvent(c->st, ev_p, 0));
+  launch_scatter_pk(g, c->stage, c->p[0], c->p[1], c->st);
+  c->launches += 2;
+  rc = check_launch("pf_step_host");
+  if (rc) return rc;
+  // the rest of the step: RHS, SOR, projection, boundary
+  if (c->opt.use_graph) {
+    rc = step_graph(c, false);
+    if (rc) return rc;
+  } else {
+    enqueue_step(c, false, false);
+  }
+  // readback: the gather of a field overlaps the copy of the previous one
+  const int b = c->cur;
+  const double* src[3] = {c->U[b], c->V[b], c->W[b]};
+  for (int f = 0; f < 4; f++) {
+    if (!out[f]) continue;
+    double* stg = f < 3 ? c->iostage + f * field : c->stage;
+    if (f < 3)
+      launch_gather_nat(g, src[f], stg, c->st);
+    else
+      launch_gather_pk(g, c->p[0], c->p[1], stg, c->st);
+    c->launches += 1;
+    PF_CUDA(cudaEventRecord(ev[nslabs + 2 + f], c->st));
+    PF_CUDA(cudaStreamWaitEvent(c->st_io, ev[nslabs + 2 + f], 0));
+    PF_CUDA(cudaMemcpyAsync(out[f], stg, field * sizeof(double), cudaMemcpyDeviceToHost, c->st_io));
+  }
+  rc = check_launch("pf_step_host");
+  if (rc) return rc;
+  PF_CUDA(cudaStreamSynchronize(c->st_io));
+  PF_CUDA(cudaStreamSynchronize(c->st));
+  return check_flags(c);
+}
+
+int pf_step_host(pf_case* c, const double* u, const double* v, const double* w, const double* p, double* u_out,
+                 double* v_out, double* w_out, double* p_out, int ld1, int ld2) {
+  if (!c || !u || !v || !p || (c->g.dim == 3 && !w)) return fail(PF_E_INVALID, "pf_step_host: null argument");
+  int rc = check_ld(c, ld1, ld2);
+  if (rc) return rc;
+  if (step_host_overlaps(c, ld1, ld2)) {
+    const double* in[4] = {u, v, w, p};
+    double* out[4] = {u_out, v_out, w_out, p_out};
+    return step_host_overlapped(c, in, out);
+  }
+  rc = pf_set_state(c, u, v, w, p, ld1, ld2);
+  if (rc == PF_OK) rc = pf_step(c, 1);
+  if (rc == PF_OK) rc = pf_get_state(c, u_out, v_out, w_out, p_out, ld1, ld2);
+  return rc;
+}
+
 int pf_snapshot_begin(pf_case* c) {
   if (!c) return fail(PF_E_INVALID, "null handle");
   if (c->snap_pending) return fail(PF_E_BUSY, "pf_snapshot_begin: the previous snapshot was not collected");
@@ -723,7 +877,7 @@ int pf_solve_p(pf_case* c) {
   if (c->opt.precision == PF_PREC_MIXED)
     enqueue_solve_p_mixed(c, false);
   else
-    enqueue_solve_p(c, false);
+    enqueue_solve_p(c, false, true);
   return check_launch("pf_solve_p");
 }
 
@@ -897,17 +1051,18 @@ int pf_debug_fused_drop_stage(pf_case* c, int stage) {
   if (!c) return fail(PF_E_INVALID, "null handle");
   if (!c->use_fused) return fail(PF_E_STATE, "the case does not run the fused correction sweep");
   c->fused.drop_stage = stage < 0 ? -1 : stage;
-  for (int b = 0; b < 2; b++)  // captured launches hold the old value
-    if (c->gexec[b]) {
-      cudaGraphExecDestroy(c->gexec[b]);
-      c->gexec[b] = nullptr;
-    }
+  for (auto& part : c->gexec)  // captured launches hold the old value
+    for (auto& x : part)
+      if (x) {
+        cudaGraphExecDestroy(x);
+        x = nullptr;
+      }
   return PF_OK;
 }
 
 int pf_memory_bytes(pf_case* c, size_t* bytes) {
   if (!c || !bytes) return fail(PF_E_INVALID, "null argument");
-  *bytes = c->bytes + c->mixed_bytes;
+  *bytes = c->bytes + c->mixed_bytes + (c->iostage ? 3 * dense_bytes(c->g) : 0);
   return PF_OK;
 }
 

@@ -25,7 +25,9 @@ struct pf_case {
   double* stage = nullptr;          // dense (m+2)(n+2)[(l+2)] staging
   unsigned long long* red = nullptr;   // [0] SOR error bits, [1] max|div| bits, [2] max|r| bits, [3] flag
   unsigned long long* hred = nullptr;  // pinned host mirror
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  // step graphs [part][buffer]: part 0 the whole step, part 1 the step after
+  // the predictor (pf_step_host issues the divergence and predictor itself)
+  cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   // profiling
   bool profiling = false;
   int64_t prof_steps = 0;
@@ -41,7 +43,12 @@ struct pf_case {
   cudaStream_t st_snap = nullptr;
   cudaEvent_t ev_snap[2] = {nullptr, nullptr};
   bool snap_pending = false;
-  int64_t graph_kernels[2] = {0, 0};
+  int64_t graph_kernels[2][2] = {{0, 0}, {0, 0}};
+  // pf_step_host, allocated on first use: dense staging of u, v, w, the
+  // stream that copies between host and staging, and its events
+  double* iostage = nullptr;
+  cudaStream_t st_io = nullptr;
+  std::vector<cudaEvent_t> ev_io;
 
   // ---- mixed precision form (pf_mixed.cu) ----
   char* mbase = nullptr;

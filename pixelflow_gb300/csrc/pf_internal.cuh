@@ -121,13 +121,15 @@ void launch_porosity_factors(const Geo& g, const Scal& s, const double* poro, do
                              double* gz, double* rinv, double* damp, cudaStream_t st);
 void launch_setup_coef(const Geo& g, const Scal& s, const double* poro, Coef<double> c0, Coef<double> c1,
                        cudaStream_t st);
+// k_lo .. k_hi: the interior planes of a 3D grid to cover (default: all)
 template <typename TV>
 void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, TV* div,
-                       cudaStream_t st);
+                       cudaStream_t st, int k_lo = 1, int k_hi = 0);
 template <typename T, typename TS>
 void launch_predictor(const Geo& g, const Scal& s, const T* uo, const T* vo, const T* wo, const T* div,
                       const T* gx, const T* gy, const T* gz, const T* rinv, const T* damp, const TS* us,
-                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st);
+                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st, int k_lo = 1,
+                      int k_hi = 0);
 template <typename TV>
 void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
                 const double* gx, const double* gy, const double* gz, Coef<double> c0, Coef<double> c1,
@@ -194,6 +196,9 @@ void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
 // staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts
 void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st);
+// planes k_lo .. k_hi (ghost planes included) of the dense staging
+void launch_scatter_nat_planes(const Geo& g, const double* stage, double* dst, int k_lo, int k_hi,
+                               cudaStream_t st);
 void launch_gather_nat(const Geo& g, const double* src, double* stage, cudaStream_t st);
 void launch_scatter_pk(const Geo& g, const double* stage, double* p0, double* p1, cudaStream_t st);
 void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* stage, cudaStream_t st);

@@ -164,14 +164,15 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
 
 // Divergence of u_old (interior).  The 2D v-term divides by dx, as the
 // reference does (ibm_2d_uniform_omp_cpu.f90:176).  Ghost columns stay 0;
-// the periodic ghost rows are read by wrapping in the predictor.
+// the periodic ghost rows are read by wrapping in the predictor.  3D grids
+// cover the planes k0+1 .. k0+gridDim.z.
 template <typename T>
 __global__ void k_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* __restrict__ vo,
-                             const T* __restrict__ wo, T* __restrict__ div) {
+                             const T* __restrict__ wo, T* __restrict__ div, int k0) {
   pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = (g.dim == 3) ? blockIdx.z + 1 : 0;
+  const int k = (g.dim == 3) ? blockIdx.z + 1 + k0 : 0;
   if (i > g.m || j > g.n) return;
   c_divergence<T>(g, s, uo, vo, wo, div, i, j, k);
 }
@@ -182,7 +183,8 @@ __global__ void k_divergence(Geo g, Scal s, const T* __restrict__ uo, const T* _
 // T: type of the stencil arithmetic and of the arrays it reads; TS: type of
 // the velocity state.  The predictor computes the increment u* - u_old in T
 // and adds it to the TS state, so with T = float, TS = double the stencils run
-// in FP32 while the state keeps FP64 precision.
+// in FP32 while the state keeps FP64 precision.  3D grids cover the planes
+// k0+1 .. k0+gridDim.z.
 template <typename T, typename TS, int DIM>
 __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __restrict__ uo,
                                                       const T* __restrict__ vo, const T* __restrict__ wo,
@@ -191,11 +193,11 @@ __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __
                                                       const T* __restrict__ rinva, const T* __restrict__ dampa,
                                                       const TS* __restrict__ su, const TS* __restrict__ sv,
                                                       const TS* __restrict__ sw, TS* __restrict__ u,
-                                                      TS* __restrict__ v, TS* __restrict__ w) {
+                                                      TS* __restrict__ v, TS* __restrict__ w, int k0) {
   pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = (DIM == 3) ? blockIdx.z + 1 : 0;
+  const int k = (DIM == 3) ? blockIdx.z + 1 + k0 : 0;
   if (i > g.m || j > g.n) return;
   c_predictor<T, TS, DIM>(g, s, uo, vo, wo, div, gxa, gya, gza, rinva, dampa, su, sv, sw, u, v, w, i, j, k);
 }
@@ -1116,32 +1118,43 @@ void launch_setup_coef(const Geo& g, const Scal& s, const double* poro, Coef<dou
   k_setup_coef<<<grid_interior(g), dim3(BX, BY), 0, st>>>(g, s, poro, c0, c1);
 }
 
+// The interior planes k_lo .. k_hi of a 3D grid (k_hi < k_lo: all of them).
+static dim3 grid_planes(const Geo& g, int k_lo, int k_hi) {
+  dim3 grid = grid_interior(g);
+  if (g.dim == 3 && k_hi >= k_lo) grid.z = k_hi - k_lo + 1;
+  return grid;
+}
+static int plane_offset(const Geo& g, int k_lo, int k_hi) { return g.dim == 3 && k_hi >= k_lo ? k_lo - 1 : 0; }
+
 template <typename TV>
 void launch_divergence(const Geo& g, const Scal& s, const TV* uo, const TV* vo, const TV* wo, TV* div,
-                       cudaStream_t st) {
-  launch_pdl(k_divergence<TV>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div);
+                       cudaStream_t st, int k_lo, int k_hi) {
+  launch_pdl(k_divergence<TV>, grid_planes(g, k_lo, k_hi), dim3(BX, BY), st, g, s, uo, vo, wo, div,
+             plane_offset(g, k_lo, k_hi));
 }
 
 template <typename T, typename TS>
 void launch_predictor(const Geo& g, const Scal& s, const T* uo, const T* vo, const T* wo, const T* div,
                       const T* gx, const T* gy, const T* gz, const T* rinv, const T* damp, const TS* us,
-                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st) {
+                      const TS* vs, const TS* ws, TS* u, TS* v, TS* w, cudaStream_t st, int k_lo, int k_hi) {
+  const dim3 grid = grid_planes(g, k_lo, k_hi);
+  const int k0 = plane_offset(g, k_lo, k_hi);
   if (g.dim == 3)
-    launch_pdl(k_predictor<T, TS, 3>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv,
-                                                                     damp, us, vs, ws, u, v, w);
+    launch_pdl(k_predictor<T, TS, 3>, grid, dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv, damp, us,
+               vs, ws, u, v, w, k0);
   else
-    launch_pdl(k_predictor<T, TS, 2>, grid_interior(g), dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv,
-                                                                     damp, us, vs, ws, u, v, w);
+    launch_pdl(k_predictor<T, TS, 2>, grid, dim3(BX, BY), st, g, s, uo, vo, wo, div, gx, gy, gz, rinv, damp, us,
+               vs, ws, u, v, w, k0);
 }
 template void launch_predictor<double, double>(const Geo&, const Scal&, const double*, const double*,
                                                const double*, const double*, const double*, const double*,
                                                const double*, const double*, const double*, const double*,
                                                const double*, const double*, double*, double*, double*,
-                                               cudaStream_t);
+                                               cudaStream_t, int, int);
 template void launch_predictor<float, double>(const Geo&, const Scal&, const float*, const float*, const float*,
                                               const float*, const float*, const float*, const float*,
                                               const float*, const float*, const double*, const double*,
-                                              const double*, double*, double*, double*, cudaStream_t);
+                                              const double*, double*, double*, double*, cudaStream_t, int, int);
 
 template <typename TV>
 void launch_rhs(const Geo& g, const Scal& s, const TV* u, const TV* v, const TV* w, const double* poro,
@@ -1401,6 +1414,13 @@ void launch_to_double(const float* src, double* dst, long long n, cudaStream_t s
 void launch_scatter_nat(const Geo& g, const double* stage, double* dst, cudaStream_t st) {
   k_scatter_nat<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, stage, dst);
 }
+void launch_scatter_nat_planes(const Geo& g, const double* stage, double* dst, int k_lo, int k_hi,
+                               cudaStream_t st) {
+  Geo gp = g;  // the planes k_lo .. k_hi of both layouts, addressed from plane k_lo
+  gp.Z = k_hi - k_lo + 1;
+  const double* src = stage + (idx_t)k_lo * (g.m + 2) * (g.n + 2);
+  k_scatter_nat<<<grid_all(gp), dim3(BX, BY), 0, st>>>(gp, src, dst + (idx_t)k_lo * g.X * g.Y);
+}
 void launch_gather_nat(const Geo& g, const double* src, double* stage, cudaStream_t st) {
   k_gather_nat<<<grid_all(g), dim3(BX, BY), 0, st>>>(g, src, stage);
 }
@@ -1414,7 +1434,7 @@ void launch_gather_pk(const Geo& g, const double* p0, const double* p1, double* 
 // explicit instantiations ------------------------------------------------
 #define PF_INST_V(TV)                                                                                        \
   template void launch_divergence<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, TV*,         \
-                                      cudaStream_t);                                                         \
+                                      cudaStream_t, int, int);                                               \
   template void launch_rhs<TV>(const Geo&, const Scal&, const TV*, const TV*, const TV*, const double*,      \
                                const double*, const double*, const double*, Coef<double>, Coef<double>,     \
                                cudaStream_t);                                                                \

@@ -69,6 +69,15 @@ module pixelflow_gpu
       integer(c_int), value :: ld1, ld2
     end function
 
+    integer(c_int) function pf_step_host(h, u, v, w, p, u_out, v_out, w_out, p_out, ld1, ld2) &
+        bind(C, name="pf_step_host")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: u(*), v(*), w(*), p(*)
+      real(c_double), intent(out) :: u_out(*), v_out(*), w_out(*), p_out(*)
+      integer(c_int), value :: ld1, ld2
+    end function
+
     integer(c_int) function pf_solve_p(h) bind(C, name="pf_solve_p")
       import :: c_int, c_ptr
       type(c_ptr), value :: h

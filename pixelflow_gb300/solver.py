@@ -218,6 +218,25 @@ class Case:
                                   ld1, ld2))
         return out
 
+    def step_host(self, state: Dict[str, np.ndarray], out: Optional[Dict[str, np.ndarray]] = None
+                  ) -> Dict[str, np.ndarray]:
+        """One step from the host fields in `state` to the host fields in `out`:
+        the same result as set_state + step(1) + get_state, with the input
+        copies overlapped with the first stages of the step where the case
+        allows it (3D periodic plain FP64, dense host fields)."""
+        if out is None:
+            out = {k: np.empty(self.field_shape) for k in (("u", "v", "p") + (("w",) if self.dim == 3 else ()))}
+        ld1, ld2 = self._check_field(state["u"])
+        names = ("u", "v", "p") + (("w",) if self.dim == 3 else ())
+        for k in names:
+            if self._check_field(state[k]) != (ld1, ld2) or self._check_field(out[k]) != (ld1, ld2):
+                raise ValueError("all fields must share leading dimensions")
+        check(self.L.pf_step_host(self.h, _ptr(state["u"]), _ptr(state["v"]), _ptr(state.get("w")),
+                                  _ptr(state["p"]), _ptr(out["u"]), _ptr(out["v"]), _ptr(out.get("w")),
+                                  _ptr(out["p"]), ld1, ld2))
+        self.steps_done = getattr(self, "steps_done", 0) + 1
+        return out
+
     def snapshot_begin(self):
         """Start copying the state as of the last enqueued step to the host
         without waiting (the copy overlaps the steps enqueued after it)."""

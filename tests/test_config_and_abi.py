@@ -144,4 +144,5 @@ def test_invalid_arguments_fail_before_any_device_work():
     assert L.pf_create(None, None, None, ctypes.byref(h)) == -1
     assert L.pf_destroy(None) == -1
     assert L.pf_step(None, 1) == -1
+    assert L.pf_step_host(None, None, None, None, None, None, None, None, None, 6, 6) == -1
     assert L.pf_strerror(-4) == b"non-finite values in the fields"
