@@ -53,6 +53,18 @@ def test_step_host_matches_three_calls(shape, use_graph):
             state = ref
 
 
+def test_step_host_in_place():
+    shape = (28, 20, 26)
+    s = G.settings_spheres_3d(iter_max=15)
+    vals = G.spheres_3d(*shape, count=3, seed=11)
+    with Case(s, shape, vals) as a, Case(s, shape, vals) as b:
+        state = _start_state(a, 2)
+        _start_state(b, 2)
+        ref = _three_calls(a, state)
+        got = b.step_host(state, state)  # the output overwrites the input arrays
+        assert got is state and _same(state, ref)
+
+
 def test_step_host_untracked_and_resident_run():
     shape = (36, 28, 22)
     s = G.settings_spheres_3d(iter_max=25, track_sor_error=0)
