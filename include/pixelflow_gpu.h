@@ -302,6 +302,14 @@ int pf_sweep_info(pf_case *c, int *fused, float *split_ms, float *fused_ms);
  * does not run the fused sweep. */
 int pf_debug_fused_drop_stage(pf_case *c, int stage);
 
+/* The schedule pf_step_host follows for a 3D case with l planes (no device
+ * work): per slab of input planes, six ints -- the planes k0, k1 it brings
+ * (ghost planes 0 and l+1 included), then the divergence planes and the
+ * predictor planes issued once it is in place (lo, hi; empty when hi < lo).
+ * Plane 1 of the predictor runs after the last slab.  Writes up to
+ * `capacity` slabs and returns the number of slabs. */
+int pf_debug_step_host_plan(int l, int *slabs, int capacity);
+
 #ifdef __cplusplus
 }
 #endif

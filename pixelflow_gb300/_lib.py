@@ -106,6 +106,7 @@ _PROTOS = {
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     "pf_debug_fused_drop_stage": (_I, [_VP, _I]),
+    "pf_debug_step_host_plan": (_I, [_I, _VP, _I]),
     "pf_sweep_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
     "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),

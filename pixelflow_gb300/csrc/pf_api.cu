@@ -669,6 +669,37 @@ static bool step_host_overlaps(const pf_case* c, int ld1, int ld2) {
          ld2 == g.n + 2;
 }
 
+// The schedule over the l+2 planes (ghosts included) of a 3D case: slab b
+// brings planes k0 .. k1; after it the divergence covers div_lo .. div_hi and
+// the predictor pred_lo .. pred_hi (empty when hi < lo).  The divergence at k
+// reads the old velocities at k-1 .. k+1; the predictor at k reads them and
+// the divergence at k-1 .. k+1 (plane l: l-1, l and plane 1 through the
+// wrap).  Plane 1 reads the divergence of plane l and runs after the last slab.
+struct HostSlab {
+  int k0, k1, div_lo, div_hi, pred_lo, pred_hi;
+};
+static std::vector<HostSlab> host_step_plan(int l) {
+  const int Z = l + 2;
+  const int slab = std::max(2, (Z + IO_SLABS - 1) / IO_SLABS);
+  std::vector<HostSlab> plan;
+  int div_to = 0, pred_to = 1;  // the last plane done (the predictor starts at plane 2)
+  for (int k0 = 0; k0 < Z; k0 += slab) {
+    HostSlab h{k0, std::min(k0 + slab, Z) - 1, 0, -1, 0, -1};
+    const int d = std::min(h.k1 - 1, l);
+    if (d > div_to) {
+      h.div_lo = div_to + 1;
+      h.div_hi = div_to = d;
+    }
+    const int pr = div_to == l ? l : div_to - 1;
+    if (pr > pred_to) {
+      h.pred_lo = pred_to + 1;
+      h.pred_hi = pred_to = pr;
+    }
+    plan.push_back(h);
+  }
+  return plan;
+}
+
 static int io_setup(pf_case* c, size_t nevents) {
   if (!c->iostage) {
     cudaError_t e = cudaMalloc(&c->iostage, 3 * dense_bytes(c->g));
@@ -689,21 +720,20 @@ static int io_setup(pf_case* c, size_t nevents) {
 static int step_host_overlapped(pf_case* c, const double* const* in, double* const* out) {
   const Geo& g = c->g;
   const Scal& s = c->s;
-  const int Z = g.Z, l = g.l;
-  const int slab = std::max(2, (Z + IO_SLABS - 1) / IO_SLABS);
-  const int nslabs = (Z + slab - 1) / slab;
+  const std::vector<HostSlab> plan = host_step_plan(g.l);
+  const int nslabs = (int)plan.size();
   int rc = io_setup(c, (size_t)nslabs + 6);
   if (rc) return rc;
   cudaEvent_t* ev = c->ev_io.data();  // [0] start, [1..nslabs] slabs, then p in, 4 fields out
   cudaEvent_t ev_p = ev[nslabs + 1];
-  const size_t plane = (size_t)(g.m + 2) * (g.n + 2), field = plane * Z;
+  const size_t plane = (size_t)(g.m + 2) * (g.n + 2), field = plane * g.Z;
   const int o = c->cur, nw = 1 - o;
   double* vel[3] = {c->U[o], c->V[o], c->W[o]};
   // the staging and the old fields may still be in use by earlier calls
   PF_CUDA(cudaEventRecord(ev[0], c->st));
   PF_CUDA(cudaStreamWaitEvent(c->st_io, ev[0], 0));
   for (int b = 0; b < nslabs; b++) {
-    const size_t k0 = (size_t)b * slab, nk = std::min<size_t>(slab, Z - k0);
+    const size_t k0 = plan[b].k0, nk = plan[b].k1 - plan[b].k0 + 1;
     for (int f = 0; f < 3; f++)
       PF_CUDA(cudaMemcpyAsync(c->iostage + f * field + k0 * plane, in[f] + k0 * plane, nk * plane * sizeof(double),
                               cudaMemcpyHostToDevice, c->st_io));
@@ -711,28 +741,20 @@ static int step_host_overlapped(pf_case* c, const double* const* in, double* con
   }
   PF_CUDA(cudaMemcpyAsync(c->stage, in[3], field * sizeof(double), cudaMemcpyHostToDevice, c->st_io));
   PF_CUDA(cudaEventRecord(ev_p, c->st_io));
-  // div_to / pred_to: the last plane done (the predictor starts at plane 2)
-  int div_to = 0, pred_to = 1;
   for (int b = 0; b < nslabs; b++) {
-    const int k0 = b * slab, k1 = std::min(k0 + slab, Z) - 1;
+    const HostSlab& h = plan[b];
     PF_CUDA(cudaStreamWaitEvent(c->st, ev[1 + b], 0));
-    for (int f = 0; f < 3; f++) launch_scatter_nat_planes(g, c->iostage + f * field, vel[f], k0, k1, c->st);
+    for (int f = 0; f < 3; f++) launch_scatter_nat_planes(g, c->iostage + f * field, vel[f], h.k0, h.k1, c->st);
     c->launches += 3;
-    // the divergence at k reads planes k-1 .. k+1; the predictor at k reads
-    // them and the divergence at k-1 .. k+1 (plane l: at l-1, l and 1)
-    const int d = std::min(k1 - 1, l);
-    if (d > div_to) {
-      launch_divergence<double>(g, s, vel[0], vel[1], vel[2], c->div, c->st, div_to + 1, d);
+    if (h.div_hi >= h.div_lo) {
+      launch_divergence<double>(g, s, vel[0], vel[1], vel[2], c->div, c->st, h.div_lo, h.div_hi);
       c->launches += 1;
-      div_to = d;
     }
-    const int pr = div_to == l ? l : div_to - 1;
-    if (pr > pred_to) {
+    if (h.pred_hi >= h.pred_lo) {
       launch_predictor<double, double>(g, s, vel[0], vel[1], vel[2], c->div, c->gx, c->gy, c->gz, c->rinv,
                                        c->damp, vel[0], vel[1], vel[2], c->U[nw], c->V[nw], c->W[nw], c->st,
-                                       pred_to + 1, pr);
+                                       h.pred_lo, h.pred_hi);
       c->launches += 1;
-      pred_to = pr;
     }
   }
   launch_predictor<double, double>(g, s, vel[0], vel[1], vel[2], c->div, c->gx, c->gy, c->gz, c->rinv, c->damp,
@@ -1045,6 +1067,18 @@ int pf_sweep_info(pf_case* c, int* fused, float* split_ms, float* fused_ms) {
   if (split_ms) *split_ms = c->sweep_ms[0];
   if (fused_ms) *fused_ms = c->sweep_ms[1];
   return PF_OK;
+}
+
+int pf_debug_step_host_plan(int l, int* slabs, int capacity) {
+  if (l < 3 || l > (1 << 20) || capacity < 0 || (capacity > 0 && !slabs))
+    return fail(PF_E_INVALID, "pf_debug_step_host_plan: bad argument");
+  const std::vector<HostSlab> plan = host_step_plan(l);
+  for (int b = 0; b < (int)plan.size() && b < capacity; b++) {
+    const HostSlab& h = plan[b];
+    const int v[6] = {h.k0, h.k1, h.div_lo, h.div_hi, h.pred_lo, h.pred_hi};
+    std::memcpy(slabs + 6 * b, v, sizeof v);
+  }
+  return (int)plan.size();
 }
 
 int pf_debug_fused_drop_stage(pf_case* c, int stage) {

@@ -146,3 +146,40 @@ def test_invalid_arguments_fail_before_any_device_work():
     assert L.pf_step(None, 1) == -1
     assert L.pf_step_host(None, None, None, None, None, None, None, None, None, 6, 6) == -1
     assert L.pf_strerror(-4) == b"non-finite values in the fields"
+
+
+def test_step_host_schedule_respects_every_dependency():
+    """pf_step_host's slab schedule, replayed on the CPU for every plane count
+    up to 300: each divergence plane k finds planes k-1 .. k+1 copied, each
+    predictor plane k finds them copied and the divergence of k-1 .. k+1 done
+    (plane l: l-1, l and 1; plane 1, issued last: l, 1 and 2), and every
+    interior plane is covered exactly once by each kernel."""
+    from pixelflow_gb300 import _lib
+    L = _lib.load()
+    for l in range(3, 301):
+        n = L.pf_debug_step_host_plan(l, None, 0)
+        assert 1 <= n <= 16
+        buf = (ctypes.c_int * (6 * n))()
+        assert L.pf_debug_step_host_plan(l, ctypes.cast(buf, ctypes.c_void_p), n) == n
+        copied, div, pred = set(), [], []
+        expect_k0 = 0
+        for b in range(n):
+            k0, k1, dlo, dhi, plo, phi = buf[6 * b: 6 * b + 6]
+            assert k0 == expect_k0 and k1 >= k0
+            expect_k0 = k1 + 1
+            copied |= set(range(k0, k1 + 1))
+            for k in range(dlo, dhi + 1):
+                assert {k - 1, k, k + 1} <= copied
+                div.append(k)
+            done = set(div)
+            for k in range(plo, phi + 1):
+                assert k != 1
+                assert {k - 1, k, k + 1} <= copied
+                assert {k - 1, k, 1 if k == l else k + 1} <= done
+                pred.append(k)
+        assert expect_k0 == l + 2  # the slabs tile the l+2 planes
+        pred.append(1)  # after the last slab
+        assert {l, 1, 2} <= set(div)
+        assert sorted(div) == list(range(1, l + 1))
+        assert sorted(pred) == list(range(1, l + 1))
+    assert L.pf_debug_step_host_plan(2, None, 0) == -1
