@@ -265,8 +265,8 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
 
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
-                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 300000,
-                  policy: str = "srpt"):
+                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 130000,
+                  policy: str = "srpt_fill"):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
     100-1000 steps each, admitted by a 150 GB HBM budget into one resident
@@ -284,7 +284,7 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
         res = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         summ = summarize(res, wall)
-        summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes)
+        summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes, policy=policy)
     # the plain FP64 single-case step on a sample of the same requests, one after another
     rng = np.random.default_rng(seed + 2)
     tot_cells, tot_ms = 0, 0.0
@@ -499,7 +499,8 @@ def run_ours(args):
                                              "sweep": msweep}}
         if not args.no_batch:
             line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
-            line["forms"]["serving"] = bench_serving(policy="srpt")
+            line["forms"]["serving"] = bench_serving(policy="srpt_fill")
+            line["forms"]["serving_srpt_equal_chunks"] = bench_serving(policy="srpt", baseline_sample=0)
             line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_sample=0)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)

@@ -18,14 +18,23 @@ Round policy: "rr" advances every active case each round; "srpt" advances
 the cases with the least remaining work (cells x steps left) first, adding
 cases in that order until a round holds at least `round_cells` cells, so the
 GPU stays full while short requests finish early (a lower p50 at the same
-throughput; the longest requests still finish last).
+throughput; the longest requests still finish last).  Both give every case
+of a round the same `chunk` steps, so a round lasts as long as its slowest
+case's chunk, and a cheap request with many steps needs many rounds.
+"srpt_fill" keeps the shortest-remaining-work order but gives each case the
+steps it runs alone in `round_ms` (a per-step cost model: a fixed launch
+latency plus a per-cell time, one rate for cases in the persistent kernel,
+one for full-GPU step graphs), and adds cases until the round's cell-steps
+reach what the GPU does in `round_ms` (`round_rate`); the case that does not
+fit whole gets the steps that fill the rest.  Cheap requests then
+finish in a round or two while the large ones fill the rest of the GPU.
 """
 from __future__ import annotations
 
 import dataclasses
 import time
 from collections import deque
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
@@ -52,11 +61,27 @@ class Result:
 
 
 class Server:
+    # per-step device time of a case running alone, in ms: launch latency plus
+    # cells x (ms per cell); measured on GB300 with clusters of 8 x 512 threads
+    # (persistent kernel: 0.4-1.2 ms per step for 2D cases whose rows fit in
+    # shared memory, up to ~125k cells; ~50 Mcell-steps/s for the others, which
+    # sweep from global memory; step graphs: 0.4-0.6 ms per 2D step, ~1.5 G
+    # cell-steps/s for large 3D cases)
+    STEP_MS = 0.35
+    ON_CHIP_CELLS = 125_000
+    ON_CHIP_MS_PER_CELL = 7.0e-6
+    CLUSTER_MS_PER_CELL = 2.0e-5
+    GRAPH_MS_PER_CELL = 0.67e-6
+
     def __init__(self, hbm_budget_bytes: int = 150 * GIB, chunk: int = 25, cluster: int = 4, threads: int = 512,
-                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 300000,
-                 policy: str = "rr", round_cells: int = 24_000_000, batch=None):
-        if policy not in ("rr", "srpt"):
+                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 130000,
+                 policy: str = "rr", round_cells: int = 24_000_000, batch=None, round_ms: float = 200.0,
+                 round_rate: float = 1.3e9):
+        if policy not in ("rr", "srpt", "srpt_fill"):
             raise ValueError(f"unknown policy {policy!r}")
+        self.large_cells = large_cells
+        self.round_ms = round_ms
+        self.round_work = round_rate * round_ms / 1e3  # cell-steps the GPU does in round_ms
         self.batch = batch if batch is not None else Batch(cluster=cluster, threads=threads, max_cases=max_cases,
                                                            hbm_budget_bytes=hbm_budget_bytes,
                                                            large_cells=large_cells)
@@ -113,8 +138,7 @@ class Server:
                 if incoming and realtime:
                     time.sleep(max(0.0, min(0.005, incoming[0].arrival_s - now())))
                 continue
-            slots = self._select(active)
-            steps = [min(self.chunk, active[s]["left"]) for s in slots]
+            slots, steps = self._plan(active)
             self.batch.step_slots(slots, steps)
             self.rounds += 1
             self.device_ms += self.batch.last_ms()
@@ -130,18 +154,43 @@ class Server:
                     del active[s]
         return sorted(results, key=lambda x: x.rid)
 
-    def _select(self, active: Dict[int, dict]) -> List[int]:
-        """The slots advanced this round (see the module docstring)."""
+    def _step_ms(self, cells: int, dim: int = 2) -> float:
+        """Modelled device time of one step of a case running alone."""
+        if cells > self.large_cells:
+            per_cell = self.GRAPH_MS_PER_CELL
+        elif dim == 2 and cells <= self.ON_CHIP_CELLS:
+            per_cell = self.ON_CHIP_MS_PER_CELL
+        else:
+            per_cell = self.CLUSTER_MS_PER_CELL
+        return self.STEP_MS + cells * per_cell
+
+    def _plan(self, active: Dict[int, dict]) -> Tuple[List[int], List[int]]:
+        """The slots advanced this round and their step counts (see the module
+        docstring)."""
         if self.policy == "rr":
-            return list(active)
+            slots = list(active)
+            return slots, [min(self.chunk, active[s]["left"]) for s in slots]
         order = sorted(active, key=lambda s: (active[s]["req"].cells * active[s]["left"], active[s]["req"].rid))
-        chosen, cells = [], 0
+        chosen, steps, cells, work = [], [], 0, 0
         for s in order:
-            chosen.append(s)
-            cells += active[s]["req"].cells
-            if cells >= self.round_cells:
+            a = active[s]
+            c = a["req"].cells
+            if self.policy == "srpt":
+                chosen.append(s)
+                steps.append(min(self.chunk, a["left"]))
+                cells += c
+                if cells >= self.round_cells:
+                    break
+                continue
+            k = min(a["left"], max(1, int(self.round_ms / self._step_ms(c, a["req"].dim))))
+            room = self.round_work - work
+            if chosen and room < c:  # the round is full
                 break
-        return chosen
+            k = min(k, max(1, int(room // c)))  # a case that does not fit whole fills the rest
+            chosen.append(s)
+            steps.append(k)
+            work += c * k
+        return chosen, steps
 
 
 def summarize(results: List[Result], wall_s: float) -> dict:

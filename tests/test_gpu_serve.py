@@ -31,12 +31,13 @@ def test_gpu_shapes_match_host_generator():
     ref.close()
 
 
-@pytest.mark.parametrize("policy", ["rr", "srpt"])
+@pytest.mark.parametrize("policy", ["rr", "srpt", "srpt_fill"])
 def test_served_results_equal_single_runs(policy):
     reqs = _small_requests()
-    # budget for ~2 of the requests at a time forces queueing and slot reuse
+    # budget for ~2 of the requests at a time forces queueing and slot reuse;
+    # srpt_fill's 2 ms rounds split every request over several rounds
     budget = int(2.2 * max(case_bytes(r.settings, r.shape) for r in reqs))
-    with Server(hbm_budget_bytes=budget, chunk=4, policy=policy, round_cells=20_000) as srv:
+    with Server(hbm_budget_bytes=budget, chunk=4, policy=policy, round_cells=20_000, round_ms=2.0) as srv:
         res = srv.run(reqs, realtime=True)
         assert srv.peak_bytes <= budget
     assert [r.rid for r in res] == [r.rid for r in reqs]
