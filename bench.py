@@ -211,7 +211,7 @@ def cpu_baseline(settings, shape, vals, budget_s: float = 20.0, max_steps: int =
 
 
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
-                baseline_sample: int = 6, baseline_steps: int = 3):
+                baseline_sample: int = 6, baseline_steps: int = 3, large_cells: int = 100000):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
     {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
     Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit),
@@ -225,7 +225,7 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
     from pixelflow_gb300.solver import Case
     cases = G.batch_cases_2d(ncases, seed=seed)
     t0 = time.perf_counter()
-    b = Batch(max_cases=ncases)
+    b = Batch(max_cases=ncases, large_cells=large_cells)
     slots = [b.add(c.settings, (c.m, c.n), c.porosity()) for c in cases]
     setup_s = time.perf_counter() - t0
     cells = sum(c.m * c.n for c in cases)
@@ -254,7 +254,8 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
         tot_cells += c.m * c.n * baseline_steps
         tot_ms += prof["step_ms"]
     plain = tot_cells / (tot_ms / 1e3) / 1e6
-    return {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25",
+    return {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25, "
+                        f"cases > {large_cells} cells as full-GPU step graphs beside the persistent kernel",
             "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
             "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
             "nonfinite_cases_after_timed_steps": nonfinite,
@@ -265,7 +266,7 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
 
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
-                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 130000,
+                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 100000,
                   policy: str = "srpt_fill"):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),

@@ -236,7 +236,7 @@ typedef struct pf_batch_options {
   uint64_t hbm_budget_bytes; /* admission limit for the cases' device memory */
   int32_t large_cells;       /* cases with more cells run full-GPU steps on their
                                 own stream, concurrently with the persistent
-                                kernel (default 300000) */
+                                kernel (default 100000) */
   int32_t reserved[7];
 } pf_batch_options;
 void pf_batch_default_options(pf_batch_options *opt); /* cluster 4, 512 threads, 1024 slots, 150 GiB */

@@ -25,7 +25,7 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
-def case_bytes(settings: Settings, shape: Sequence[int], large_cells: int = 300000) -> int:
+def case_bytes(settings: Settings, shape: Sequence[int], large_cells: int = 100000) -> int:
     """Device bytes one case of this shape takes in a batch: the allocation
     pf_batch_add makes (precision form; a case the persistent kernel steps,
     at most `large_cells` cells, uses the split FP32 sweep)."""
@@ -42,7 +42,7 @@ def case_bytes(settings: Settings, shape: Sequence[int], large_cells: int = 3000
 
 class Batch:
     def __init__(self, cluster: int = 4, threads: int = 512, max_cases: int = 1024,
-                 hbm_budget_bytes: int = 150 * GIB, global_passes: bool = False, large_cells: int = 300000):
+                 hbm_budget_bytes: int = 150 * GIB, global_passes: bool = False, large_cells: int = 100000):
         self.L = _lib.load()
         o = PfBatchOptions()
         self.L.pf_batch_default_options(ctypes.byref(o))

@@ -461,7 +461,13 @@ int pf_batch_create(const pf_batch_options* opt, pf_batch** out) {
   b->slots.assign(b->capacity, nullptr);
   b->pending.assign(b->capacity, 0);
   b->case_ev.assign(b->capacity, nullptr);
-  if (b->opt.large_cells <= 0) b->opt.large_cells = 300000;
+  // 2D cases beyond ~100k cells no longer keep their rows in the shared
+  // memory of a cluster and sweep from global memory (~50 M cell-steps/s on
+  // a few SMs); as full-GPU step graphs beside the persistent kernel they run
+  // faster and the batch with them (512 2D cases of 64..512 per side, 20
+  // steps on GB300: 1326 Mcell-steps/s with 300k, 1792 with 130k, 1906 with
+  // 100k, 1900 with 65k)
+  if (b->opt.large_cells <= 0) b->opt.large_cells = 100000;
   *out = b;
   return PF_OK;
 }

@@ -77,7 +77,7 @@ class Server:
     GRAPH_MS_PER_CELL = 0.67e-6
 
     def __init__(self, hbm_budget_bytes: int = 150 * GIB, chunk: int = 25, cluster: int = 4, threads: int = 512,
-                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 130000,
+                 max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 100000,
                  policy: str = "rr", round_cells: int = 24_000_000, batch=None, round_ms: float = 200.0,
                  round_rate: float = 2.6e9):
         if policy not in ("rr", "srpt", "srpt_fill"):
@@ -112,7 +112,7 @@ class Server:
         request is available at once (a closed batch)."""
         reqs = sorted(requests, key=lambda r: r.arrival_s)
         for r in reqs:
-            need = case_bytes(r.settings, r.shape)
+            need = case_bytes(r.settings, r.shape, self.large_cells)
             if need > self.batch.memory()[1]:
                 raise ValueError(f"request {r.rid} needs {need} bytes, more than the whole budget")
         t0 = time.perf_counter()

@@ -52,7 +52,7 @@ def _requests():
 @pytest.mark.parametrize("policy", ["rr", "srpt", "srpt_fill"])
 def test_every_request_gets_exactly_its_steps(policy, monkeypatch):
     import pixelflow_gb300.serve as S
-    monkeypatch.setattr(S, "case_bytes", lambda settings, shape: 1)
+    monkeypatch.setattr(S, "case_bytes", lambda *a, **k: 1)
     fb = FakeBatch()
     srv = Server(chunk=10, policy=policy, round_cells=300_000, batch=fb)
     res = srv.run(_requests(), realtime=False)
@@ -82,7 +82,7 @@ def test_srpt_finishes_short_requests_first(monkeypatch):
     completes the cheap requests earlier and lowers the mean completion time,
     for the same total work and the same completion time of the last request."""
     import pixelflow_gb300.serve as S
-    monkeypatch.setattr(S, "case_bytes", lambda settings, shape: 1)
+    monkeypatch.setattr(S, "case_bytes", lambda *a, **k: 1)
     reqs = _requests()
     finish, total = {}, {}
     for policy in ("rr", "srpt"):
@@ -113,7 +113,7 @@ def test_srpt_fill_finishes_cheap_requests_in_fewer_rounds(monkeypatch):
     which gives every case of a round the same chunk, and the last request
     no later than srpt does."""
     import pixelflow_gb300.serve as S
-    monkeypatch.setattr(S, "case_bytes", lambda settings, shape: 1)
+    monkeypatch.setattr(S, "case_bytes", lambda *a, **k: 1)
     s = Settings()
     sizes = [(192, 192), (288, 288), (1024, 1024), (192, 192, 192), (64, 64, 64), (320, 320), (160, 160, 160)]
     steps = [900, 350, 400, 500, 900, 750, 800]
