@@ -116,3 +116,24 @@ def test_step_host_staging_is_counted():
         c.step_host(state)
         field = (shape[0] + 2) * (shape[1] + 2) * (shape[2] + 2) * 8
         assert c.memory_bytes() == before + 3 * field
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_step_host_between_resident_steps(use_graph):
+    """Host steps and resident steps interleaved on one case (the two step
+    graphs of each buffer parity, the buffer swap) equal the three-call
+    sequence interleaved the same way."""
+    shape = (30, 22, 19)
+    s = G.settings_spheres_3d(iter_max=12)
+    vals = G.spheres_3d(*shape, count=3, seed=12)
+    with Case(s, shape, vals, use_graph=use_graph) as a, Case(s, shape, vals, use_graph=use_graph) as b:
+        state = _start_state(a, 1)
+        _start_state(b, 1)
+        for resident in (1, 2, 3):
+            ref = _three_calls(a, state)
+            got = b.step_host(state)
+            assert _same(got, ref)
+            a.step(resident)
+            b.step(resident)
+            state = a.get_state()
+            assert _same(b.get_state(), state)
