@@ -563,6 +563,8 @@ static int flags_fail(unsigned long long f) {
     return fail(PF_E_TIMEOUT, "fused correction sweep: a shared-memory staging wait expired");
   return fail(PF_E_CUDA, "unknown device error flag");
 }
+// Reads the device error word behind everything enqueued on the case's
+// stream, so it also waits for that work.
 static int check_flags(pf_case* c) {
   PF_CUDA(cudaMemcpyAsync(&c->hred[RED_FLAGS], &c->red[RED_FLAGS], sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost, c->st));
@@ -644,8 +646,7 @@ int pf_get_state(pf_case* c, double* u, double* v, double* w, double* p, int ld1
   }
   rc = check_launch("pf_get_state");
   if (rc) return rc;
-  PF_CUDA(cudaStreamSynchronize(c->st));
-  return check_flags(c);
+  return check_flags(c);  // waits for the copies too
 }
 
 // ---- one step from host state to host state ------------------------------
@@ -789,8 +790,7 @@ static int step_host_overlapped(pf_case* c, const double* const* in, double* con
   rc = check_launch("pf_step_host");
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st_io));
-  PF_CUDA(cudaStreamSynchronize(c->st));
-  return check_flags(c);
+  return check_flags(c);  // waits for the case's stream
 }
 
 int pf_step_host(pf_case* c, const double* u, const double* v, const double* w, const double* p, double* u_out,
@@ -946,7 +946,6 @@ int pf_step(pf_case* c, int nsteps) {
 
 int pf_synchronize(pf_case* c) {
   if (!c) return fail(PF_E_INVALID, "null handle");
-  PF_CUDA(cudaStreamSynchronize(c->st));
   return check_flags(c);
 }
 
