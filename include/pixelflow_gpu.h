@@ -281,7 +281,10 @@ int pf_batch_last_ms(pf_batch *b, double *ms);
  * rejected with PF_E_INVALID.  All calls share that array, so calls that
  * overlap on the GPU race and must be serialised by the caller.  The first
  * call on a device looks up the array's address (cudaGetSymbolAddress); make
- * it before any stream capture begins. */
+ * it before any stream capture begins.  That address is kept per device
+ * ordinal for the rest of the process: it belongs to the device's primary
+ * context, so call this only with the primary context current, and not after
+ * a cudaDeviceReset of that device. */
 #define PF_NOALLOC_MAX_ROWS 262144
 int pf_max_div_noalloc(const pf_params *prm, const double *u, const double *v, const double *w,
                        const double *porosity, int ld1, int ld2, double *max_div, void *stream);
@@ -299,7 +302,11 @@ int pf_sweep_info(pf_case *c, int *fused, float *split_ms, float *fused_ms);
  * is set; pf_synchronize, pf_get_state and pf_norms then return
  * PF_E_TIMEOUT for the rest of the case's life.  stage < 0 restores normal
  * operation of later steps (the error word stays).  PF_E_STATE when the case
- * does not run the fused sweep. */
+ * does not run the fused sweep.  After PF_E_TIMEOUT the case's fields are
+ * undefined: the sweeps that gave up stopped part way through a pass, so
+ * the correction and the pressure hold a mix of old and new values (no
+ * result is computed from a stage that never landed).  Restart the case
+ * from a saved state. */
 int pf_debug_fused_drop_stage(pf_case *c, int stage);
 
 /* The schedule pf_step_host follows for a 3D case with l planes (no device

@@ -959,12 +959,15 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS)
     float sE1 = 0.f, sE2 = 0.f, sP1 = 0.f, sP2 = 0.f;
     for (int it = 0; it < nit; it++) {
       const int k = k0 - 1 + it, kw = wrapz(k);
-      if (mbar_wait_bounded(&bar[waited % FSTAGES], (waited / FSTAGES) & 1))
+      // a thread whose wait ran out neither reads the stage that never landed
+      // nor stores a result from it; every thread leaves at the barrier below
+      const bool landed = mbar_wait_bounded(&bar[waited % FSTAGES], (waited / FSTAGES) & 1);
+      if (landed)
         confirmed = waited + 1;
       else
         abort_flag = 1;
       waited++;
-      if (red_item) {  // colour 0 of plane k
+      if (red_item && landed) {  // colour 0 of plane k
         const int s = (jw + kw) & 1;
         const float* E1c = sm + L.e1 + ((it + 1) % FZE) * plane1 + (rl + 1) * H + h0;  // row jw, plane k
         const float* E1p = sm + L.e1 + ((it + 2) % FZE) * plane1 + (rl + 1) * H + h0;  // plane k+1

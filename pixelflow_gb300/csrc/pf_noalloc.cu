@@ -19,7 +19,10 @@
 // streams, different host threads) race on it and must be serialised by the
 // caller.  The first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture begins.
+// that first call before any stream capture begins.  The cached address is
+// the array's address in the device's primary context: it stays valid for
+// the life of the process as long as the caller uses the primary context and
+// does not reset the device (cudaDeviceReset unloads the library's module).
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -6,7 +6,10 @@ measured as the vector field (u, v[, w]) and pressure on its own):
   * a few steps / single stages: 1e-12 -- the GPU reorders the floating point
     operations of each expression (reciprocal multiplies, FMAs), so it is not
     bit-identical, but every stage agrees to a few ulp;
-  * long runs: 1e-10 after 1000 steps (the parity bar for the plain FP64 step).
+  * long runs: 1e-10 after 1000 steps (the parity bar for the plain FP64 step),
+    asserted for u, v[, w] and p each on its own as well: the 2D cylinder for
+    its 1000 steps, the 3D geometry at 64^3 for 60 steps, and the benchmarked
+    256^3 case for the 25 steps the benchmark runs.
 """
 import ctypes
 import os
@@ -30,9 +33,18 @@ def fields(dim):
 
 
 def errors(got, ref, dim):
-    """{'vel': vector relative L2, 'p': pressure relative L2}"""
+    """{'vel': vector relative L2, 'p': pressure relative L2, 'fields': {f:
+    relative L2 of each field u, v[, w], p on its own}}"""
     r = ref if isinstance(ref, dict) else {f: getattr(ref, f) for f in fields(dim)}
-    return {"vel": rel_vel(got, r, dim), "p": rel_l2(got["p"], r["p"])}
+    return {"vel": rel_vel(got, r, dim), "p": rel_l2(got["p"], r["p"]),
+            "fields": {f: rel_l2(got[f], r[f]) for f in fields(dim)}}
+
+
+def assert_each_field(errs, bound):
+    """Every field within `bound` on its own: a small component (v, w beside
+    the inflow u) must not hide inside the vector norm."""
+    bad = {f: e for f, e in errs["fields"].items() if not e < bound}
+    assert not bad, (bound, errs)
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -124,6 +136,32 @@ def test_state_roundtrip_fortran_leading_dims():
 
 
 @pytest.mark.parametrize("dim", [2, 3])
+def test_padded_get_state_right_after_steps(dim):
+    """pf_get_state into padded (pageable, strided) arrays called straight
+    after steps are enqueued returns the finished step: the same bits as the
+    dense read of the same state."""
+    if dim == 2:
+        s, shape = G.settings_cylinder_2d(iter_max=40), (200, 96)
+        vals = G.cylinder_2d(*shape, radius=0.15, cx=0.6, cy=0.5)
+    else:
+        s, shape = G.settings_spheres_3d(iter_max=40), (64, 48, 40)
+        vals = G.spheres_3d(*shape, count=4, seed=3)
+    with Case(s, shape, vals) as c:
+        c.initial_conditions()
+        fs = c.field_shape
+        pad = fs[:-2] + (fs[-2] + 5, fs[-1] + 9)
+        for _ in range(2):
+            c.step(4)  # asynchronous: still running when get_state is called
+            out = {f: np.full(pad, np.nan) for f in fields(dim)}
+            c.get_state(out)
+            dense = c.get_state()
+            for f in fields(dim):
+                got = out[f][..., : fs[-2], : fs[-1]]
+                assert np.array_equal(got, dense[f]), f
+                assert np.isnan(out[f][..., fs[-2]:, :]).all() and np.isnan(out[f][..., :, fs[-1]:]).all()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
 def test_graph_replay_matches_eager_launches(dim):
     if dim == 2:
         s, shape = G.settings_cylinder_2d(iter_max=15), (48, 30)
@@ -204,6 +242,7 @@ def test_cylinder_512x256_1000_steps_parity():
     errs = errors(got, ref, 2)
     print("1000-step relative L2 vs oracle:", errs, "max|div|", max_div, ref.divergence_diag())
     assert errs["vel"] < 1e-10 and errs["p"] < 1e-10, errs
+    assert_each_field(errs, 1e-10)
 
 
 @pytest.mark.slow
@@ -222,6 +261,35 @@ def test_spheres_3d_reduced_parity():
     errs = errors(got, ref, 3)
     print("3D 64^3 60-step relative L2 vs oracle:", errs)
     assert errs["vel"] < 1e-10 and errs["p"] < 1e-10, errs
+    assert_each_field(errs, 1e-10)
+
+
+@pytest.mark.slow
+def test_spheres_3d_256_benchmark_case_parity():
+    """The benchmarked case itself -- 256^3, 32 seeded spheres, iter_max 100,
+    omega 1.7, nu 1e-3, dt 1e-4 -- for its first 25 steps (the steps the
+    benchmark warms up on and times), GPU against the oracle run on all host
+    cores: u, v, w and p each within 1e-10 relative L2, the reference's SOR
+    error within 1e-8 and max|div u| within 1e-8 relative."""
+    s = G.settings_spheres_3d()
+    shape = (256, 256, 256)
+    vals = G.spheres_3d(*shape)
+    steps = 25
+    with Case(s, shape, vals) as c:
+        c.initial_conditions()
+        c.step(steps)
+        got = c.get_state()
+        max_div, sor_err = c.norms()
+    ref = OracleCase(s, shape, vals)
+    ref.initialize()
+    e_ref = ref.step(steps)
+    errs = errors(got, ref, 3)
+    ref_div = ref.divergence_diag()
+    print("3D 256^3 25-step relative L2 vs oracle, per field:", errs["fields"], "max|div|", max_div, ref_div,
+          "sor error", sor_err, e_ref)
+    assert_each_field(errs, 1e-10)
+    assert abs(sor_err - e_ref) <= 1e-8 * abs(e_ref)
+    assert abs(max_div - ref_div) <= 1e-8 * ref_div
 
 
 @pytest.mark.parametrize("dim", [2, 3])

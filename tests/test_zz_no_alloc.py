@@ -22,8 +22,17 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).to("cuda:0")
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_noalloc_max_div_matches_pf_norms(dim):
+def _padded(a, ld1, ld2):
+    """The field in a caller's static array: leading dimensions ld1 >= m+2,
+    ld2 >= n+2 (Fortran a(0:md,0:nd[,0:l+1])), the padding filled with NaN
+    so that a read outside the case's extent would show in the result."""
+    out = np.full(a.shape[:-2] + (ld2, ld1), np.nan)
+    out[..., : a.shape[-2], : a.shape[-1]] = a
+    return out
+
+
+@pytest.mark.parametrize("dim,pad", [(2, (0, 0)), (3, (0, 0)), (2, (7, 3)), (3, (5, 4))])
+def test_noalloc_max_div_matches_pf_norms(dim, pad):
     import torch
     if dim == 2:
         s, shape = G.settings_cylinder_2d(iter_max=30), (96, 48)
@@ -32,26 +41,30 @@ def test_noalloc_max_div_matches_pf_norms(dim):
         s, shape = G.settings_spheres_3d(iter_max=20), (40, 32, 24)
         vals = G.spheres_3d(*shape, count=4, seed=7)
     L = _lib.load()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    side = torch.cuda.Stream()  # a caller's own stream, not the legacy default one
     with Case(s, shape, vals) as c:
         c.initial_conditions()
         results = []
-        for _ in range(2):  # two calls in a row, the state moving in between
+        for call in range(2):  # two calls in a row, the state moving in between
             c.step(3)
             want, _ = c.norms()
             st = c.get_state()
-            poro = c.porosity()
-            d = {k: _dev(a) for k, a in st.items()}
-            dp = _dev(poro)
+            ld1, ld2 = st["u"].shape[-1] + pad[0], st["u"].shape[-2] + pad[1]
+            d = {k: _dev(_padded(a, ld1, ld2)) for k, a in st.items()}
+            dp = _dev(_padded(c.porosity(), ld1, ld2))
             out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda:0")
-            torch.cuda.synchronize()
-            ptr = lambda t: ctypes.c_void_p(t.data_ptr())
             w = ptr(d["w"]) if dim == 3 else None
-            rc = L.pf_max_div_noalloc(ctypes.byref(c.params), ptr(d["u"]), ptr(d["v"]), w, ptr(dp),
-                                      st["u"].shape[-1], st["u"].shape[-2], ptr(out), None)
-            assert rc == 0, L.pf_last_error()
             torch.cuda.synchronize()
-            got = float(out.item())
-            results.append((got, want))
+            free0 = torch.cuda.mem_get_info()[0]
+            rc = L.pf_max_div_noalloc(ctypes.byref(c.params), ptr(d["u"]), ptr(d["v"]), w, ptr(dp),
+                                      ld1, ld2, ptr(out), ctypes.c_void_p(side.cuda_stream))
+            assert rc == 0, L.pf_last_error()
+            side.synchronize()
+            free1 = torch.cuda.mem_get_info()[0]
+            if call == 1:  # the first call on the device may load the library's kernels
+                assert free1 == free0, ("device memory in use changed across the call", free0, free1)
+            results.append((float(out.item()), want))
     for got, want in results:
         assert np.isfinite(got) and want > 0
         assert abs(got - want) <= 1e-12 * want, (got, want)
