@@ -210,106 +210,133 @@ def cpu_baseline(settings, shape, vals, budget_s: float = 20.0, max_steps: int =
                       f"({sum(times):.1f} s, oracle = C restatement of the reference OpenMP step, FP64)"}
 
 
+def _plain_sequential(items, steps: int):
+    """The plain FP64 single-case step on every given case, one case after
+    another: each case is created, stepped once (its step graph captured),
+    then `steps` graph replays are timed on the host clock (launches
+    included).  items: (settings, shape, porosity values or None, shapes)."""
+    from pixelflow_gb300.solver import Case
+    tot_cells, tot_s = 0, 0.0
+    for s, shape, vals, shapes in items:
+        s = s.replace(precision="fp64")
+        c = Case(s, shape, vals) if vals is not None else Case.from_shapes(s, shape, shapes)
+        with c:
+            c.initial_conditions()
+            c.step(1)
+            c.synchronize()
+            t0 = time.perf_counter()
+            c.step(steps)
+            c.synchronize()
+            tot_s += time.perf_counter() - t0
+        tot_cells += int(np.prod(shape)) * steps
+    return {"value": tot_cells / tot_s / 1e6, "unit": UNIT, "cases": len(items), "steps_each": steps,
+            "timing": "host clock around graph replays, one case after another"}
+
+
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
-                baseline_sample: int = 6, baseline_steps: int = 3, large_cells: int = 100000):
+                baseline_steps: int = 20, large_cells: int = 100000, plain_value: float = 0.0):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
     {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
-    Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit),
-    precision form (FP32 sweeps in FP64 defect correction, 4 x 25), advanced by
-    the persistent batch kernel.  Reports device-timed aggregate Mcell-steps/s
-    and, as the comparison, the plain FP64 single-case step run sequentially
-    on a sample of the same cases."""
+    Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit,
+    porosity threshold 0.1), precision form (FP32 sweeps in FP64 defect
+    correction, 4 x 25), advanced by the persistent batch kernel.  Reports
+    device-timed aggregate Mcell-steps/s over the cases that stay finite and,
+    as the comparison, the plain FP64 single-case step run on every case, one
+    after another."""
     from pixelflow_gb300 import geometry as G
     from pixelflow_gb300.autotune import tune_batch
     from pixelflow_gb300.batch import Batch
-    from pixelflow_gb300.solver import Case
     cases = G.batch_cases_2d(ncases, seed=seed)
     t0 = time.perf_counter()
     b = Batch(max_cases=ncases, large_cells=large_cells)
     slots = [b.add(c.settings, (c.m, c.n), c.porosity()) for c in cases]
     setup_s = time.perf_counter() - t0
-    cells = sum(c.m * c.n for c in cases)
     best, trials = tune_batch(b, slots, steps=warmup_steps, use_cache=False)
     l0 = b.kernel_launches()
     b.step_slots(slots, [steps] * len(slots))
     ms = b.last_ms()
     launches = b.kernel_launches() - l0
-    value = cells * steps / (ms / 1e3) / 1e6
     mem = b.memory()[0]
-    nonfinite = sum(1 for sl in slots if not np.isfinite(b.norms(sl)[0]))
+    finite = [bool(np.isfinite(b.norms(sl)[0])) for sl in slots]
     b.close()
-    # plain FP64 single-case step, one case after another, on a sample
-    rng = np.random.default_rng(seed + 1)
-    sample = rng.choice(len(cases), size=min(baseline_sample, len(cases)), replace=False)
-    tot_cells, tot_ms = 0, 0.0
-    for k in sample:
-        c = cases[int(k)]
-        with Case(c.settings.replace(precision="fp64"), (c.m, c.n), c.porosity()) as sc:
-            sc.initial_conditions()
-            sc.step(1)
-            sc.synchronize()
-            sc.profile_begin()
-            sc.step(baseline_steps)
-            prof = sc.profile_end()
-        tot_cells += c.m * c.n * baseline_steps
-        tot_ms += prof["step_ms"]
-    plain = tot_cells / (tot_ms / 1e3) / 1e6
-    return {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25, "
-                        f"cases > {large_cells} cells as full-GPU step graphs beside the persistent kernel",
-            "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
-            "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
-            "nonfinite_cases_after_timed_steps": nonfinite,
-            "autotune": {"best": list(best), "trials": trials},
-            "plain_fp64_sequential": {"value": plain, "unit": UNIT, "sample_cases": len(sample),
-                                      "steps_each": baseline_steps},
-            "speedup_vs_plain_fp64_sequential": value / plain}
+    cells = sum(c.m * c.n for c, ok in zip(cases, finite) if ok)
+    value = cells * steps / (ms / 1e3) / 1e6
+    plain = _plain_sequential([(c.settings, (c.m, c.n), c.porosity(), None) for c in cases], baseline_steps)
+    out = {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25, "
+                       f"cases > {large_cells} cells as full-GPU step graphs beside the persistent kernel",
+           "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
+           "value_counts": "cell-steps of the cases finite after the timed steps",
+           "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
+           "nonfinite_cases_after_timed_steps": len(finite) - sum(finite),
+           "autotune": {"best": list(best), "trials": trials},
+           "plain_fp64_sequential": plain,
+           "speedup_vs_plain_fp64_sequential": value / plain["value"]}
+    if plain_value:
+        out["speedup_vs_plain_fp64_256"] = value / plain_value
+    return out
 
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
-                  baseline_sample: int = 4, baseline_steps: int = 3, large_cells: int = 100000,
-                  policy: str = "srpt_fill"):
+                  baseline_steps: int = 20, large_cells: int = 100000, policy: str = "srpt_fill",
+                  plain_value: float = 0.0):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
     100-1000 steps each, admitted by a 150 GB HBM budget into one resident
-    batch and advanced `chunk` steps per round: cases up to `large_cells`
-    cells in the persistent launch, larger ones as full-GPU step graphs on
-    their own streams beside it.  Latency is wall-clock from arrival to the
-    result (fields and norms) on the host."""
+    batch: cases up to `large_cells` cells in the persistent launch, larger
+    ones as full-GPU step graphs on their own streams beside it.  Latency is
+    wall-clock from arrival to the result (fields and norms) on the host.
+    baseline_steps > 0 adds the plain FP64 step run on every request, one
+    after another, for that many steps each."""
     from pixelflow_gb300 import geometry as G
     from pixelflow_gb300.serve import Server, summarize
-    from pixelflow_gb300.solver import Case
     reqs = G.serving_requests(count=count, rate=rate, seed=seed)
     t0 = time.perf_counter()
-    with Server(chunk=chunk, cluster=8, threads=512, keep_state=True, large_cells=large_cells,
+    with Server(chunk=chunk, cluster=8, threads=512, keep_state=False, large_cells=large_cells,
                 policy=policy) as srv:
         res = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         summ = summarize(res, wall)
-        summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes, policy=policy)
-    # the plain FP64 single-case step on a sample of the same requests, one after another
-    rng = np.random.default_rng(seed + 2)
-    tot_cells, tot_ms = 0, 0.0
-    for k in rng.choice(len(reqs), size=min(baseline_sample, len(reqs)), replace=False):
-        r = reqs[int(k)]
-        with Case.from_shapes(r.settings.replace(precision="fp64"), r.shape, r.shapes) as c:
-            c.initial_conditions()
-            c.step(1)
-            c.synchronize()
-            c.profile_begin()
-            c.step(baseline_steps)
-            prof = c.profile_end()
-        tot_cells += r.cells * baseline_steps
-        tot_ms += prof["step_ms"]
+        summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes, policy=policy,
+                    max_waiting=srv.max_waiting)
     summ["workload"] = (f"{count} requests, Poisson {rate:g}/s, 70% 2D 128^2-1024^2 / 30% 3D 64^3-192^3, "
                         f"100-1000 steps, 150 GB budget, chunk {chunk}, large cases > {large_cells} cells "
                         f"on own streams, round policy {policy}")
-    if tot_ms > 0:
-        plain = tot_cells / (tot_ms / 1e3) / 1e6
-        summ["plain_fp64_sequential"] = {"value": plain, "unit": UNIT,
-                                         "sample_requests": int(min(baseline_sample, len(reqs))),
-                                         "steps_each": baseline_steps}
-        summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain
+    if baseline_steps:
+        plain = _plain_sequential([(r.settings, r.shape, None, r.shapes) for r in reqs], baseline_steps)
+        summ["plain_fp64_sequential"] = plain
+        summ["speedup_vs_plain_fp64_sequential"] = summ["mcell_steps_per_s"] / plain["value"]
+    if plain_value:
+        summ["speedup_vs_plain_fp64_256"] = summ["mcell_steps_per_s"] / plain_value
     return summ
+
+
+def bench_serving_rates(rates=(0.5, 1.0, 2.0), count: int = 32, seed: int = 0):
+    """The serving form at sustainable arrival rates: per rate, `count`
+    requests of the same mix; p50/p99 latency, the aggregate, the longest
+    queue, and the latency growth (mean latency of the last quarter of the
+    arrivals over the first quarter: about 1 while the queue stays bounded,
+    growing with the backlog beyond the GPU's capacity)."""
+    out = []
+    for r in rates:
+        from pixelflow_gb300 import geometry as G
+        from pixelflow_gb300.serve import Server, summarize
+        reqs = G.serving_requests(count=count, rate=r, seed=seed)
+        t0 = time.perf_counter()
+        with Server(chunk=25, cluster=8, threads=512, keep_state=False, policy="srpt_fill") as srv:
+            res = srv.run(reqs, realtime=True)
+            wall = time.perf_counter() - t0
+            summ = summarize(res, wall)
+            summ["max_waiting"] = srv.max_waiting
+        lat = [x.latency_s for x in sorted(res, key=lambda x: x.arrival_s)]
+        q = max(1, len(lat) // 4)
+        summ["latency_growth"] = float(np.mean(lat[-q:]) / max(np.mean(lat[:q]), 1e-9))
+        summ["rate_per_s"] = r
+        summ["offered_mcell_steps_per_s"] = sum(x.cells * x.steps for x in reqs) / max(reqs[-1].arrival_s, 1e-9) / 1e6
+        out.append(summ)
+    bounded = [x["rate_per_s"] for x in out if x["latency_growth"] < 2.0 and x["max_waiting"] <= 2]
+    return {"workload": f"{count} requests per rate, the serving mix, round policy srpt_fill",
+            "rates": out, "bounded_up_to_per_s": max(bounded) if bounded else None,
+            "bounded_rule": "latency growth < 2 and at most 2 requests waiting for admission"}
 
 
 def run_reference(args):
@@ -349,8 +376,7 @@ def run_batch_line(args):
     rank, world, local = dist_setup()
     from pixelflow_gb300 import _lib
     _lib.check(_lib.load().pf_set_device(local))
-    r = bench_batch(ncases=args.cases, steps=args.steps, warmup_steps=max(1, args.warmup // 2),
-                    baseline_sample=min(6, args.cases))
+    r = bench_batch(ncases=args.cases, steps=args.steps, warmup_steps=max(1, args.warmup // 2))
     line = {"metric": METRIC, "value": r["value"] * world, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
@@ -499,10 +525,12 @@ def run_ours(args):
                                              "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation",
                                              "sweep": msweep}}
         if not args.no_batch:
-            line["forms"]["batch2d_512"] = bench_batch(steps=args.steps)
-            line["forms"]["serving"] = bench_serving(policy="srpt_fill")
-            line["forms"]["serving_srpt_equal_chunks"] = bench_serving(policy="srpt", baseline_sample=0)
-            line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_sample=0)
+            line["forms"]["batch2d_512"] = bench_batch(steps=args.steps, plain_value=value)
+            line["forms"]["serving"] = bench_serving(policy="srpt_fill", plain_value=value)
+            line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_steps=0)
+            if args.serving_rates:
+                rates = tuple(float(x) for x in args.serving_rates.split(","))
+                line["forms"]["serving_rates"] = bench_serving_rates(rates, count=args.rate_requests)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)
     barrier(world)
@@ -524,6 +552,9 @@ def main():
     ap.add_argument("--forms", type=int, default=1, help="also measure the precision and batched forms")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--cases", type=int, default=512, help="batch2d workload: number of 2D cases")
+    ap.add_argument("--serving-rates", default="0.5,1,2",
+                    help="serving form at these arrival rates (requests/s); empty to skip")
+    ap.add_argument("--rate-requests", type=int, default=32, help="requests per arrival rate")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         raise SystemExit("--warmup must be >= 3")

@@ -85,10 +85,19 @@ typedef struct pf_options {
   int32_t fused_rows;      /* mixed, fused sweep: y rows per tile (0: auto) */
   int32_t fused_planes;    /* mixed, fused sweep: cap on the (tile, plane)
                               pairs of one CTA (0: one wave of CTAs) */
-  int32_t reserved[2];
+  int32_t sor_path;        /* plain FP64, 3D: PF_SOR_AUTO walks per-colour
+                              cell lists with the pure-fluid cells (porosity
+                              1 around them) first, whose six neighbours are
+                              summed exactly and whose coefficients are the
+                              one fluid constant; PF_SOR_CELLS updates every
+                              cell with its own six stored coefficients.  The
+                              same red-black iterates up to the rounding of
+                              the fluid cells' neighbour sum */
+  int32_t reserved[1];
 } pf_options;
 
 enum { PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1, PF_SWEEP_FUSED = 2 };
+enum { PF_SOR_AUTO = 0, PF_SOR_CELLS = 1 };
 
 typedef struct pf_case pf_case;
 
@@ -316,6 +325,18 @@ int pf_debug_fused_drop_stage(pf_case *c, int stage);
  * Plane 1 of the predictor runs after the last slab.  Writes up to
  * `capacity` slabs and returns the number of slabs. */
 int pf_debug_step_host_plan(int l, int *slabs, int capacity);
+
+/* The plain sweep's cell lists (no reference counterpart): *listed = 1 when
+ * the case's SOR walks cell lists (PF_SOR_AUTO, 3D plain FP64 without
+ * walls); fluid[c] / total[c] = the pure-fluid cells and all cells of
+ * colour c (either array may be NULL). */
+int pf_sor_info(pf_case *c, int *listed, int fluid[2], int total[2]);
+
+/* Testing of the exact six-term sum of the list sweep's fluid cells (no
+ * reference counterpart): out[i] = x[6i] + ... + x[6i+5] rounded once to
+ * FP64, ok[i] = 0 where an input is Inf/NaN or the sum is not a normal
+ * number (the sweep then adds in FP64).  Host arrays; allocates. */
+int pf_debug_sum6(const double *x, int n, double *out, int *ok);
 
 #ifdef __cplusplus
 }

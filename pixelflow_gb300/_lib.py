@@ -15,6 +15,7 @@ PF_OK = 0
 PF_PREC_FP64 = 0
 PF_PREC_MIXED = 1
 PF_SWEEP_AUTO, PF_SWEEP_SPLIT, PF_SWEEP_FUSED = 0, 1, 2
+PF_SOR_AUTO, PF_SOR_CELLS = 0, 1
 ERRORS = {
     -1: "PF_E_INVALID", -2: "PF_E_CUDA", -3: "PF_E_NOMEM", -4: "PF_E_NONFINITE",
     -5: "PF_E_TIMEOUT", -6: "PF_E_STATE", -7: "PF_E_BUSY",
@@ -40,7 +41,7 @@ class PfOptions(ctypes.Structure):
         ("precision", ctypes.c_int32), ("outer_max", ctypes.c_int32), ("inner_sweeps", ctypes.c_int32),
         ("track_sor_error", ctypes.c_int32), ("dc_tol", ctypes.c_double), ("use_graph", ctypes.c_int32),
         ("sweep_form", ctypes.c_int32), ("fused_rows", ctypes.c_int32), ("fused_planes", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("sor_path", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1),
     ]
 
 
@@ -109,6 +110,8 @@ _PROTOS = {
     "pf_debug_step_host_plan": (_I, [_I, _VP, _I]),
     "pf_sweep_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
+    "pf_sor_info": (_I, [_VP, ctypes.POINTER(_I), _VP, _VP]),
+    "pf_debug_sum6": (_I, [_VP, _I, _VP, _VP]),
     "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfBatchOptions), ctypes.POINTER(_VP)]),
     "pf_batch_destroy": (_I, [_VP]),

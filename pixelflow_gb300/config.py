@@ -31,7 +31,7 @@ GROUPS = {
 }
 GPU_GROUP = "gpu_control"
 GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls",
-            "sweep_form", "fused_rows", "fused_planes"]
+            "sweep_form", "fused_rows", "fused_planes", "sor_path"]
 WALL_FACES = ("top", "bottom", "east", "west", "north", "south")
 
 
@@ -76,6 +76,10 @@ class Settings:
     sweep_form: str = "auto"
     fused_rows: int = 0
     fused_planes: int = 0
+    # plain FP64, 3D: "auto" walks cell lists with the pure-fluid cells first
+    # (exact neighbour sum, no coefficient loads for them); "cells" updates
+    # every cell with its own stored coefficients
+    sor_path: str = "auto"
     # inflow and initial velocities scaled by porosity: the boundary and initial
     # conditions of ibm_2d_backstep_omp_cpu.f90 (:533-534, :615-618)
     inflow_porosity: bool = False

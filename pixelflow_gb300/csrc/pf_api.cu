@@ -260,6 +260,7 @@ static void case_free(pf_case* c) {
   if (c->iostage) cudaFree(c->iostage);
   if (c->st_io) cudaStreamDestroy(c->st_io);
   if (c->base) cudaFree(c->base);
+  if (c->list_base) cudaFree(c->list_base);
   mixed_free(c);
   if (c->hred) cudaFreeHost(c->hred);
   if (c->snap) cudaFree(c->snap);
@@ -299,7 +300,10 @@ static void enqueue_solve_p(pf_case* c, bool prof, bool head) {
       // the operator loads may precede the dependency wait unless the previous
       // kernel is the RHS, which writes bbn
       const bool early = it > 0 || col > 0 || halo;
-      launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, early, st);
+      if (c->use_list)
+        launch_sor_list(c, col, omw, err, early, st);
+      else
+        launch_sor_half<double>(g, c->C[col], c->p[col], c->p[1 - col], omw, col, err, nullptr, early, st);
     }
   }
   if (prof) cudaEventRecord(c->ev_cur[2], st);
@@ -439,6 +443,8 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "unknown sweep_form");
   if (rc == PF_OK && (c->opt.fused_rows < 0 || c->opt.fused_planes < 0))
     rc = fail(PF_E_INVALID, "fused_rows and fused_planes must be >= 0");
+  if (rc == PF_OK && c->opt.sor_path != PF_SOR_AUTO && c->opt.sor_path != PF_SOR_CELLS)
+    rc = fail(PF_E_INVALID, "unknown sor_path");
   if (rc != PF_OK) {
     delete c;
     return rc;
@@ -476,6 +482,11 @@ static int finish_setup(pf_case* c) {
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st));
   if (c->opt.precision == PF_PREC_MIXED) return mixed_choose_sweep(c);
+  if (c->opt.sor_path == PF_SOR_AUTO && sor_list_eligible(g)) {
+    rc = sor_list_setup(c);
+    if (rc) return rc;
+    c->use_list = true;
+  }
   return PF_OK;
 }
 
@@ -1095,7 +1106,17 @@ int pf_debug_fused_drop_stage(pf_case* c, int stage) {
 
 int pf_memory_bytes(pf_case* c, size_t* bytes) {
   if (!c || !bytes) return fail(PF_E_INVALID, "null argument");
-  *bytes = c->bytes + c->mixed_bytes + (c->iostage ? 3 * dense_bytes(c->g) : 0);
+  *bytes = c->bytes + c->mixed_bytes + c->list_bytes + (c->iostage ? 3 * dense_bytes(c->g) : 0);
+  return PF_OK;
+}
+
+int pf_sor_info(pf_case* c, int* listed, int fluid[2], int total[2]) {
+  if (!c || !listed) return fail(PF_E_INVALID, "null argument");
+  *listed = c->use_list ? 1 : 0;
+  for (int col = 0; col < 2; col++) {
+    if (fluid) fluid[col] = c->list_nfluid[col];
+    if (total) total[col] = c->list_ntotal[col];
+  }
   return PF_OK;
 }
 

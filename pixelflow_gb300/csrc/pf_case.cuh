@@ -50,6 +50,16 @@ struct pf_case {
   cudaStream_t st_io = nullptr;
   std::vector<cudaEvent_t> ev_io;
 
+  // ---- the plain 3D sweep driven by cell lists (pf_sor_list.cu) ----
+  // per colour: packed (h, j, k) of every cell, pure-fluid cells first
+  bool use_list = false;
+  unsigned* list_base = nullptr;
+  unsigned* list[2] = {nullptr, nullptr};
+  size_t list_bytes = 0;
+  int list_nfluid[2] = {0, 0}, list_ntotal[2] = {0, 0};
+  double list_const[6] = {0, 0, 0, 0, 0, 0};  // the fluid cells' normalised coefficients
+  bool list_iso = false;                        // all six equal (dx = dy = dz)
+
   // ---- mixed precision form (pf_mixed.cu) ----
   char* mbase = nullptr;
   size_t mixed_bytes = 0;
@@ -88,4 +98,9 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof);
 void enqueue_projection_mixed(pf_case* c);
 void enqueue_boundary_mixed(pf_case* c);
 int geometry_to_stage(pf_case* c, const pf_shape* shapes, int nshapes, double edge);
+// The list-driven plain sweep (3D, no walls, sizes that pack into 32 bits).
+bool sor_list_eligible(const Geo& g);
+int sor_list_setup(pf_case* c);
+void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool early,
+                     cudaStream_t st);
 }  // namespace pf

@@ -69,6 +69,30 @@ __device__ __forceinline__ void pdl_begin() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Launch with programmatic stream serialization (the kernel starts with
+// pdl_begin): the launch of the next kernel of the SOR loop overlaps the
+// tail of the current one; CUDA graph capture keeps these as programmatic
+// edges.
+template <typename... KArgs, typename... Args>
+void launch_pdl_smem(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  launch_pdl_smem(kernel, grid, block, 0, st, args...);
+}
+
 __device__ __forceinline__ int red_slot() {
   return (int)((blockIdx.x + 37u * blockIdx.y + 101u * blockIdx.z) & (RED_SLOTS - 1));
 }
@@ -144,6 +168,25 @@ __device__ __forceinline__ void block_max_atomic(unsigned v, unsigned long long*
   }
 }
 
+
+// The reference's ae..ab (ibm_3d:386-400) of a cell from its own and its six
+// neighbours' porosity (2D: the first four).
+__device__ __forceinline__ void coef_set(const Geo& g, const Scal& s, double e, double pe, double pw, double pn,
+                                         double ps, double pt, double pb, double a[6], double& ap) {
+  const double small = 1.e-6, dt = s.dt;
+  a[0] = dt * fmax(small, (pe + e) * 0.5) / s.dx / s.dx;
+  a[1] = dt * fmax(small, (e + pw) * 0.5) / s.dx / s.dx;
+  a[2] = dt * fmax(small, (pn + e) * 0.5) / s.dy / s.dy;
+  a[3] = dt * fmax(small, (e + ps) * 0.5) / s.dy / s.dy;
+  ap = -a[0] - a[1] - a[2] - a[3];
+  if (g.dim == 3) {
+    a[4] = dt * fmax(small, (pt + e) * 0.5) / s.dz / s.dz;
+    a[5] = dt * fmax(small, (e + pb) * 0.5) / s.dz / s.dz;
+    ap = ap - a[4] - a[5];
+  } else {
+    a[4] = a[5] = 0.0;
+  }
+}
 
 // Packed sweeps over a flat thread index: slot h = 0 .. m/2 of every
 // interior row, rows j fastest then planes k.  Warps are full across row

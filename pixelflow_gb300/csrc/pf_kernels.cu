@@ -29,30 +29,6 @@ namespace pf {
 
 namespace {
 
-// Launch with programmatic stream serialization (the kernel starts with
-// pdl_begin): the launch of the next kernel of the SOR loop overlaps the
-// tail of the current one; CUDA graph capture keeps these as programmatic
-// edges.
-template <typename... KArgs, typename... Args>
-void launch_pdl_smem(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                     Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-template <typename... KArgs, typename... Args>
-void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
-  launch_pdl_smem(kernel, grid, block, 0, st, args...);
-}
-
 inline dim3 grid_interior(const Geo& g) {
   return dim3((g.m + BX - 1) / BX, (g.n + BY - 1) / BY, g.dim == 3 ? g.l : 1);
 }
@@ -79,25 +55,6 @@ __global__ void k_porosity_factors(Geo g, Scal s, const double* __restrict__ po,
   if (g.dim == 3) gz[q] = (po[q + XY] - po[q - XY]) * s.hz;
   rinv[q] = s.dt / e;
   damp[q] = s.nonslip ? s.xnue * s.dt * 32.0 * e * (1.0 - e) * (1.0 - e) / (s.thickness * s.thickness) : 0.0;
-}
-
-// The reference's ae..ab (ibm_3d:386-400) of a cell from its own and its six
-// neighbours' porosity (2D: the first four).
-__device__ __forceinline__ void coef_set(const Geo& g, const Scal& s, double e, double pe, double pw, double pn,
-                                         double ps, double pt, double pb, double a[6], double& ap) {
-  const double small = 1.e-6, dt = s.dt;
-  a[0] = dt * fmax(small, (pe + e) * 0.5) / s.dx / s.dx;
-  a[1] = dt * fmax(small, (e + pw) * 0.5) / s.dx / s.dx;
-  a[2] = dt * fmax(small, (pn + e) * 0.5) / s.dy / s.dy;
-  a[3] = dt * fmax(small, (e + ps) * 0.5) / s.dy / s.dy;
-  ap = -a[0] - a[1] - a[2] - a[3];
-  if (g.dim == 3) {
-    a[4] = dt * fmax(small, (pt + e) * 0.5) / s.dz / s.dz;
-    a[5] = dt * fmax(small, (e + pb) * 0.5) / s.dz / s.dz;
-    ap = ap - a[4] - a[5];
-  } else {
-    a[4] = a[5] = 0.0;
-  }
 }
 
 // boundary_matrix of the air-condition program (ibm_3d_air_condition_omp_cpu.f90:

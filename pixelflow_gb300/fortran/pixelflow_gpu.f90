@@ -28,7 +28,8 @@ module pixelflow_gpu
     integer(c_int32_t) :: sweep_form
     integer(c_int32_t) :: fused_rows
     integer(c_int32_t) :: fused_planes
-    integer(c_int32_t) :: reserved(2)
+    integer(c_int32_t) :: sor_path
+    integer(c_int32_t) :: reserved(1)
   end type pf_options
 
   interface

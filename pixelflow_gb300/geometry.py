@@ -20,7 +20,7 @@ All random draws use ``numpy.random.default_rng(seed)``.
 from __future__ import annotations
 
 import dataclasses
-from typing import List, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -162,13 +162,27 @@ class BatchCase2D:
 
 def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
                    sizes: Sequence[int] = tuple(range(64, 513, 32)),
-                   iter_max: int = 100) -> List[BatchCase2D]:
+                   iter_max: int = 100, threshold: float = 0.1, cell_re: Optional[float] = 2.0,
+                   dt_rule: str = "stable") -> List[BatchCase2D]:
     """Independent 2D cases of uneven size: nx, ny from `sizes`, 1-4 circles or
     ellipses with semi-axes 0.02-0.1 of the height at random angles, Re uniform
     in [50, 400] (nu = U*D/Re with D twice the first obstacle's larger
-    semi-axis, raised to cell Reynolds number <= 2 by `grid_nu`), unit
-    inflow, dt from CFL 0.2 of the full stability limit (`cfl_dt`), square
-    cells."""
+    semi-axis), unit inflow, square cells.
+
+    Stability of the reference scheme sets three choices (each checked with
+    the FP64 oracle over 500 steps):
+    * `threshold`, the namelist porosity floor (&porosity_control; the
+      template's 1e-6): with 1e-6 a third of the cases overflow within 40
+      steps, from the first step on -- the pressure solve leaves large
+      gradients inside the solid cores, where the non-slip damping
+      eps(1-eps)^2 vanishes, and the advection term then squares the velocity
+      there every step.  0.1 keeps every case finite;
+    * `cell_re`: nu is raised where needed to cell Reynolds number
+      U*h/nu <= cell_re (`grid_nu`); None keeps nu = U*D/Re, under which half
+      of the cases still diverge with threshold 0.1;
+    * `dt_rule`: "stable" takes CFL 0.2 of the predictor's full stability
+      limit (`cfl_dt`); "cfl" the plain advective 0.2*h/U, which diverges
+      for most cases."""
     rng = np.random.default_rng(seed)
     cases = []
     for _ in range(count):
@@ -190,11 +204,13 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
         re = float(rng.uniform(50.0, 400.0))
         d_ref = 2.0 * max(shapes[0][2], shapes[0][3])
         u_in = 1.0
-        nu = grid_nu(u_in * d_ref / re, h, u_in)
-        dt = cfl_dt(h, nu, u_in, 2)
+        nu = u_in * d_ref / re
+        if cell_re is not None:
+            nu = grid_nu(nu, h, u_in, cell_re)
+        dt = cfl_dt(h, nu, u_in, 2) if dt_rule == "stable" else 0.2 * h / u_in
         s = Settings(xnue=nu, xlambda=0.0, density=1.0, width=width, height=height, depth=0.0,
                      time=dt * steps, inlet_velocity=u_in, outlet_pressure=0.0, aoa=0.0,
-                     istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6,
+                     istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=threshold,
                      radius=d_ref / 2, nonslip=True, iter_max=iter_max, relux_factor=1.7,
                      precision="mixed")
         cases.append(BatchCase2D(m, n, s, shapes))
@@ -242,13 +258,14 @@ class Request:
 def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2d: float = 0.7,
                      sizes_2d: Sequence[int] = tuple(range(128, 1025, 32)),
                      sizes_3d: Sequence[int] = (64, 96, 128, 160, 192),
-                     steps_range: Tuple[int, int] = (100, 1000)) -> List[Request]:
+                     steps_range: Tuple[int, int] = (100, 1000), threshold: float = 0.1) -> List[Request]:
     """Poisson arrivals (exponential gaps, mean 1/rate) of mixed cases.
     2D: n x n unit squares, 1-4 circles/ellipses (semi-axes 0.02-0.1),
     Re 50-400 on the first obstacle's diameter.  3D: n^3 unit cubes, 4-16
     spheres (radii 0.03-0.08, centres in [0.15, 0.85]^3), nu 2e-3..1e-2.
     Unit inflow; nu raised to cell Reynolds number <= 2 (`grid_nu`); dt at
-    CFL 0.2 of the full stability limit (`cfl_dt`).
+    CFL 0.2 of the full stability limit (`cfl_dt`); porosity threshold 0.1
+    (see `batch_cases_2d` for these three choices).
     Steps per request uniform in steps_range."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -270,7 +287,7 @@ def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2
             nu = grid_nu(2.0 * max(shapes[0][2], shapes[0][3]) / re, h)
             dt = cfl_dt(h, nu, 1.0, 2)
             s = Settings(xnue=nu, width=1.0, height=1.0, depth=0.0, time=dt * steps, inlet_velocity=1.0,
-                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
+                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=threshold, nonslip=True,
                          iter_max=100, relux_factor=1.7, precision="mixed")
             out.append(Request(rid, t, 2, (n, n), s, shapes, steps))
         else:
@@ -281,7 +298,7 @@ def serving_requests(count: int = 64, rate: float = 200.0, seed: int = 0, frac_2
             nu = grid_nu(float(rng.uniform(2e-3, 1e-2)), h)
             dt = cfl_dt(h, nu, 1.0, 3)
             s = Settings(xnue=nu, width=1.0, height=1.0, depth=1.0, time=dt * steps, inlet_velocity=1.0,
-                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=1e-6, nonslip=True,
+                         istep_max=steps, istep_out=10 ** 9, thickness=2.0, threshold=threshold, nonslip=True,
                          iter_max=100, relux_factor=1.7, precision="mixed")
             out.append(Request(rid, t, 3, (n, n, n), s, [tuple(r) for r in sph], steps))
     return out

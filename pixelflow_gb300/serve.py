@@ -94,6 +94,7 @@ class Server:
         self.keep_state = keep_state
         self.edge = edge
         self.peak_bytes = 0
+        self.max_waiting = 0  # longest queue of arrived requests not yet admitted
         self.rounds = 0
         self.device_ms = 0.0
 
@@ -125,6 +126,7 @@ class Server:
             t = now()
             while incoming and (not realtime or incoming[0].arrival_s <= t):
                 waiting.append(incoming.popleft())
+            self.max_waiting = max(self.max_waiting, len(waiting))
             # admission in arrival order while memory and slots allow
             while waiting:
                 r = waiting[0]

@@ -24,6 +24,7 @@ from ._lib import PfOptions, PfParams, check
 
 PRECISIONS = {"fp64": _lib.PF_PREC_FP64, "plain": _lib.PF_PREC_FP64, "mixed": _lib.PF_PREC_MIXED}
 SWEEP_FORMS = {"auto": _lib.PF_SWEEP_AUTO, "split": _lib.PF_SWEEP_SPLIT, "fused": _lib.PF_SWEEP_FUSED}
+SOR_PATHS = {"auto": _lib.PF_SOR_AUTO, "cells": _lib.PF_SOR_CELLS}
 
 
 def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
@@ -56,6 +57,10 @@ def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
     o.sweep_form = SWEEP_FORMS[form]
     o.fused_rows = int(s.fused_rows)
     o.fused_planes = int(s.fused_planes)
+    path = str(s.sor_path).lower()
+    if path not in SOR_PATHS:
+        raise ValueError(f"unknown sor_path {s.sor_path!r}")
+    o.sor_path = SOR_PATHS[path]
     return o
 
 
@@ -294,6 +299,16 @@ class Case:
         f, a, b = ctypes.c_int(), ctypes.c_float(), ctypes.c_float()
         check(self.L.pf_sweep_info(self.h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)))
         return {"form": "fused" if f.value else "split", "split_ms": a.value, "fused_ms": b.value}
+
+    def sor_info(self) -> Dict[str, object]:
+        """The plain sweep's path: {"listed": bool, "fluid": [c0, c1],
+        "total": [c0, c1]} -- listed when the SOR walks cell lists with the
+        pure-fluid cells first (3D plain FP64, sor_path "auto")."""
+        li = ctypes.c_int()
+        fl = (ctypes.c_int * 2)()
+        tot = (ctypes.c_int * 2)()
+        check(self.L.pf_sor_info(self.h, ctypes.byref(li), fl, tot))
+        return {"listed": bool(li.value), "fluid": list(fl), "total": list(tot)}
 
     def memory_bytes(self) -> int:
         b = ctypes.c_size_t()
