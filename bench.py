@@ -234,7 +234,8 @@ def _plain_sequential(items, steps: int):
 
 
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
-                baseline_steps: int = 20, large_cells: int = 100000, plain_value: float = 0.0):
+                baseline_steps: int = 20, large_cells: int = 100000, plain_value: float = 0.0,
+                schedule_bound: float = 1e-5):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
     {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
     Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit,
@@ -244,12 +245,14 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
     as the comparison, the plain FP64 single-case step run on every case, one
     after another."""
     from pixelflow_gb300 import geometry as G
-    from pixelflow_gb300.autotune import tune_batch
+    from pixelflow_gb300.autotune import tune_batch, tune_batch_schedule
     from pixelflow_gb300.batch import Batch
     cases = G.batch_cases_2d(ncases, seed=seed)
+    sched, sched_trials = tune_batch_schedule(cases, bound=schedule_bound, use_cache=False)
     t0 = time.perf_counter()
     b = Batch(max_cases=ncases, large_cells=large_cells)
-    slots = [b.add(c.settings, (c.m, c.n), c.porosity()) for c in cases]
+    slots = [b.add(c.settings.replace(outer_max=sched[0], inner_sweeps=sched[1]), (c.m, c.n), c.porosity())
+             for c in cases]
     setup_s = time.perf_counter() - t0
     best, trials = tune_batch(b, slots, steps=warmup_steps, use_cache=False)
     l0 = b.kernel_launches()
@@ -257,18 +260,22 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
     ms = b.last_ms()
     launches = b.kernel_launches() - l0
     mem = b.memory()[0]
+    graph_stats = dict(zip(("captured", "replays"), b.graph_stats()))
     finite = [bool(np.isfinite(b.norms(sl)[0])) for sl in slots]
     b.close()
     cells = sum(c.m * c.n for c, ok in zip(cases, finite) if ok)
     value = cells * steps / (ms / 1e3) / 1e6
     plain = _plain_sequential([(c.settings, (c.m, c.n), c.porosity(), None) for c in cases], baseline_steps)
-    out = {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed 4x25, "
+    out = {"workload": f"{ncases} 2D ibm2 cases, nx,ny in 64..512 step 32, seed {seed}, mixed "
+                       f"{sched[0]}x{sched[1]} (autotuned within {schedule_bound:g} relative L2 of FP64), "
                        f"cases > {large_cells} cells as full-GPU step graphs beside the persistent kernel",
            "cells": cells, "value": value, "unit": UNIT, "steps": steps, "ms": ms,
            "value_counts": "cell-steps of the cases finite after the timed steps",
            "launches_in_timed_region": launches, "setup_s": setup_s, "device_bytes": mem,
            "nonfinite_cases_after_timed_steps": len(finite) - sum(finite),
-           "autotune": {"best": list(best), "trials": trials},
+           "autotune": {"best": list(best), "trials": trials, "schedule": list(sched),
+                        "schedule_bound": schedule_bound, "schedule_trials": sched_trials},
+           "graph_stats": graph_stats,
            "plain_fp64_sequential": plain,
            "speedup_vs_plain_fp64_sequential": value / plain["value"]}
     if plain_value:
@@ -499,8 +506,14 @@ def run_ours(args):
     line["clocks"] = clocks
     case.close()
     if args.forms and args.precision == "fp64" and args.workload.startswith("spheres3d"):
-        # the precision form on the same case, and the batched form (2D batch)
-        mc = Case(s.replace(precision="mixed"), shape, vals)
+        # the precision form on the same case (config 3's 4 x 25 schedule; the
+        # FP32 sweep's form and tile from the autotuner, which also reports
+        # the schedules' speed and error), and the batched form (2D batch)
+        from pixelflow_gb300.autotune import tune_fused, tune_schedule
+        ms_ = s.replace(precision="mixed")
+        tile, tile_trials = tune_fused(ms_, shape, vals, use_cache=False)
+        sched, sched_trials = tune_schedule(ms_, shape, vals, bound=args.schedule_bound, use_cache=False)
+        mc = Case(ms_.replace(**tile), shape, vals)
         mc.initial_conditions()
         mc.step(args.warmup)
         mc.synchronize()
@@ -523,9 +536,14 @@ def run_ours(args):
                                              "speedup_vs_plain_fp64": mval / value,
                                              "rel_l2_vs_fp64": err, "after_steps": args.warmup + args.steps,
                                              "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation",
-                                             "sweep": msweep}}
+                                             "sweep": msweep,
+                                             "autotune": {"tile": tile, "tile_trials": tile_trials,
+                                                          "schedule_bound": args.schedule_bound,
+                                                          "schedule_pick": list(sched),
+                                                          "schedule_trials": sched_trials}}}
         if not args.no_batch:
-            line["forms"]["batch2d_512"] = bench_batch(steps=args.steps, plain_value=value)
+            line["forms"]["batch2d_512"] = bench_batch(steps=args.steps, plain_value=value,
+                                                       schedule_bound=args.schedule_bound)
             line["forms"]["serving"] = bench_serving(policy="srpt_fill", plain_value=value)
             line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_steps=0)
             if args.serving_rates:
@@ -555,6 +573,9 @@ def main():
     ap.add_argument("--serving-rates", default="0.5,1,2",
                     help="serving form at these arrival rates (requests/s); empty to skip")
     ap.add_argument("--rate-requests", type=int, default=32, help="requests per arrival rate")
+    ap.add_argument("--schedule-bound", type=float, default=1e-5,
+                    help="precision form: the autotuner's bound on the relative L2 error against FP64 when it "
+                         "picks the outer x inner schedule")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         raise SystemExit("--warmup must be >= 3")

@@ -246,7 +246,14 @@ typedef struct pf_batch_options {
   int32_t large_cells;       /* cases with more cells run full-GPU steps on their
                                 own stream, concurrently with the persistent
                                 kernel (default 100000) */
-  int32_t reserved[7];
+  int32_t use_graph;         /* 1 (default): the descriptor upload and the
+                                persistent launches of a call run as a CUDA
+                                graph, captured once per composition (cases
+                                per dimension, shared memory, launch shape)
+                                and replayed by later calls of the same
+                                composition; the large cases replay their own
+                                step graphs.  0: plain launches */
+  int32_t reserved[6];
 } pf_batch_options;
 void pf_batch_default_options(pf_batch_options *opt); /* cluster 4, 512 threads, 1024 slots, 150 GiB */
 int pf_batch_create(const pf_batch_options *opt, pf_batch **out);
@@ -274,6 +281,9 @@ int pf_batch_kernel_launches(pf_batch *b, int64_t *n);
 int pf_batch_configure(pf_batch *b, int cluster, int threads);
 /* Device time (CUDA events on the batch stream) of the last step call. */
 int pf_batch_last_ms(pf_batch *b, double *ms);
+/* Graphs of the persistent launch captured so far, and calls that replayed
+ * one without capturing. */
+int pf_batch_graph_stats(pf_batch *b, int64_t *captured, int64_t *replays);
 
 /* max|div u| without allocating device memory.  No counterpart in the
  * reference: it exists for callers that must not call cudaMalloc at this

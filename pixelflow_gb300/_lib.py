@@ -59,7 +59,7 @@ class PfBatchOptions(ctypes.Structure):
     _fields_ = [
         ("cluster", ctypes.c_int32), ("threads", ctypes.c_int32), ("max_cases", ctypes.c_int32),
         ("global_passes", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("large_cells", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -129,6 +129,7 @@ _PROTOS = {
     "pf_batch_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_batch_configure": (_I, [_VP, _I, _I]),
     "pf_batch_last_ms": (_I, [_VP, ctypes.POINTER(_D)]),
+    "pf_batch_graph_stats": (_I, [_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
 }
 
 

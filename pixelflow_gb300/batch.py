@@ -42,13 +42,15 @@ def case_bytes(settings: Settings, shape: Sequence[int], large_cells: int = 1000
 
 class Batch:
     def __init__(self, cluster: int = 4, threads: int = 512, max_cases: int = 1024,
-                 hbm_budget_bytes: int = 150 * GIB, global_passes: bool = False, large_cells: int = 100000):
+                 hbm_budget_bytes: int = 150 * GIB, global_passes: bool = False, large_cells: int = 100000,
+                 use_graph: bool = True):
         self.L = _lib.load()
         o = PfBatchOptions()
         self.L.pf_batch_default_options(ctypes.byref(o))
         o.cluster, o.threads, o.max_cases, o.hbm_budget_bytes = cluster, threads, max_cases, int(hbm_budget_bytes)
         o.global_passes = 1 if global_passes else 0
         o.large_cells = int(large_cells)
+        o.use_graph = 1 if use_graph else 0
         h = ctypes.c_void_p()
         check(self.L.pf_batch_create(ctypes.byref(o), ctypes.byref(h)))
         self.h = h
@@ -149,6 +151,12 @@ class Batch:
         ms = ctypes.c_double()
         check(self.L.pf_batch_last_ms(self.h, ctypes.byref(ms)))
         return ms.value
+
+    def graph_stats(self) -> Tuple[int, int]:
+        """(graphs of the persistent launch captured, calls that replayed one)."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(self.L.pf_batch_graph_stats(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def kernel_launches(self) -> int:
         n = ctypes.c_int64()

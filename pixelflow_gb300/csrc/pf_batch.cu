@@ -370,13 +370,24 @@ struct pf_batch {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   double last_ms = 0.0;  // device time of the last pf_batch_step_slots
   std::vector<cudaEvent_t> case_ev;  // per slot: completion of a large case's steps
+  // The persistent part of a call (descriptor upload + one launch per
+  // dimension) as a CUDA graph: the descriptors are staged in pinned host
+  // memory, which the graph's copy nodes read when it runs, so a graph fits
+  // every call with the same composition (key) and is captured again when
+  // the composition changes.
+  CaseDesc* h_desc = nullptr;
+  int* h_order = nullptr;
+  int* h_misc = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  long long gkey[6] = {-1, -1, -1, -1, -1, -1};  // n2, n3, smem2, cluster, threads, grid clusters
+  int64_t graphs_captured = 0, graph_replays = 0;
 };
 
-static int batch_fail(int code, const std::string& m) { return fail(code, m); }
-
+// Launch shape of one dimension's persistent kernel: the function attributes
+// (shared memory, non-portable cluster size) and the number of co-resident
+// clusters.  Not a stream operation, so it runs before any capture.
 template <int DIM, int BT>
-static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, size_t smem, const int* order, const int* ncases,
-                               int* head) {
+static int prepare_batch_kernel(int cluster, size_t smem, int ncl, int* nclusters) {
   cudaError_t e = cudaFuncSetAttribute(k_batch<DIM, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(smem)");
   if (cluster > 8) {
@@ -386,7 +397,6 @@ static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, size_t smem, c
   cudaLaunchConfig_t cfg = {};
   cfg.blockDim = dim3(BT);
   cfg.dynamicSmemBytes = smem;
-  cfg.stream = b->st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cluster;
@@ -398,21 +408,58 @@ static int launch_batch_kernel(pf_batch* b, int ncl, int cluster, size_t smem, c
   int maxc = 0;
   e = cudaOccupancyMaxActiveClusters(&maxc, (void*)k_batch<DIM, BT>, &cfg);
   if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters");
-  if (maxc < 1) return batch_fail(PF_E_INVALID, "batch: cluster configuration cannot be scheduled");
-  const int nclusters = std::max(1, std::min(maxc, ncl));
+  if (maxc < 1) return fail(PF_E_INVALID, "batch: cluster configuration cannot be scheduled");
+  *nclusters = std::max(1, std::min(maxc, ncl));
+  return PF_OK;
+}
+
+template <int DIM, int BT>
+static int launch_batch_kernel(pf_batch* b, int nclusters, int cluster, size_t smem, const int* order,
+                               const int* ncases, int* head) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(BT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = b->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   cfg.gridDim = dim3(nclusters * cluster);
-  e = cudaLaunchKernelEx(&cfg, k_batch<DIM, BT>, (const CaseDesc*)b->d_desc, order, ncases, head);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch<DIM, BT>, (const CaseDesc*)b->d_desc, order, ncases, head);
   if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelEx(k_batch)");
-  b->launches += 1;
   return PF_OK;
 }
 
 template <int DIM>
-static int launch_dim(pf_batch* b, int ncl, size_t smem, const int* order, const int* ncases, int* head) {
+static int prepare_dim(pf_batch* b, size_t smem, int ncl, int* nclusters) {
   const int c = b->opt.cluster;
-  if (b->opt.threads == 256) return launch_batch_kernel<DIM, 256>(b, ncl, c, smem, order, ncases, head);
-  if (b->opt.threads == 512) return launch_batch_kernel<DIM, 512>(b, ncl, c, smem, order, ncases, head);
-  return launch_batch_kernel<DIM, 1024>(b, ncl, c, smem, order, ncases, head);
+  if (b->opt.threads == 256) return prepare_batch_kernel<DIM, 256>(c, smem, ncl, nclusters);
+  if (b->opt.threads == 512) return prepare_batch_kernel<DIM, 512>(c, smem, ncl, nclusters);
+  return prepare_batch_kernel<DIM, 1024>(c, smem, ncl, nclusters);
+}
+
+template <int DIM>
+static int launch_dim(pf_batch* b, int nclusters, size_t smem, const int* order, const int* ncases, int* head) {
+  const int c = b->opt.cluster;
+  if (b->opt.threads == 256) return launch_batch_kernel<DIM, 256>(b, nclusters, c, smem, order, ncases, head);
+  if (b->opt.threads == 512) return launch_batch_kernel<DIM, 512>(b, nclusters, c, smem, order, ncases, head);
+  return launch_batch_kernel<DIM, 1024>(b, nclusters, c, smem, order, ncases, head);
+}
+
+// The persistent part of a call, enqueued on the batch stream: the
+// descriptor upload from the pinned staging and one launch per dimension.
+static int enqueue_persistent(pf_batch* b, int n2, int n3, size_t smem2, int ncl2, int ncl3) {
+  const int n = n2 + n3;
+  PF_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc, sizeof(CaseDesc) * n, cudaMemcpyHostToDevice, b->st));
+  PF_CUDA(cudaMemcpyAsync(b->d_order, b->h_order, sizeof(int) * n, cudaMemcpyHostToDevice, b->st));
+  PF_CUDA(cudaMemcpyAsync(b->d_misc, b->h_misc, sizeof(int) * 8, cudaMemcpyHostToDevice, b->st));
+  int rc = PF_OK;
+  if (n2) rc = launch_dim<2>(b, ncl2, smem2, b->d_order, b->d_misc + 0, b->d_misc + 1);
+  if (rc == PF_OK && n3) rc = launch_dim<3>(b, ncl3, 0, b->d_order + n2, b->d_misc + 2, b->d_misc + 3);
+  return rc;
 }
 
 // Dynamic shared memory a CTA may take for the on-chip passes (the 227 KB
@@ -428,6 +475,7 @@ void pf_batch_default_options(pf_batch_options* o) {
   o->threads = 512;
   o->max_cases = 1024;
   o->hbm_budget_bytes = (uint64_t)150 << 30;
+  o->use_graph = 1;
 }
 
 int pf_batch_create(const pf_batch_options* opt, pf_batch** out) {
@@ -451,9 +499,15 @@ int pf_batch_create(const pf_batch_options* opt, pf_batch** out) {
   if (e == cudaSuccess) e = cudaMalloc(&b->d_misc, sizeof(int) * 8);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[0]);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev[1]);
+  if (e == cudaSuccess) e = cudaHostAlloc(&b->h_desc, sizeof(CaseDesc) * b->capacity, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaHostAlloc(&b->h_order, sizeof(int) * 2 * b->capacity, cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaHostAlloc(&b->h_misc, sizeof(int) * 8, cudaHostAllocDefault);
   if (e != cudaSuccess) {
     if (b->d_desc) cudaFree(b->d_desc);
     if (b->d_order) cudaFree(b->d_order);
+    if (b->d_misc) cudaFree(b->d_misc);
+    if (b->h_desc) cudaFreeHost(b->h_desc);
+    if (b->h_order) cudaFreeHost(b->h_order);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return cuda_fail(e, "pf_batch_create");
@@ -479,9 +533,13 @@ int pf_batch_destroy(pf_batch* b) {
     if (c) pf_destroy(c);
   for (auto e : b->case_ev)
     if (e) cudaEventDestroy(e);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
   cudaFree(b->d_desc);
   cudaFree(b->d_order);
   cudaFree(b->d_misc);
+  cudaFreeHost(b->h_desc);
+  cudaFreeHost(b->h_order);
+  cudaFreeHost(b->h_misc);
   cudaEventDestroy(b->ev[0]);
   cudaEventDestroy(b->ev[1]);
   cudaStreamDestroy(b->st);
@@ -681,17 +739,54 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
   for (auto& p : order2) order.push_back(p.second);
   for (auto& p : order3) order.push_back(p.second);
   if ((int)desc.size() > b->capacity) return fail(PF_E_INVALID, "too many cases");
-  int misc[8] = {(int)order2.size(), 0, (int)order3.size(), 0, 0, 0, 0, 0};
-  if (!desc.empty()) {
-    PF_CUDA(cudaMemcpyAsync(b->d_desc, desc.data(), sizeof(CaseDesc) * desc.size(), cudaMemcpyHostToDevice, b->st));
-    PF_CUDA(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->st));
-    PF_CUDA(cudaMemcpyAsync(b->d_misc, misc, sizeof(misc), cudaMemcpyHostToDevice, b->st));
-  }
+  const int n2 = (int)order2.size(), n3 = (int)order3.size();
   int rc = PF_OK;
-  if (!order2.empty()) rc = launch_dim<2>(b, (int)order2.size(), smem2, b->d_order, b->d_misc + 0, b->d_misc + 1);
-  if (rc == PF_OK && !order3.empty())
-    rc = launch_dim<3>(b, (int)order3.size(), 0, b->d_order + order2.size(), b->d_misc + 2, b->d_misc + 3);
-  if (rc) return rc;
+  if (!desc.empty()) {
+    // the previous call ended with a stream synchronisation, so no copy of
+    // an earlier call still reads the pinned staging
+    std::memcpy(b->h_desc, desc.data(), sizeof(CaseDesc) * desc.size());
+    std::memcpy(b->h_order, order.data(), sizeof(int) * order.size());
+    const int misc[8] = {n2, 0, n3, 0, 0, 0, 0, 0};
+    std::memcpy(b->h_misc, misc, sizeof(misc));
+    int ncl2 = 0, ncl3 = 0;
+    if (n2) rc = prepare_dim<2>(b, smem2, n2, &ncl2);
+    if (rc == PF_OK && n3) rc = prepare_dim<3>(b, 0, n3, &ncl3);
+    if (rc) return rc;
+    if (!b->opt.use_graph) {
+      rc = enqueue_persistent(b, n2, n3, smem2, ncl2, ncl3);
+      if (rc) return rc;
+    } else {
+      const long long key[6] = {n2, n3, (long long)smem2, b->opt.cluster, b->opt.threads,
+                                (long long)ncl2 * 65536 + ncl3};
+      if (!b->gexec || std::memcmp(key, b->gkey, sizeof(key)) != 0) {
+        if (b->gexec) {
+          cudaGraphExecDestroy(b->gexec);
+          b->gexec = nullptr;
+        }
+        PF_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_persistent(b, n2, n3, smem2, ncl2, ncl3);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(b->st, &graph);
+        if (rc) {
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+        if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(batch)");
+        const cudaError_t ei = cudaGraphInstantiate(&b->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+          b->gexec = nullptr;
+          return cuda_fail(ei, "cudaGraphInstantiate(batch)");
+        }
+        std::memcpy(b->gkey, key, sizeof(key));
+        b->graphs_captured++;
+      } else {
+        b->graph_replays++;
+      }
+      PF_CUDA(cudaGraphLaunch(b->gexec, b->st));
+    }
+    b->launches += (n2 ? 1 : 0) + (n3 ? 1 : 0);
+  }
   for (auto& lc : large) PF_CUDA(cudaStreamWaitEvent(b->st, b->case_ev[lc.first], 0));
   PF_CUDA(cudaEventRecord(b->ev[1], b->st));
   // the host arrays above must outlive the async copies
@@ -753,6 +848,13 @@ int pf_batch_configure(pf_batch* b, int cluster, int threads) {
     return fail(PF_E_INVALID, "pf_batch_configure: cluster must be 1,2,4,8,16 and threads 256,512,1024");
   b->opt.cluster = cluster;
   b->opt.threads = threads;
+  return PF_OK;
+}
+
+int pf_batch_graph_stats(pf_batch* b, int64_t* captured, int64_t* replays) {
+  if (!b) return fail(PF_E_INVALID, "null batch");
+  if (captured) *captured = b->graphs_captured;
+  if (replays) *replays = b->graph_replays;
   return PF_OK;
 }
 

@@ -121,6 +121,35 @@ def test_batch_launch_is_persistent_one_per_dimension():
         assert b.kernel_launches() - n0 == 2  # one 2D launch + one 3D launch for 3 steps of 5 cases
 
 
+def test_persistent_launch_graph_replays_match_plain_launches():
+    """The persistent part of a call runs as a CUDA graph captured per
+    composition: repeated calls of the same composition replay it (the
+    descriptors, which change between calls, are read from the pinned
+    staging when the graph runs), a new composition or launch shape captures
+    again, and the fields equal those of plain launches bit for bit."""
+    cases = _cases()
+    plan = [([0, 1, 2, 3, 4], [2, 2, 2, 2, 2]), ([0, 1, 2, 3, 4], [1, 3, 2, 1, 2]), ([0, 1, 2, 3, 4], [2] * 5),
+            ([0, 2, 4], [1, 1, 1]), ([0, 1, 2, 3, 4], [1] * 5)]
+    outs = []
+    for graph in (True, False):
+        with Batch(cluster=2, threads=512, use_graph=graph) as b:
+            slots = [b.add(*c) for c in cases]
+            for k, (which, steps) in enumerate(plan):
+                if k == 3:
+                    b.configure(4, 256)
+                b.step_slots([slots[i] for i in which], steps)
+            outs.append(([b.get_state(sl) for sl in slots], [b.norms(sl) for sl in slots]))
+            captured, replays = b.graph_stats()
+            if graph:
+                # plan[1] and plan[2] have plan[0]'s composition; plan[3] differs; plan[4] has a new shape
+                assert captured == 3 and replays == 2, (captured, replays)
+            else:
+                assert captured == 0 and replays == 0
+    for k in range(len(cases)):
+        assert _same(outs[0][0][k], outs[1][0][k]), k
+        assert outs[0][1][k] == outs[1][1][k]
+
+
 def test_admission_bytes_equal_the_allocation():
     """The admission estimate (pf_case_bytes through case_bytes) is the
     allocation a batch makes for the case, for small cases (stepped by the

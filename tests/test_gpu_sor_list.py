@@ -85,26 +85,42 @@ def test_sum6_error_bound_any_exponents_and_special_values():
     assert not ok[7]                # result below the normal range
 
 
-def _fluid_counts(vals, shape):
-    """Pure-fluid cells per colour from the porosity, by the face values of
-    the reference's coefficients, max(1e-6, (eps_c + eps_nb) * 0.5), all six
-    exactly 1 (IEEE double arithmetic, as on the device: a neighbour of
-    porosity 1 - 2^-53 still gives a face of exactly 1), at interior
-    i = 2 .. m-1 (the inlet and outlet rows carry the matrix edits).
-    Porosity ghosts: x copies, y/z periodic."""
+def _fluid_counts(s, vals, shape):
+    """Pure-fluid cells per colour from the porosity: the six normalised
+    coefficients a_d * omega/ap, with a_d = dt*max(1e-6, (eps_c + eps_nb)*0.5)
+    /h/h and ap = -a_e - a_w - a_n - a_s - a_t - a_b, evaluated in IEEE double
+    in the library's order, equal those of a cell whose neighbourhood has
+    porosity exactly 1 (a neighbour of 1 - 2^-53 can still round to the same
+    coefficient), at interior i = 2 .. m-1 (the inlet and outlet rows carry
+    the matrix edits).  Porosity ghosts: x copies, y/z periodic."""
     m, n, l = shape
-    e = np.pad(np.maximum(vals, 1e-6), 1, mode="wrap")
+    dx, dy, dz = s.width / (m - 1), s.height / (n - 1), s.depth / (l - 1)
+    dt = s.time / s.istep_max
+    e = np.pad(np.maximum(vals, s.threshold), 1, mode="wrap")
     e[:, :, 0] = e[:, :, 1]
     e[:, :, -1] = e[:, :, -2]
     c = e[1:-1, 1:-1, 1:-1]
-    face = lambda nb: np.maximum(1e-6, (c + nb) * 0.5) == 1.0
-    fl = (face(e[1:-1, 1:-1, 2:]) & face(e[1:-1, 1:-1, :-2]) & face(e[1:-1, 2:, 1:-1]) & face(e[1:-1, :-2, 1:-1])
-          & face(e[2:, 1:-1, 1:-1]) & face(e[:-2, 1:-1, 1:-1]))
+    nbs = [(e[1:-1, 1:-1, 2:], dx), (e[1:-1, 1:-1, :-2], dx), (e[1:-1, 2:, 1:-1], dy), (e[1:-1, :-2, 1:-1], dy),
+           (e[2:, 1:-1, 1:-1], dz), (e[:-2, 1:-1, 1:-1], dz)]
+
+    def coefs(cc, nb_list):
+        a = [dt * np.maximum(1e-6, (nb + cc) * 0.5 if d % 2 == 0 else (cc + nb) * 0.5) / h / h
+             for d, (nb, h) in enumerate(nb_list)]
+        ap = -a[0] - a[1] - a[2] - a[3] - a[4] - a[5]
+        wap = s.relux_factor / ap
+        return [x * wap for x in a]
+
+    got = coefs(c, nbs)
+    one = np.ones(1)
+    ref = coefs(one, [(one, h) for _, h in nbs])
+    fl = np.ones(c.shape, bool)
+    for x, r in zip(got, ref):
+        fl &= x == r[0]
     fl[:, :, 0] = False
     fl[:, :, -1] = False
     k, j, i = np.meshgrid(np.arange(1, l + 1), np.arange(1, n + 1), np.arange(1, m + 1), indexing="ij")
     colour = (i + j + k) & 1
-    return [int(np.sum(fl & (colour == c))) for c in (0, 1)], [int(np.sum(colour == c)) for c in (0, 1)]
+    return [int(np.sum(fl & (colour == q))) for q in (0, 1)], [int(np.sum(colour == q)) for q in (0, 1)]
 
 
 @pytest.mark.parametrize("shape", [(48, 40, 36), (47, 41, 35), (64, 64, 64)])
@@ -113,7 +129,7 @@ def test_list_classification_matches_host_count(shape):
     vals = G.spheres_3d(*shape, count=6, seed=4)
     with Case(s, shape, vals) as c:
         info = c.sor_info()
-    fluid, total = _fluid_counts(vals, shape)
+    fluid, total = _fluid_counts(s, vals, shape)
     assert info["listed"]
     assert info["fluid"] == fluid and info["total"] == total, (info, fluid, total)
     assert 0 < fluid[0] < total[0]
