@@ -481,12 +481,12 @@ static int finish_setup(pf_case* c) {
   int rc = check_launch("case set-up kernels");
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st));
-  if (c->opt.precision == PF_PREC_MIXED) return mixed_choose_sweep(c);
   if (c->opt.sor_path == PF_SOR_AUTO && sor_list_eligible(g)) {
     rc = sor_list_setup(c);
     if (rc) return rc;
     c->use_list = true;
   }
+  if (c->opt.precision == PF_PREC_MIXED) return mixed_choose_sweep(c);
   return PF_OK;
 }
 

@@ -562,6 +562,8 @@ int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
   size_t b = nat8 * (6 + (d == 3) + 2 * d) + pk8 * (2 + 2 * (2 * d + 3));
   b += r256((size_t)(g.m + 2) * (g.n + 2) * g.Z * 8) + RED_TOTAL * sizeof(unsigned long long);
   if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * (mixed_fused(g, *opt) ? 8 : 6) + 256;
+  // the cell lists of the 3D sweep and residual: one 32-bit entry per cell
+  if (sor_list_eligible(g) && (!opt || opt->sor_path == PF_SOR_AUTO)) b += sor_list_bytes(g);
   *bytes = b;
   return PF_OK;
 }
@@ -607,7 +609,7 @@ static int batch_add_impl(pf_batch* b, const pf_params* prm, const pf_options* o
   }
   b->slots[free_slot] = c;
   b->pending[free_slot] = 0;
-  b->bytes_in_use += c->bytes + c->mixed_bytes;
+  b->bytes_in_use += c->bytes + c->mixed_bytes + c->list_bytes;
   *slot = free_slot;
   return PF_OK;
 }
@@ -632,7 +634,7 @@ int pf_batch_remove(pf_batch* b, int slot) {
   if (!b || slot < 0 || slot >= b->capacity || !b->slots[slot]) return fail(PF_E_INVALID, "pf_batch_remove: bad slot");
   PF_CUDA(cudaStreamSynchronize(b->st));
   pf_case* c = b->slots[slot];
-  b->bytes_in_use -= c->bytes + c->mixed_bytes;
+  b->bytes_in_use -= c->bytes + c->mixed_bytes + c->list_bytes;
   pf_destroy(c);
   b->slots[slot] = nullptr;
   b->pending[slot] = 0;

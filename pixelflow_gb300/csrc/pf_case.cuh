@@ -51,12 +51,15 @@ struct pf_case {
   std::vector<cudaEvent_t> ev_io;
 
   // ---- the plain 3D sweep driven by cell lists (pf_sor_list.cu) ----
-  // per colour: packed (h, j, k) of every cell, pure-fluid cells first
+  // per colour: every cell's packed index and flags, in chunks of 32 that
+  // are all fluid or all other cells, merged by position
   bool use_list = false;
   unsigned* list_base = nullptr;
   unsigned* list[2] = {nullptr, nullptr};
   size_t list_bytes = 0;
-  int list_nfluid[2] = {0, 0}, list_ntotal[2] = {0, 0};
+  int list_nfluid[2] = {0, 0}, list_ntotal[2] = {0, 0};  // cells per colour: fluid, all
+  int list_nchunks[2] = {0, 0};                            // chunks of 32 entries per colour
+  int list_grid = 0;                                       // CTAs of the persistent launch
   double list_const[6] = {0, 0, 0, 0, 0, 0};  // the fluid cells' normalised coefficients
   bool list_iso = false;                        // all six equal (dx = dy = dz)
 
@@ -100,7 +103,11 @@ void enqueue_boundary_mixed(pf_case* c);
 int geometry_to_stage(pf_case* c, const pf_shape* shapes, int nshapes, double edge);
 // The list-driven plain sweep (3D, no walls, sizes that pack into 32 bits).
 bool sor_list_eligible(const Geo& g);
+size_t sor_list_bytes(const Geo& g);
 int sor_list_setup(pf_case* c);
 void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool early,
                      cudaStream_t st);
+// The precision form's FP64 residual over the same lists.
+void launch_residual_list(const pf_case* c, int col, float* rf, float* ec, unsigned long long* rmax, const int* skip,
+                          cudaStream_t st);
 }  // namespace pf

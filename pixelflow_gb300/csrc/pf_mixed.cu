@@ -175,9 +175,13 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   const bool fused = c->use_fused;
   for (int pass = 0; pass < c->opt.outer_max; pass++) {
     launch_zero_u64(&c->red[RED_RMAX], RED_SLOTS, st);
-    for (int col = 0; col < 2; col++)
-      launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col],
-                      &c->red[RED_RMAX], skip, st);
+    for (int col = 0; col < 2; col++) {
+      if (c->use_list)
+        launch_residual_list(c, col, c->rf[col], c->e[col], &c->red[RED_RMAX], skip, st);
+      else
+        launch_residual(g, c->C[col], c->p[col], c->p[1 - col], s.omega, col, c->rf[col], c->e[col],
+                        &c->red[RED_RMAX], skip, st);
+    }
     if (early) launch_dc_check(&c->red[RED_RMAX], c->opt.dc_tol * s.omega, c->skip, st);
     const float* efin[2] = {c->e[0], c->e[1]};
     if (fused) {

@@ -19,10 +19,23 @@
 // A warp must not mix the two paths (a masked-off lane still occupies the
 // FP64 pipe, and a run of 32 cells along x that touches any obstacle would
 // drop the whole warp to the slow path).  So at set-up each colour's cells
-// are listed once, the fluid cells first and then the others, each part in
-// memory order, and one launch per half-sweep walks the list: thread t
-// updates cell list[t], and only the warp at the boundary of the two parts
-// diverges.  Entries pack (h, j, k) into 32 bits (11 + 11 + 10 bits).
+// are split into a fluid list and a list of the others, each in memory
+// order and cut into chunks of 32 (one warp); the chunks of both lists are
+// then merged by position, so a warp's chunk is all fluid or all other, and
+// warps working side by side touch the same region of the arrays (a first
+// version ran all fluid cells before all others: the others' sectors were
+// fetched twice, +35 % DRAM reads).  An entry is the cell's packed index q
+// (26 bits), its x parity and whether it sits on the first or last row or
+// plane (the periodic neighbours), and the fluid bit, so every neighbour
+// address is q plus a constant.
+//
+// The list entry is one more dependent load ahead of the cell's operands: a
+// launch of one cell per thread (36 waves of short CTAs at 256^3) paid two
+// DRAM round trips per wave and ran latency-bound (60 us at 192^3 against
+// 49 us for the per-cell sweep, DRAM 58 %, issue 43 %).  The sweep is
+// therefore one wave of persistent CTAs, each warp looping over chunks and
+// loading the next chunk's entry while the current cell's operands are in
+// flight.
 //
 // Arithmetic against k_sor_half: the fluid cells' neighbour sum is rounded
 // once instead of six times, so the iterates differ in the last bits; the
@@ -32,6 +45,7 @@
 
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "pf_case.cuh"
@@ -137,84 +151,143 @@ __global__ void k_fluid_flags(Geo g, Scal s, Coef<double> C, int colour, unsigne
   flags[t] = out;
 }
 
-// One half-sweep over the list: entries [0, nfluid) are fluid cells,
-// [nfluid, ntotal) the others.  ISO: the six fluid constants are equal
-// (dx = dy = dz); otherwise the fluid cells use the three constants with
-// FP64 FMAs (still without coefficient loads).  EARLY: the list entry and
-// the operator load before griddepcontrol.wait (see k_sor_half).
-template <bool TRACK, bool EARLY, bool ISO>
+constexpr unsigned LIST_Q = 0x03ffffffu;   // packed index field (26 bits)
+constexpr unsigned LIST_NONE = LIST_Q;     // padding entry: no cell
+constexpr int LIST_S = 26, LIST_JLO = 27, LIST_JHI = 28, LIST_KLO = 29, LIST_KHI = 30, LIST_FLUID = 31;
+
+// Neighbour offsets of the periodic edges: a cell on row n reads row jn_n
+// (the opposite interior row or the ghost row), and so on.
+struct ListOffsets {
+  idx_t H, HY, dN, dS, dT, dB;
+};
+__host__ __device__ inline ListOffsets list_offsets(const Geo& g) {
+  ListOffsets o;
+  o.H = g.H;
+  o.HY = (idx_t)g.H * g.Y;
+  o.dN = (idx_t)(g.jn_n - g.n) * g.H;
+  o.dS = (idx_t)(g.js_1 - 1) * g.H;
+  o.dT = (idx_t)(g.kt_l - g.l) * o.HY;
+  o.dB = (idx_t)(g.kb_1 - 1) * o.HY;
+  return o;
+}
+
+// The cell of entry e: its index and its six neighbours' (e, w, n, s, t, b).
+__device__ __forceinline__ idx_t list_cell(unsigned e, const ListOffsets& o, idx_t nb[6]) {
+  const idx_t q = (idx_t)(e & LIST_Q);
+  const idx_t s = (e >> LIST_S) & 1u;
+  nb[0] = q + s;
+  nb[1] = q - 1 + s;
+  nb[2] = q + (((e >> LIST_JHI) & 1u) ? o.dN : o.H);
+  nb[3] = q + (((e >> LIST_JLO) & 1u) ? o.dS : -o.H);
+  nb[4] = q + (((e >> LIST_KHI) & 1u) ? o.dT : o.HY);
+  nb[5] = q + (((e >> LIST_KLO) & 1u) ? o.dB : -o.HY);
+  return q;
+}
+
+// sum_nb a_nb p_nb of one cell: the exact sum times the fluid constant for a
+// fluid cell (ISO), the three constants, or the cell's own coefficients.
+template <bool ISO>
+__device__ __forceinline__ double list_stencil(bool fl, const double (&x)[6], const Coef<double>& C, idx_t q,
+                                               double tt, double ax, double ay, double az) {
+  if (fl) {
+    if (ISO) {
+      double sum;
+      if (!sum6_exact(x, sum)) sum = ((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5];
+      return fma(-ax, sum, tt);
+    }
+    tt = fma(-ax, x[0], tt);
+    tt = fma(-ax, x[1], tt);
+    tt = fma(-ay, x[2], tt);
+    tt = fma(-ay, x[3], tt);
+    tt = fma(-az, x[4], tt);
+    return fma(-az, x[5], tt);
+  }
+  double c[6];
+#pragma unroll
+  for (int d = 0; d < 6; d++) c[d] = C.a[d][q];
+#pragma unroll
+  for (int d = 0; d < 6; d++) tt = fma(-c[d], x[d], tt);
+  return tt;
+}
+
+// One half-sweep over the chunked list of one colour: warp w takes chunks
+// w, w + W, ... (W warps in the grid), one entry per lane, and loads the
+// next chunk's entry before working on the current one.  ISO: the six fluid
+// constants are equal (dx = dy = dz); otherwise the fluid cells use the
+// three constants with FP64 FMAs (still without coefficient loads).
+template <bool TRACK, bool ISO>
 __global__ void __launch_bounds__(LIST_THREADS)
     k_sor_list3(Geo g, Coef<double> C, double* __restrict__ pc, const double* __restrict__ po, double omw,
-                int colour, const unsigned* __restrict__ list, int nfluid, int ntotal, double ax, double ay,
-                double az, unsigned long long* __restrict__ err, const int* __restrict__ skip) {
-  const int t = blockIdx.x * LIST_THREADS + threadIdx.x;
-  const bool act = t < ntotal;
-  const bool fl = t < nfluid;
-  int h = 0, j = 1, k = 1;
-  idx_t q = 0;
-  double cb = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0, c5 = 0.0;
-  auto locate = [&]() {
-    const unsigned e = list[t];
-    h = (int)(e & 0x7ffu);
-    j = (int)((e >> 11) & 0x7ffu);
-    k = (int)(e >> 22);
-    q = pk_idx(g, h, j, k);
-  };
-  auto load_operator = [&]() {
-    cb = C.bbn[q];
-    if (!fl) {
-      c0 = C.a[0][q];
-      c1 = C.a[1][q];
-      c2 = C.a[2][q];
-      c3 = C.a[3][q];
-      c4 = C.a[4][q];
-      c5 = C.a[5][q];
-    }
-  };
-  if (act) locate();
-  if (EARLY && act) load_operator();
+                const unsigned* __restrict__ list, int nchunks, double ax, double ay, double az,
+                unsigned long long* __restrict__ err, const int* __restrict__ skip) {
+  const int lane = threadIdx.x & 31;
+  const int W = gridDim.x * (LIST_THREADS / 32);
+  int w = blockIdx.x * (LIST_THREADS / 32) + (threadIdx.x >> 5);
+  unsigned e = w < nchunks ? list[(size_t)w * 32 + lane] : LIST_NONE;
   pdl_begin();
   if (skip && *skip) return;
-  if (!EARLY && act) load_operator();
-  unsigned long long e = 0;
-  if (act) {
-    const int s = (colour + j + k) & 1;
-    const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
-    const idx_t qn = (j == g.n) ? pk_idx(g, h, g.jn_n, k) : q + H;
-    const idx_t qs = (j == 1) ? pk_idx(g, h, g.js_1, k) : q - H;
-    const idx_t qt = (k == g.l) ? pk_idx(g, h, j, g.kt_l) : q + HY;
-    const idx_t qb = (k == 1) ? pk_idx(g, h, j, g.kb_1) : q - HY;
-    const double pold = pc[q];
-    const double x[6] = {po[q + s], po[q - 1 + s], po[qn], po[qs], po[qt], po[qb]};
-    double tt;
-    if (fl) {
-      if (ISO) {
-        double sum;
-        if (!sum6_exact(x, sum)) sum = ((((x[0] + x[1]) + x[2]) + x[3]) + x[4]) + x[5];
-        tt = fma(-ax, sum, cb);
-      } else {
-        tt = cb;
-        tt = fma(-ax, x[0], tt);
-        tt = fma(-ax, x[1], tt);
-        tt = fma(-ay, x[2], tt);
-        tt = fma(-ay, x[3], tt);
-        tt = fma(-az, x[4], tt);
-        tt = fma(-az, x[5], tt);
+  const ListOffsets o = list_offsets(g);
+  unsigned long long emax = 0;
+  for (; w < nchunks; w += W) {
+    const unsigned en = w + W < nchunks ? list[(size_t)(w + W) * 32 + lane] : LIST_NONE;
+    if (e != LIST_NONE) {
+      idx_t nb[6];
+      const idx_t q = list_cell(e, o, nb);
+      const bool fl = (e >> LIST_FLUID) & 1u;
+      const double cb = C.bbn[q];
+      const double pold = pc[q];
+      double x[6];
+#pragma unroll
+      for (int d = 0; d < 6; d++) x[d] = po[nb[d]];
+      const double pnew = fma(omw, pold, list_stencil<ISO>(fl, x, C, q, cb, ax, ay, az));
+      pc[q] = pnew;
+      if (TRACK) {
+        const unsigned long long b = abs_diff_bits(pnew, pold);
+        emax = b > emax ? b : emax;
       }
-    } else {
-      tt = cb;
-      tt = fma(-c0, x[0], tt);
-      tt = fma(-c1, x[1], tt);
-      tt = fma(-c2, x[2], tt);
-      tt = fma(-c3, x[3], tt);
-      tt = fma(-c4, x[4], tt);
-      tt = fma(-c5, x[5], tt);
     }
-    const double pnew = fma(omw, pold, tt);
-    pc[q] = pnew;
-    if (TRACK) e = abs_diff_bits(pnew, pold);
+    e = en;
   }
-  if (TRACK) warp_max_atomic(e, err);
+  if (TRACK) warp_max_atomic(emax, err);
+}
+
+// The precision form's FP64 residual over the same lists, r = bbn - omega p -
+// sum_nb a_nb p_nb (normalised by omega/ap), stored as the FP32 right-hand
+// side of the correction sweeps; zeroes the cell's correction and reduces
+// max |r|.
+template <bool ISO>
+__global__ void __launch_bounds__(LIST_THREADS)
+    k_residual_list3(Geo g, Coef<double> C, const double* __restrict__ pc, const double* __restrict__ po,
+                     double omega, const unsigned* __restrict__ list, int nchunks, double ax, double ay, double az,
+                     float* __restrict__ rf, float* __restrict__ ec, unsigned long long* __restrict__ rmax,
+                     const int* __restrict__ skip) {
+  const int lane = threadIdx.x & 31;
+  const int W = gridDim.x * (LIST_THREADS / 32);
+  int w = blockIdx.x * (LIST_THREADS / 32) + (threadIdx.x >> 5);
+  unsigned e = w < nchunks ? list[(size_t)w * 32 + lane] : LIST_NONE;
+  pdl_begin();
+  if (skip && *skip) return;
+  const ListOffsets o = list_offsets(g);
+  unsigned long long rm = 0;
+  for (; w < nchunks; w += W) {
+    const unsigned en = w + W < nchunks ? list[(size_t)(w + W) * 32 + lane] : LIST_NONE;
+    if (e != LIST_NONE) {
+      idx_t nb[6];
+      const idx_t q = list_cell(e, o, nb);
+      const bool fl = (e >> LIST_FLUID) & 1u;
+      double x[6];
+#pragma unroll
+      for (int d = 0; d < 6; d++) x[d] = po[nb[d]];
+      double tt = list_stencil<ISO>(fl, x, C, q, C.bbn[q], ax, ay, az);
+      tt = fma(-omega, pc[q], tt);
+      rf[q] = (float)tt;
+      ec[q] = 0.0f;
+      const unsigned long long b = abs_bits(tt);
+      rm = b > rm ? b : rm;
+    }
+    e = en;
+  }
+  warp_max_atomic(rm, rmax);
 }
 
 // Exact six-term sums of n groups (testing entry point).
@@ -232,13 +305,18 @@ __global__ void k_sum6(const double* __restrict__ x, int n, double* __restrict__
 
 }  // namespace
 
-bool sor_list_eligible(const Geo& g) {
-  return g.dim == 3 && !g.wall && ((g.m >> 1) + 1) < 2048 && g.n < 2048 && g.l < 1024;
-}
+bool sor_list_eligible(const Geo& g) { return g.dim == 3 && !g.wall && g.pk < (long long)LIST_Q; }
 
-// Builds both colours' lists on the device: flags per work item, copied to
-// the host, partitioned (fluid cells, then the rest, each in memory order),
-// packed and copied back into one allocation.
+// Device bytes of a case's lists, fixed by the grid alone (admission
+// control needs it before the porosity is known): every cell once plus the
+// padding of at most four partial chunks (two lists per colour).
+size_t sor_list_bytes(const Geo& g) { return ((size_t)g.m * g.n * g.l + 4 * 32) * sizeof(unsigned); }
+
+// Builds both colours' lists: flags per work item on the device, copied to
+// the host; per colour the fluid cells and the others in memory order, cut
+// into chunks of 32 entries (the last chunk of each padded with LIST_NONE),
+// the two chunk sequences merged by the position of their first cell; one
+// device allocation for both colours.  Also sizes the persistent launch.
 int sor_list_setup(pf_case* c) {
   const Geo& g = c->g;
   const long long items = packed_items(g);
@@ -254,6 +332,7 @@ int sor_list_setup(pf_case* c) {
   std::vector<unsigned> lists[2];
   double consts[6] = {0, 0, 0, 0, 0, 0};
   const unsigned grid = (unsigned)((items + LIST_THREADS - 1) / LIST_THREADS);
+  const int W = packed_width(g);
   int rc = PF_OK;
   for (int col = 0; col < 2 && rc == PF_OK; col++) {
     k_fluid_flags<<<grid, LIST_THREADS, 0, c->st>>>(g, c->s, c->C[col], col, dflags, dconst);
@@ -264,32 +343,47 @@ int sor_list_setup(pf_case* c) {
       rc = cuda_fail(e, "fluid flags");
       break;
     }
-    std::vector<unsigned>& L = lists[col];
-    const int W = packed_width(g);
-    int nfl = 0;
-    for (int pass = 1; pass <= 2; pass++) {
-      for (long long t = 0; t < items; t++) {
-        if (flags[(size_t)t] != pass) continue;
-        const int row = (int)(t / W);
-        const int h = (int)(t - (long long)row * W);
-        const int k = row / g.n + 1, j = row - (k - 1) * g.n + 1;
-        L.push_back((unsigned)h | ((unsigned)j << 11) | ((unsigned)k << 22));
-      }
-      if (pass == 1) nfl = (int)L.size();
+    std::vector<unsigned> part[2];  // [0] fluid, [1] the others
+    for (long long t = 0; t < items; t++) {
+      const unsigned char f = flags[(size_t)t];
+      if (!f) continue;
+      const int row = (int)(t / W);
+      const int h = (int)(t - (long long)row * W);
+      const int k = row / g.n + 1, j = row - (k - 1) * g.n + 1;
+      const int sd = (col + j + k) & 1;
+      const unsigned q = (unsigned)pk_idx(g, h, j, k);
+      part[f == 1 ? 0 : 1].push_back(q | ((unsigned)sd << LIST_S) | ((unsigned)(j == 1) << LIST_JLO) |
+                                      ((unsigned)(j == g.n) << LIST_JHI) | ((unsigned)(k == 1) << LIST_KLO) |
+                                      ((unsigned)(k == g.l) << LIST_KHI) | ((unsigned)(f == 1) << LIST_FLUID));
     }
-    c->list_nfluid[col] = nfl;
-    c->list_ntotal[col] = (int)L.size();
+    c->list_nfluid[col] = (int)part[0].size();
+    c->list_ntotal[col] = (int)(part[0].size() + part[1].size());
+    std::vector<unsigned>& L = lists[col];
+    size_t at[2] = {0, 0};
+    while (at[0] < part[0].size() || at[1] < part[1].size()) {
+      int pick;
+      if (at[0] >= part[0].size())
+        pick = 1;
+      else if (at[1] >= part[1].size())
+        pick = 0;
+      else
+        pick = (part[0][at[0]] & LIST_Q) < (part[1][at[1]] & LIST_Q) ? 0 : 1;
+      for (int r = 0; r < 32; r++) L.push_back(at[pick] + r < part[pick].size() ? part[pick][at[pick] + r] : LIST_NONE);
+      at[pick] += 32;
+    }
+    c->list_nchunks[col] = (int)(L.size() / 32);
   }
   cudaFree(dflags);
   cudaFree(dconst);
   if (rc) return rc;
   const size_t n0 = lists[0].size(), n1 = lists[1].size();
+  if ((n0 + n1) * sizeof(unsigned) > sor_list_bytes(g)) return fail(PF_E_INVALID, "cell lists exceed their bound");
   unsigned* d = nullptr;
-  PF_CUDA(cudaMalloc(&d, (n0 + n1) * sizeof(unsigned)));
+  PF_CUDA(cudaMalloc(&d, sor_list_bytes(g)));
   c->list_base = d;
   c->list[0] = d;
   c->list[1] = d + n0;
-  c->list_bytes = (n0 + n1) * sizeof(unsigned);
+  c->list_bytes = sor_list_bytes(g);
   PF_CUDA(cudaMemcpyAsync(c->list[0], lists[0].data(), n0 * sizeof(unsigned), cudaMemcpyHostToDevice, c->st));
   PF_CUDA(cudaMemcpyAsync(c->list[1], lists[1].data(), n1 * sizeof(unsigned), cudaMemcpyHostToDevice, c->st));
   PF_CUDA(cudaStreamSynchronize(c->st));
@@ -302,31 +396,51 @@ int sor_list_setup(pf_case* c) {
   c->list_iso = bits(consts[0]) == bits(consts[1]) && bits(consts[0]) == bits(consts[2]) &&
                 bits(consts[0]) == bits(consts[3]) && bits(consts[0]) == bits(consts[4]) &&
                 bits(consts[0]) == bits(consts[5]);
+  // one wave of persistent CTAs (the fewest resident of the sweep's and the
+  // residual's variants), no more than the chunks need
+  int dev = 0, sms = 0;
+  PF_CUDA(cudaGetDevice(&dev));
+  PF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = 1 << 20;
+  for (const void* k : {(const void*)k_sor_list3<true, true>, (const void*)k_sor_list3<false, true>,
+                        (const void*)k_sor_list3<true, false>, (const void*)k_sor_list3<false, false>,
+                        (const void*)k_residual_list3<true>, (const void*)k_residual_list3<false>}) {
+    int n = 0;
+    PF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, LIST_THREADS, 0));
+    per_sm = std::min(per_sm, n);
+  }
+  per_sm = std::max(1, per_sm);
+  const long long need = ((long long)std::max(c->list_nchunks[0], c->list_nchunks[1]) + LIST_THREADS / 32 - 1) /
+                         (LIST_THREADS / 32);
+  c->list_grid = (int)std::max(1LL, std::min<long long>((long long)sms * per_sm, need));
   return PF_OK;
 }
 
-void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool early,
+void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool /*early*/,
                      cudaStream_t st) {
-  const Geo& g = c->g;
-  const int nt = c->list_ntotal[col];
-  const unsigned grid = (unsigned)((nt + LIST_THREADS - 1) / LIST_THREADS);
   const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
-#define PF_SL(TR, EA, ISO)                                                                                      \
-  launch_pdl(k_sor_list3<TR, EA, ISO>, dim3(grid), dim3(LIST_THREADS), st, g, c->C[col], c->p[col],          \
-             (const double*)c->p[1 - col], omw, col, (const unsigned*)c->list[col], c->list_nfluid[col], nt, ax, \
-             ay, az, err, (const int*)nullptr)
-  if (c->list_iso) {
-    if (err)
-      early ? PF_SL(true, true, true) : PF_SL(true, false, true);
-    else
-      early ? PF_SL(false, true, true) : PF_SL(false, false, true);
-  } else {
-    if (err)
-      early ? PF_SL(true, true, false) : PF_SL(true, false, false);
-    else
-      early ? PF_SL(false, true, false) : PF_SL(false, false, false);
-  }
+#define PF_SL(TR, ISO)                                                                                          \
+  launch_pdl(k_sor_list3<TR, ISO>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col], c->p[col],      \
+             (const double*)c->p[1 - col], omw, (const unsigned*)c->list[col], c->list_nchunks[col], ax, ay, az, \
+             err, (const int*)nullptr)
+  if (c->list_iso)
+    err ? PF_SL(true, true) : PF_SL(false, true);
+  else
+    err ? PF_SL(true, false) : PF_SL(false, false);
 #undef PF_SL
+}
+
+void launch_residual_list(const pf_case* c, int col, float* rf, float* ec, unsigned long long* rmax, const int* skip,
+                          cudaStream_t st) {
+  const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
+  if (c->list_iso)
+    launch_pdl(k_residual_list3<true>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+               (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
+               c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
+  else
+    launch_pdl(k_residual_list3<false>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+               (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
+               c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
 }
 
 }  // namespace pf

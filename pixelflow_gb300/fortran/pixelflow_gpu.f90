@@ -10,6 +10,7 @@ module pixelflow_gpu
   integer(c_int), parameter :: PF_OK = 0
   integer(c_int), parameter :: PF_PREC_FP64 = 0, PF_PREC_MIXED = 1
   integer(c_int), parameter :: PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1, PF_SWEEP_FUSED = 2
+  integer(c_int), parameter :: PF_SOR_AUTO = 0, PF_SOR_CELLS = 1
 
   type, bind(C) :: pf_params
     integer(c_int32_t) :: dim, m, n, l

@@ -170,3 +170,28 @@ def test_list_path_graph_and_eager_agree():
             outs.append(c.get_state())
     for f in ("u", "v", "w", "p"):
         assert np.array_equal(outs[0][f], outs[1][f]), f
+
+
+def test_mixed_form_residual_over_lists():
+    """The precision form's FP64 residual walks the same lists (3D): against
+    the per-cell residual the FP32 right-hand side can differ in its last bit,
+    so the two runs agree to FP32 level, and both stay within the form's
+    bound against the plain FP64 step."""
+    s = G.settings_spheres_3d(iter_max=20, outer_max=4, inner_sweeps=5)
+    shape = (48, 40, 36)
+    vals = G.spheres_3d(*shape, count=5, seed=9)
+    with Case(s, shape, vals) as c:
+        c.initial_conditions()
+        c.step(6)
+        ref = c.get_state()
+    out = {}
+    for path in ("auto", "cells"):
+        with Case(s.replace(precision="mixed", sor_path=path), shape, vals) as c:
+            assert c.sor_info()["listed"] == (path == "auto")
+            c.initial_conditions()
+            c.step(6)
+            out[path] = c.get_state()
+    for f in ("u", "v", "w", "p"):
+        assert rel_l2(out["auto"][f], out["cells"][f]) < 1e-6, f
+        for path in out:
+            assert rel_l2(out[path][f], ref[f]) < 1e-4, (path, f)
