@@ -149,6 +149,18 @@ def grid_nu(nu: float, h: float, u: float = 1.0, cell_re: float = 2.0) -> float:
     return max(nu, u * h / cell_re)
 
 
+def _fit_streamwise(a: float, b: float, cx: float, width: float) -> Tuple[float, float, float]:
+    """Semi-axes scaled so the larger is at most width/4 and the centre moved
+    so the obstacle (a circle of its larger semi-axis) stays width/10 clear
+    of the inlet and outlet; unchanged when it already fits."""
+    r = max(a, b)
+    rmax = 0.25 * width
+    if r > rmax:
+        a, b, r = a * rmax / r, b * rmax / r, rmax
+    lo, hi = r + 0.1 * width, width - r - 0.1 * width
+    return a, b, min(max(cx, lo), hi)
+
+
 @dataclasses.dataclass
 class BatchCase2D:
     m: int
@@ -163,7 +175,7 @@ class BatchCase2D:
 def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
                    sizes: Sequence[int] = tuple(range(64, 513, 32)),
                    iter_max: int = 100, threshold: float = 0.1, cell_re: Optional[float] = 2.0,
-                   dt_rule: str = "stable") -> List[BatchCase2D]:
+                   dt_rule: str = "stable", fit_streamwise: bool = True) -> List[BatchCase2D]:
     """Independent 2D cases of uneven size: nx, ny from `sizes`, 1-4 circles or
     ellipses with semi-axes 0.02-0.1 of the height at random angles, Re uniform
     in [50, 400] (nu = U*D/Re with D twice the first obstacle's larger
@@ -182,7 +194,13 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
       of the cases still diverge with threshold 0.1;
     * `dt_rule`: "stable" takes CFL 0.2 of the predictor's full stability
       limit (`cfl_dt`); "cfl" the plain advective 0.2*h/U, which diverges
-      for most cases."""
+      for most cases;
+    * `fit_streamwise`: in domains much shorter than high (nx = 64 with ny
+      up to 512) an obstacle of 0.1 height reaches the inlet and outlet rows,
+      and those cases diverge even with the two choices above; its semi-axes
+      are then scaled so its largest one is at most a quarter of the width
+      and its centre kept a tenth of the width clear of both ends
+      (`_fit_streamwise`).  The random draws are the same either way."""
     rng = np.random.default_rng(seed)
     cases = []
     for _ in range(count):
@@ -200,6 +218,8 @@ def batch_cases_2d(count: int = 512, seed: int = 0, steps: int = 500,
             ang = float(rng.uniform(0.0, np.pi))
             cx = float(rng.uniform(0.2, 0.8)) * width
             cy = float(rng.uniform(0.2, 0.8)) * height
+            if fit_streamwise:
+                a, b, cx = _fit_streamwise(a, b, cx, width)
             shapes.append((cx, cy, a, b, ang))
         re = float(rng.uniform(50.0, 400.0))
         d_ref = 2.0 * max(shapes[0][2], shapes[0][3])
