@@ -235,7 +235,7 @@ def _plain_sequential(items, steps: int):
 
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
                 baseline_steps: int = 20, large_cells: int = 100000, plain_value: float = 0.0,
-                schedule_bound: float = 1e-5):
+                schedule_bound: float = 5e-5):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
     {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
     Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit,
@@ -441,8 +441,13 @@ def run_ours(args):
     achieved = alg_bytes / (sor_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     fused = args.precision == "mixed" and prof["sor_launches"] == sweeps * prof["steps"]
-    kernel = "k_sor_half" if args.precision == "fp64" else ("k_sor_fused3" if fused else "k_sor_dc4")
-    kname = f"{'sor_fused' if fused else 'sor_half'}_{args.precision}_{args.workload}"
+    listed = case.sor_info()["listed"]
+    if args.precision == "fp64":
+        kernel = "k_sor_list3" if listed else "k_sor_half"
+    else:
+        kernel = "k_sor_fused3" if fused else "k_sor_dc4"
+    form = "sor_fused" if fused else ("sor_list" if (listed and args.precision == "fp64") else "sor_half")
+    kname = f"{form}_{args.precision}_{args.workload}"
     traffic = ncu_traffic(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
@@ -450,14 +455,23 @@ def run_ours(args):
                 "sor_share_of_step": prof["sor_ms"] / prof["step_ms"], "avg_launch_ms": sor_launch_ms,
                 "algorithmic_bytes_per_launch": alg_bytes}
     if args.precision == "fp64":
-        # The FP64 sweep is bound by the FP64 units (2 FMA/clk/SM on GB300), not by
-        # HBM: 7 FMAs per cell update (6 neighbours, the (1-w) p term) = 14 flops.
+        # The FP64 roof (2 FMA/clk/SM on GB300): the reference's update is 7 FMAs
+        # per cell (6 neighbours, the (1-w) p term) = 14 flops.  The list sweep
+        # does 2 FMAs for a pure-fluid cell (the neighbour sum is exact integer
+        # arithmetic), so its rate on the reference's flop count is "effective"
+        # and can exceed the DGEMM roof.
         fp64_peak = fp64_peak_tflops()
         flops = cells / 2 * 14
         alu = flops / (sor_launch_ms / 1e3) / 1e12
         roofline["fp64_alu"] = {"achieved": alu, "peak": fp64_peak, "unit": "TFLOP/s", "frac": alu / fp64_peak,
-                                "flops_per_launch": flops, "peak_source": "cuBLAS DGEMM 4096^3 measured live"}
-        roofline["binding"] = "fp64_alu" if alu / fp64_peak > achieved / peak else "hbm"
+                                "flops_per_launch": flops, "peak_source": "cuBLAS DGEMM 4096^3 measured live",
+                                "counting": "effective (reference's 14 flops per update)" if listed else
+                                            "executed"}
+        if listed:
+            roofline["binding"] = "hbm"
+            roofline["fluid_cells"] = case.sor_info()["fluid"]
+        else:
+            roofline["binding"] = "fp64_alu" if alu / fp64_peak > achieved / peak else "hbm"
 
     # ---- end to end through the C ABI with host buffers ----------------------
     host = case.get_state()
@@ -477,17 +491,22 @@ def run_ours(args):
         case.step(1)
         case.get_state(out)
     barrier(world)
+    calls_a, calls_b = [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        ta = time.perf_counter()
         case.step_host(host, out)
+        calls_a.append(1e3 * (time.perf_counter() - ta))
     t1 = time.perf_counter()
     e2e_s = reduce_max(t1 - t0, world)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        ta = time.perf_counter()
         case.set_state(host["u"], host["v"], host["p"], host.get("w"))
         case.step(1)
         case.get_state(out)
+        calls_b.append(1e3 * (time.perf_counter() - ta))
     t1 = time.perf_counter()
     three_s = reduce_max(t1 - t0, world)
     for a in list(host.values()) + list(out.values()):
@@ -495,7 +514,11 @@ def run_ours(args):
     nbytes = sum(a.nbytes for a in host.values())
     e2e = {"value": world * cells * args.steps / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes, "call": "pf_step_host",
-           "three_calls": world * cells * args.steps / three_s / 1e6}
+           "three_calls": world * cells * args.steps / three_s / 1e6,
+           "per_call_ms": {"pf_step_host": {"median": statistics.median(calls_a), "min": min(calls_a),
+                                            "max": max(calls_a)},
+                           "three_calls": {"median": statistics.median(calls_b), "min": min(calls_b),
+                                           "max": max(calls_b)}}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
@@ -580,7 +603,7 @@ def main():
     ap.add_argument("--serving-rates", default="0.5,1,2",
                     help="serving form at these arrival rates (requests/s); empty to skip")
     ap.add_argument("--rate-requests", type=int, default=32, help="requests per arrival rate")
-    ap.add_argument("--schedule-bound", type=float, default=1e-5,
+    ap.add_argument("--schedule-bound", type=float, default=5e-5,
                     help="precision form: the autotuner's bound on the relative L2 error against FP64 when it "
                          "picks the outer x inner schedule")
     args = ap.parse_args()

@@ -253,7 +253,8 @@ typedef struct pf_batch_options {
                                 graph, captured once per composition (cases
                                 per dimension, shared memory, launch shape)
                                 and replayed by later calls of the same
-                                composition; the large cases replay their own
+                                composition (the last 16 compositions are
+                                kept); the large cases replay their own
                                 step graphs.  0: plain launches */
   int32_t reserved[6];
 } pf_batch_options;

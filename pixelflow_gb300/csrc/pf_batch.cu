@@ -373,15 +373,21 @@ struct pf_batch {
   // The persistent part of a call (descriptor upload + one launch per
   // dimension) as a CUDA graph: the descriptors are staged in pinned host
   // memory, which the graph's copy nodes read when it runs, so a graph fits
-  // every call with the same composition (key) and is captured again when
-  // the composition changes.
+  // every call with the same composition (key).  The graphs of the last
+  // kGraphCache compositions are kept (least recently used replaced), so
+  // calls that alternate between a few compositions replay them.
   CaseDesc* h_desc = nullptr;
   int* h_order = nullptr;
   int* h_misc = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  long long gkey[6] = {-1, -1, -1, -1, -1, -1};  // n2, n3, smem2, cluster, threads, grid clusters
+  struct Graph {
+    long long key[6];  // n2, n3, smem2, cluster, threads, grid clusters
+    cudaGraphExec_t exec;
+    int64_t used;
+  };
+  std::vector<Graph> graphs;
   int64_t graphs_captured = 0, graph_replays = 0;
 };
+static const size_t kGraphCache = 16;
 
 // Launch shape of one dimension's persistent kernel: the function attributes
 // (shared memory, non-portable cluster size) and the number of co-resident
@@ -533,7 +539,7 @@ int pf_batch_destroy(pf_batch* b) {
     if (c) pf_destroy(c);
   for (auto e : b->case_ev)
     if (e) cudaEventDestroy(e);
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (auto& gr : b->graphs) cudaGraphExecDestroy(gr.exec);
   cudaFree(b->d_desc);
   cudaFree(b->d_order);
   cudaFree(b->d_misc);
@@ -760,11 +766,10 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
     } else {
       const long long key[6] = {n2, n3, (long long)smem2, b->opt.cluster, b->opt.threads,
                                 (long long)ncl2 * 65536 + ncl3};
-      if (!b->gexec || std::memcmp(key, b->gkey, sizeof(key)) != 0) {
-        if (b->gexec) {
-          cudaGraphExecDestroy(b->gexec);
-          b->gexec = nullptr;
-        }
+      pf_batch::Graph* hit = nullptr;
+      for (auto& gr : b->graphs)
+        if (std::memcmp(key, gr.key, sizeof(key)) == 0) hit = &gr;
+      if (!hit) {
         PF_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
         rc = enqueue_persistent(b, n2, n3, smem2, ncl2, ncl3);
         cudaGraph_t graph = nullptr;
@@ -774,18 +779,28 @@ int pf_batch_step_slots(pf_batch* b, const int* slots, const int* nsteps, int n)
           return rc;
         }
         if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture(batch)");
-        const cudaError_t ei = cudaGraphInstantiate(&b->gexec, graph, 0);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) {
-          b->gexec = nullptr;
-          return cuda_fail(ei, "cudaGraphInstantiate(batch)");
+        if (ei != cudaSuccess) return cuda_fail(ei, "cudaGraphInstantiate(batch)");
+        if (b->graphs.size() >= kGraphCache) {  // replace the least recently used
+          auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                      [](const pf_batch::Graph& x, const pf_batch::Graph& y) { return x.used < y.used; });
+          cudaGraphExecDestroy(lru->exec);
+          b->graphs.erase(lru);
         }
-        std::memcpy(b->gkey, key, sizeof(key));
+        pf_batch::Graph gr;
+        std::memcpy(gr.key, key, sizeof(key));
+        gr.exec = exec;
+        gr.used = 0;
+        b->graphs.push_back(gr);
+        hit = &b->graphs.back();
         b->graphs_captured++;
       } else {
         b->graph_replays++;
       }
-      PF_CUDA(cudaGraphLaunch(b->gexec, b->st));
+      hit->used = b->graphs_captured + b->graph_replays;
+      PF_CUDA(cudaGraphLaunch(hit->exec, b->st));
     }
     b->launches += (n2 ? 1 : 0) + (n3 ? 1 : 0);
   }
