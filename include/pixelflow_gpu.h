@@ -93,9 +93,7 @@ typedef struct pf_options {
                               cell with its own six stored coefficients.  The
                               same red-black iterates up to the rounding of
                               the fluid cells' neighbour sum */
-  int32_t sor_cells;       /* the list walk's cells per thread and loop
-                              iteration, 1 or 2 (0: the library's choice);
-                              same results */
+  int32_t reserved[1];
 } pf_options;
 
 enum { PF_SWEEP_AUTO = 0, PF_SWEEP_SPLIT = 1, PF_SWEEP_FUSED = 2 };

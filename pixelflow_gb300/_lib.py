@@ -41,7 +41,7 @@ class PfOptions(ctypes.Structure):
         ("precision", ctypes.c_int32), ("outer_max", ctypes.c_int32), ("inner_sweeps", ctypes.c_int32),
         ("track_sor_error", ctypes.c_int32), ("dc_tol", ctypes.c_double), ("use_graph", ctypes.c_int32),
         ("sweep_form", ctypes.c_int32), ("fused_rows", ctypes.c_int32), ("fused_planes", ctypes.c_int32),
-        ("sor_path", ctypes.c_int32), ("sor_cells", ctypes.c_int32),
+        ("sor_path", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1),
     ]
 
 

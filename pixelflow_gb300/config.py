@@ -31,7 +31,7 @@ GROUPS = {
 }
 GPU_GROUP = "gpu_control"
 GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls",
-            "sweep_form", "fused_rows", "fused_planes", "sor_path", "sor_cells"]
+            "sweep_form", "fused_rows", "fused_planes", "sor_path"]
 WALL_FACES = ("top", "bottom", "east", "west", "north", "south")
 
 
@@ -80,7 +80,6 @@ class Settings:
     # (exact neighbour sum, no coefficient loads for them); "cells" updates
     # every cell with its own stored coefficients
     sor_path: str = "auto"
-    sor_cells: int = 0               # the list walk's cells per thread (0: library default)
     # inflow and initial velocities scaled by porosity: the boundary and initial
     # conditions of ibm_2d_backstep_omp_cpu.f90 (:533-534, :615-618)
     inflow_porosity: bool = False

@@ -445,8 +445,6 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "fused_rows and fused_planes must be >= 0");
   if (rc == PF_OK && c->opt.sor_path != PF_SOR_AUTO && c->opt.sor_path != PF_SOR_CELLS)
     rc = fail(PF_E_INVALID, "unknown sor_path");
-  if (rc == PF_OK && (c->opt.sor_cells < 0 || c->opt.sor_cells > 2))
-    rc = fail(PF_E_INVALID, "sor_cells must be 0, 1 or 2");
   if (rc != PF_OK) {
     delete c;
     return rc;
@@ -484,7 +482,6 @@ static int finish_setup(pf_case* c) {
   if (rc) return rc;
   PF_CUDA(cudaStreamSynchronize(c->st));
   if (c->opt.sor_path == PF_SOR_AUTO && sor_list_eligible(g)) {
-    c->list_cells = c->opt.sor_cells > 0 ? c->opt.sor_cells : kListCellsDefault;
     rc = sor_list_setup(c);
     if (rc) return rc;
     c->use_list = true;

@@ -60,7 +60,6 @@ struct pf_case {
   int list_nfluid[2] = {0, 0}, list_ntotal[2] = {0, 0};  // cells per colour: fluid, all
   int list_nchunks[2] = {0, 0};                            // chunks of 32 entries per colour
   int list_grid = 0;                                       // CTAs of the persistent launch
-  int list_cells = 1;                                      // cells per thread and loop iteration (1, 2)
   double list_const[6] = {0, 0, 0, 0, 0, 0};  // the fluid cells' normalised coefficients
   bool list_iso = false;                        // all six equal (dx = dy = dz)
 
@@ -104,8 +103,6 @@ void enqueue_boundary_mixed(pf_case* c);
 int geometry_to_stage(pf_case* c, const pf_shape* shapes, int nshapes, double edge);
 // The list-driven plain sweep (3D, no walls, sizes that pack into 32 bits).
 bool sor_list_eligible(const Geo& g);
-// cells per thread of the list walk when pf_options.sor_cells is 0
-constexpr int kListCellsDefault = 1;
 size_t sor_list_bytes(const Geo& g);
 int sor_list_setup(pf_case* c);
 void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool early,

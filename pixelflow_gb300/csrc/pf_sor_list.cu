@@ -184,12 +184,11 @@ __device__ __forceinline__ idx_t list_cell(unsigned e, const ListOffsets& o, idx
   return q;
 }
 
-// sum_nb a_nb p_nb of one cell subtracted from tt: the exact sum times the
-// fluid constant for a fluid cell (ISO), the three constants, or the cell's
-// own coefficients c.
+// sum_nb a_nb p_nb of one cell: the exact sum times the fluid constant for a
+// fluid cell (ISO), the three constants, or the cell's own coefficients.
 template <bool ISO>
-__device__ __forceinline__ double list_stencil(bool fl, const double (&x)[6], const double (&c)[6], double tt,
-                                               double ax, double ay, double az) {
+__device__ __forceinline__ double list_stencil(bool fl, const double (&x)[6], const Coef<double>& C, idx_t q,
+                                               double tt, double ax, double ay, double az) {
   if (fl) {
     if (ISO) {
       double sum;
@@ -203,50 +202,20 @@ __device__ __forceinline__ double list_stencil(bool fl, const double (&x)[6], co
     tt = fma(-az, x[4], tt);
     return fma(-az, x[5], tt);
   }
+  double c[6];
+#pragma unroll
+  for (int d = 0; d < 6; d++) c[d] = C.a[d][q];
 #pragma unroll
   for (int d = 0; d < 6; d++) tt = fma(-c[d], x[d], tt);
   return tt;
 }
 
-// The operands of NC cells (one entry each), all loads issued before any
-// arithmetic: a cell's own value and RHS, its six neighbours and, for a cell
-// that is not fluid, its six coefficients.
-template <int NC>
-struct ListOperands {
-  idx_t q[NC];
-  bool act[NC], fl[NC];
-  double b[NC], p[NC], x[NC][6], c[NC][6];
-};
-template <int NC>
-__device__ __forceinline__ void list_load(const unsigned (&e)[NC], const ListOffsets& o, const Coef<double>& C,
-                                          const double* __restrict__ pc, const double* __restrict__ po,
-                                          ListOperands<NC>& L) {
-#pragma unroll
-  for (int k = 0; k < NC; k++) {
-    L.act[k] = e[k] != LIST_NONE;
-    L.fl[k] = (e[k] >> LIST_FLUID) & 1u;
-    if (L.act[k]) {
-      idx_t nb[6];
-      L.q[k] = list_cell(e[k], o, nb);
-      L.b[k] = C.bbn[L.q[k]];
-      L.p[k] = pc[L.q[k]];
-#pragma unroll
-      for (int d = 0; d < 6; d++) L.x[k][d] = po[nb[d]];
-      if (!L.fl[k]) {
-#pragma unroll
-        for (int d = 0; d < 6; d++) L.c[k][d] = C.a[d][L.q[k]];
-      }
-    }
-  }
-}
-
-// One half-sweep over the chunked list of one colour: warp w takes NC
-// chunks w, w + W, ..., w + (NC-1) W per iteration (W warps in the grid),
-// one entry of each per lane, loads the next iteration's entries first,
-// then all operands of its NC cells, then updates them.  ISO: the six fluid
+// One half-sweep over the chunked list of one colour: warp w takes chunks
+// w, w + W, ... (W warps in the grid), one entry per lane, and loads the
+// next chunk's entry before working on the current one.  ISO: the six fluid
 // constants are equal (dx = dy = dz); otherwise the fluid cells use the
 // three constants with FP64 FMAs (still without coefficient loads).
-template <bool TRACK, bool ISO, int NC>
+template <bool TRACK, bool ISO>
 __global__ void __launch_bounds__(LIST_THREADS)
     k_sor_list3(Geo g, Coef<double> C, double* __restrict__ pc, const double* __restrict__ po, double omw,
                 const unsigned* __restrict__ list, int nchunks, double ax, double ay, double az,
@@ -254,34 +223,30 @@ __global__ void __launch_bounds__(LIST_THREADS)
   const int lane = threadIdx.x & 31;
   const int W = gridDim.x * (LIST_THREADS / 32);
   int w = blockIdx.x * (LIST_THREADS / 32) + (threadIdx.x >> 5);
-  unsigned e[NC];
-#pragma unroll
-  for (int k = 0; k < NC; k++) e[k] = w + k * W < nchunks ? list[(size_t)(w + k * W) * 32 + lane] : LIST_NONE;
+  unsigned e = w < nchunks ? list[(size_t)w * 32 + lane] : LIST_NONE;
   pdl_begin();
   if (skip && *skip) return;
   const ListOffsets o = list_offsets(g);
   unsigned long long emax = 0;
-  for (; w < nchunks; w += NC * W) {
-    unsigned en[NC];
+  for (; w < nchunks; w += W) {
+    const unsigned en = w + W < nchunks ? list[(size_t)(w + W) * 32 + lane] : LIST_NONE;
+    if (e != LIST_NONE) {
+      idx_t nb[6];
+      const idx_t q = list_cell(e, o, nb);
+      const bool fl = (e >> LIST_FLUID) & 1u;
+      const double cb = C.bbn[q];
+      const double pold = pc[q];
+      double x[6];
 #pragma unroll
-    for (int k = 0; k < NC; k++) {
-      const int wn = w + (NC + k) * W;
-      en[k] = wn < nchunks ? list[(size_t)wn * 32 + lane] : LIST_NONE;
-    }
-    ListOperands<NC> L;
-    list_load<NC>(e, o, C, pc, po, L);
-#pragma unroll
-    for (int k = 0; k < NC; k++) {
-      if (!L.act[k]) continue;
-      const double pnew = fma(omw, L.p[k], list_stencil<ISO>(L.fl[k], L.x[k], L.c[k], L.b[k], ax, ay, az));
-      pc[L.q[k]] = pnew;
+      for (int d = 0; d < 6; d++) x[d] = po[nb[d]];
+      const double pnew = fma(omw, pold, list_stencil<ISO>(fl, x, C, q, cb, ax, ay, az));
+      pc[q] = pnew;
       if (TRACK) {
-        const unsigned long long b = abs_diff_bits(pnew, L.p[k]);
+        const unsigned long long b = abs_diff_bits(pnew, pold);
         emax = b > emax ? b : emax;
       }
     }
-#pragma unroll
-    for (int k = 0; k < NC; k++) e[k] = en[k];
+    e = en;
   }
   if (TRACK) warp_max_atomic(emax, err);
 }
@@ -289,8 +254,8 @@ __global__ void __launch_bounds__(LIST_THREADS)
 // The precision form's FP64 residual over the same lists, r = bbn - omega p -
 // sum_nb a_nb p_nb (normalised by omega/ap), stored as the FP32 right-hand
 // side of the correction sweeps; zeroes the cell's correction and reduces
-// max |r|.  Same walk as the sweep.
-template <bool ISO, int NC>
+// max |r|.
+template <bool ISO>
 __global__ void __launch_bounds__(LIST_THREADS)
     k_residual_list3(Geo g, Coef<double> C, const double* __restrict__ pc, const double* __restrict__ po,
                      double omega, const unsigned* __restrict__ list, int nchunks, double ax, double ay, double az,
@@ -299,34 +264,28 @@ __global__ void __launch_bounds__(LIST_THREADS)
   const int lane = threadIdx.x & 31;
   const int W = gridDim.x * (LIST_THREADS / 32);
   int w = blockIdx.x * (LIST_THREADS / 32) + (threadIdx.x >> 5);
-  unsigned e[NC];
-#pragma unroll
-  for (int k = 0; k < NC; k++) e[k] = w + k * W < nchunks ? list[(size_t)(w + k * W) * 32 + lane] : LIST_NONE;
+  unsigned e = w < nchunks ? list[(size_t)w * 32 + lane] : LIST_NONE;
   pdl_begin();
   if (skip && *skip) return;
   const ListOffsets o = list_offsets(g);
   unsigned long long rm = 0;
-  for (; w < nchunks; w += NC * W) {
-    unsigned en[NC];
+  for (; w < nchunks; w += W) {
+    const unsigned en = w + W < nchunks ? list[(size_t)(w + W) * 32 + lane] : LIST_NONE;
+    if (e != LIST_NONE) {
+      idx_t nb[6];
+      const idx_t q = list_cell(e, o, nb);
+      const bool fl = (e >> LIST_FLUID) & 1u;
+      double x[6];
 #pragma unroll
-    for (int k = 0; k < NC; k++) {
-      const int wn = w + (NC + k) * W;
-      en[k] = wn < nchunks ? list[(size_t)wn * 32 + lane] : LIST_NONE;
-    }
-    ListOperands<NC> L;
-    list_load<NC>(e, o, C, pc, po, L);
-#pragma unroll
-    for (int k = 0; k < NC; k++) {
-      if (!L.act[k]) continue;
-      double tt = list_stencil<ISO>(L.fl[k], L.x[k], L.c[k], L.b[k], ax, ay, az);
-      tt = fma(-omega, L.p[k], tt);
-      rf[L.q[k]] = (float)tt;
-      ec[L.q[k]] = 0.0f;
+      for (int d = 0; d < 6; d++) x[d] = po[nb[d]];
+      double tt = list_stencil<ISO>(fl, x, C, q, C.bbn[q], ax, ay, az);
+      tt = fma(-omega, pc[q], tt);
+      rf[q] = (float)tt;
+      ec[q] = 0.0f;
       const unsigned long long b = abs_bits(tt);
       rm = b > rm ? b : rm;
     }
-#pragma unroll
-    for (int k = 0; k < NC; k++) e[k] = en[k];
+    e = en;
   }
   warp_max_atomic(rm, rmax);
 }
@@ -443,14 +402,9 @@ int sor_list_setup(pf_case* c) {
   PF_CUDA(cudaGetDevice(&dev));
   PF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 1 << 20;
-  const int nc = c->list_cells;
-  for (const void* k :
-       {nc == 2 ? (const void*)k_sor_list3<true, true, 2> : (const void*)k_sor_list3<true, true, 1>,
-        nc == 2 ? (const void*)k_sor_list3<false, true, 2> : (const void*)k_sor_list3<false, true, 1>,
-        nc == 2 ? (const void*)k_sor_list3<true, false, 2> : (const void*)k_sor_list3<true, false, 1>,
-        nc == 2 ? (const void*)k_sor_list3<false, false, 2> : (const void*)k_sor_list3<false, false, 1>,
-        nc == 2 ? (const void*)k_residual_list3<true, 2> : (const void*)k_residual_list3<true, 1>,
-        nc == 2 ? (const void*)k_residual_list3<false, 2> : (const void*)k_residual_list3<false, 1>}) {
+  for (const void* k : {(const void*)k_sor_list3<true, true>, (const void*)k_sor_list3<false, true>,
+                        (const void*)k_sor_list3<true, false>, (const void*)k_sor_list3<false, false>,
+                        (const void*)k_residual_list3<true>, (const void*)k_residual_list3<false>}) {
     int n = 0;
     PF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, LIST_THREADS, 0));
     per_sm = std::min(per_sm, n);
@@ -465,36 +419,28 @@ int sor_list_setup(pf_case* c) {
 void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool /*early*/,
                      cudaStream_t st) {
   const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
-#define PF_SL(TR, ISO, NC)                                                                                      \
-  launch_pdl(k_sor_list3<TR, ISO, NC>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col], c->p[col],  \
+#define PF_SL(TR, ISO)                                                                                          \
+  launch_pdl(k_sor_list3<TR, ISO>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col], c->p[col],      \
              (const double*)c->p[1 - col], omw, (const unsigned*)c->list[col], c->list_nchunks[col], ax, ay, az, \
              err, (const int*)nullptr)
-  if (c->list_cells == 2) {
-    if (c->list_iso)
-      err ? PF_SL(true, true, 2) : PF_SL(false, true, 2);
-    else
-      err ? PF_SL(true, false, 2) : PF_SL(false, false, 2);
-  } else {
-    if (c->list_iso)
-      err ? PF_SL(true, true, 1) : PF_SL(false, true, 1);
-    else
-      err ? PF_SL(true, false, 1) : PF_SL(false, false, 1);
-  }
+  if (c->list_iso)
+    err ? PF_SL(true, true) : PF_SL(false, true);
+  else
+    err ? PF_SL(true, false) : PF_SL(false, false);
 #undef PF_SL
 }
 
 void launch_residual_list(const pf_case* c, int col, float* rf, float* ec, unsigned long long* rmax, const int* skip,
                           cudaStream_t st) {
   const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
-#define PF_RL(ISO, NC)                                                                                       \
-  launch_pdl(k_residual_list3<ISO, NC>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],         \
-             (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col], \
-             c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip)
-  if (c->list_cells == 2)
-    c->list_iso ? PF_RL(true, 2) : PF_RL(false, 2);
+  if (c->list_iso)
+    launch_pdl(k_residual_list3<true>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+               (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
+               c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
   else
-    c->list_iso ? PF_RL(true, 1) : PF_RL(false, 1);
-#undef PF_RL
+    launch_pdl(k_residual_list3<false>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+               (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
+               c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
 }
 
 }  // namespace pf

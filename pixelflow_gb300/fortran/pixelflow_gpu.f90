@@ -30,7 +30,7 @@ module pixelflow_gpu
     integer(c_int32_t) :: fused_rows
     integer(c_int32_t) :: fused_planes
     integer(c_int32_t) :: sor_path
-    integer(c_int32_t) :: sor_cells
+    integer(c_int32_t) :: reserved(1)
   end type pf_options
 
   interface

@@ -61,7 +61,6 @@ def make_options(s: Settings, use_graph: bool = True) -> PfOptions:
     if path not in SOR_PATHS:
         raise ValueError(f"unknown sor_path {s.sor_path!r}")
     o.sor_path = SOR_PATHS[path]
-    o.sor_cells = int(s.sor_cells)
     return o
 
 

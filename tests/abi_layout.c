@@ -21,7 +21,7 @@ int main(int argc, char **argv) {
   F(pf_params, inflow_porosity); F(pf_params, wall_mode); F(pf_params, walls);
   F(pf_options, precision); F(pf_options, outer_max); F(pf_options, inner_sweeps);
   F(pf_options, track_sor_error); F(pf_options, dc_tol); F(pf_options, use_graph); F(pf_options, sweep_form);
-  F(pf_options, fused_rows); F(pf_options, fused_planes); F(pf_options, sor_path); F(pf_options, sor_cells);
+  F(pf_options, fused_rows); F(pf_options, fused_planes); F(pf_options, sor_path); F(pf_options, reserved);
   F(pf_shape, kind); F(pf_shape, reserved); F(pf_shape, cx); F(pf_shape, cy); F(pf_shape, cz);
   F(pf_shape, a); F(pf_shape, b); F(pf_shape, angle);
   F(pf_batch_options, cluster); F(pf_batch_options, threads); F(pf_batch_options, max_cases);

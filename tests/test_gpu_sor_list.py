@@ -195,21 +195,3 @@ def test_mixed_form_residual_over_lists():
         assert rel_l2(out["auto"][f], out["cells"][f]) < 1e-6, f
         for path in out:
             assert rel_l2(out[path][f], ref[f]) < 1e-4, (path, f)
-
-
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_cells_per_thread_give_the_same_bits(precision):
-    """One or two list entries per thread and loop iteration change only the
-    order in which the cells of one colour are updated: the same bits."""
-    s = G.settings_spheres_3d(iter_max=20, outer_max=4, inner_sweeps=5, precision=precision)
-    shape = (40, 36, 30)
-    vals = G.spheres_3d(*shape, count=4, seed=6)
-    outs = []
-    for cells in (1, 2):
-        with Case(s.replace(sor_cells=cells), shape, vals) as c:
-            c.initial_conditions()
-            c.step(5)
-            outs.append((c.get_state(), c.norms()))
-    for f in ("u", "v", "w", "p"):
-        assert np.array_equal(outs[0][0][f], outs[1][0][f]), f
-    assert outs[0][1] == outs[1][1]
