@@ -59,7 +59,7 @@ struct pf_case {
   size_t list_bytes = 0;
   int list_nfluid[2] = {0, 0}, list_ntotal[2] = {0, 0};  // cells per colour: fluid, all
   int list_nchunks[2] = {0, 0};                            // chunks of 32 entries per colour
-  int list_grid = 0;                                       // CTAs of the persistent launch
+  int list_grid[3] = {0, 0, 0};  // CTAs of the persistent launches: sweep, tracked sweep, residual
   double list_const[6] = {0, 0, 0, 0, 0, 0};  // the fluid cells' normalised coefficients
   bool list_iso = false;                        // all six equal (dx = dy = dz)
 

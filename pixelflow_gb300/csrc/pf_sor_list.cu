@@ -396,23 +396,23 @@ int sor_list_setup(pf_case* c) {
   c->list_iso = bits(consts[0]) == bits(consts[1]) && bits(consts[0]) == bits(consts[2]) &&
                 bits(consts[0]) == bits(consts[3]) && bits(consts[0]) == bits(consts[4]) &&
                 bits(consts[0]) == bits(consts[5]);
-  // one wave of persistent CTAs (the fewest resident of the sweep's and the
-  // residual's variants), no more than the chunks need
+  // one wave of persistent CTAs per kernel (the untracked sweep holds fewer
+  // registers than the tracked one: 5 CTAs per SM against 4 at 256 threads),
+  // no more than the chunks need
   int dev = 0, sms = 0;
   PF_CUDA(cudaGetDevice(&dev));
   PF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  int per_sm = 1 << 20;
-  for (const void* k : {(const void*)k_sor_list3<true, true>, (const void*)k_sor_list3<false, true>,
-                        (const void*)k_sor_list3<true, false>, (const void*)k_sor_list3<false, false>,
-                        (const void*)k_residual_list3<true>, (const void*)k_residual_list3<false>}) {
-    int n = 0;
-    PF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, LIST_THREADS, 0));
-    per_sm = std::min(per_sm, n);
-  }
-  per_sm = std::max(1, per_sm);
   const long long need = ((long long)std::max(c->list_nchunks[0], c->list_nchunks[1]) + LIST_THREADS / 32 - 1) /
                          (LIST_THREADS / 32);
-  c->list_grid = (int)std::max(1LL, std::min<long long>((long long)sms * per_sm, need));
+  const bool iso = c->list_iso;
+  const void* kern[3] = {iso ? (const void*)k_sor_list3<false, true> : (const void*)k_sor_list3<false, false>,
+                         iso ? (const void*)k_sor_list3<true, true> : (const void*)k_sor_list3<true, false>,
+                         iso ? (const void*)k_residual_list3<true> : (const void*)k_residual_list3<false>};
+  for (int v = 0; v < 3; v++) {
+    int per_sm = 0;
+    PF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern[v], LIST_THREADS, 0));
+    c->list_grid[v] = (int)std::max(1LL, std::min<long long>((long long)sms * std::max(1, per_sm), need));
+  }
   return PF_OK;
 }
 
@@ -420,7 +420,8 @@ void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* 
                      cudaStream_t st) {
   const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
 #define PF_SL(TR, ISO)                                                                                          \
-  launch_pdl(k_sor_list3<TR, ISO>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col], c->p[col],      \
+  launch_pdl(k_sor_list3<TR, ISO>, dim3(c->list_grid[TR ? 1 : 0]), dim3(LIST_THREADS), st, c->g, c->C[col],     \
+             c->p[col],                                                                                         \
              (const double*)c->p[1 - col], omw, (const unsigned*)c->list[col], c->list_nchunks[col], ax, ay, az, \
              err, (const int*)nullptr)
   if (c->list_iso)
@@ -434,11 +435,11 @@ void launch_residual_list(const pf_case* c, int col, float* rf, float* ec, unsig
                           cudaStream_t st) {
   const double ax = c->list_const[0], ay = c->list_const[2], az = c->list_const[4];
   if (c->list_iso)
-    launch_pdl(k_residual_list3<true>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+    launch_pdl(k_residual_list3<true>, dim3(c->list_grid[2]), dim3(LIST_THREADS), st, c->g, c->C[col],
                (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
                c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
   else
-    launch_pdl(k_residual_list3<false>, dim3(c->list_grid), dim3(LIST_THREADS), st, c->g, c->C[col],
+    launch_pdl(k_residual_list3<false>, dim3(c->list_grid[2]), dim3(LIST_THREADS), st, c->g, c->C[col],
                (const double*)c->p[col], (const double*)c->p[1 - col], c->s.omega, (const unsigned*)c->list[col],
                c->list_nchunks[col], ax, ay, az, rf, ec, rmax, skip);
 }
