@@ -265,7 +265,11 @@ __device__ __forceinline__ void c_divergence(Geo g, Scal s, const T* __restrict_
   }
 }
 
-template <typename T, typename TS, int DIM>
+// FLUID: the caller has found gx = gy = gz = damp = 0 for this cell (every
+// cell of its warp): the porosity-gradient terms and the non-slip damping
+// multiply zeros, so they are left out (the same values, up to the sign of a
+// zero sum).
+template <typename T, typename TS, int DIM, bool FLUID = false>
 __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__ uo,
                                                       const T* __restrict__ vo, const T* __restrict__ wo,
                                                       const T* __restrict__ div, const T* __restrict__ gxa,
@@ -331,33 +335,45 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
     // u
     T conv = fma(wc, duz, fma(vc, duy, uc * dux));
     T lap = fma(luz, iz2, fma(luy, iy2, lux * ix2));
-    T por = fma(duz + dwx, gz, fma(duy + dvx, gy, (dux + dux) * gx)) * nu;
-    por = fma(lam * dc, gx, por);
     T t = -dt * conv;
     t = fma(dtnu, lap, t);
     t = fma(dtnl, (dE - dW) * hx, t);
-    t = fma(rv, por, t);
-    u[q] = su[q] + (TS)fma(-uc, dp * ix2, t);
+    if (FLUID) {
+      u[q] = su[q] + (TS)t;
+    } else {
+      T por = fma(duz + dwx, gz, fma(duy + dvx, gy, (dux + dux) * gx)) * nu;
+      por = fma(lam * dc, gx, por);
+      t = fma(rv, por, t);
+      u[q] = su[q] + (TS)fma(-uc, dp * ix2, t);
+    }
     // v
     conv = fma(wc, dvz, fma(vc, dvy, uc * dvx));
     lap = fma(lvz, iz2, fma(lvy, iy2, lvx * ix2));
-    por = fma(dvz + dwy, gz, fma(dvy + dvy, gy, (dvx + duy) * gx)) * nu;
-    por = fma(lam * dc, gy, por);
     t = -dt * conv;
     t = fma(dtnu, lap, t);
     t = fma(dtnl, (dN - dS) * hy, t);
-    t = fma(rv, por, t);
-    v[q] = sv[q] + (TS)fma(-vc, dp * iy2, t);
+    if (FLUID) {
+      v[q] = sv[q] + (TS)t;
+    } else {
+      T por = fma(dvz + dwy, gz, fma(dvy + dvy, gy, (dvx + duy) * gx)) * nu;
+      por = fma(lam * dc, gy, por);
+      t = fma(rv, por, t);
+      v[q] = sv[q] + (TS)fma(-vc, dp * iy2, t);
+    }
     // w
     conv = fma(wc, dwz, fma(vc, dwy, uc * dwx));
     lap = fma(lwz, iz2, fma(lwy, iy2, lwx * ix2));
-    por = fma(dwz + dwz, gz, fma(dwy + dvz, gy, (dwx + duz) * gx)) * nu;
-    por = fma(lam * dc, gz, por);
     t = -dt * conv;
     t = fma(dtnu, lap, t);
     t = fma(dtnl, (dT - dB) * hz, t);
-    t = fma(rv, por, t);
-    w[q] = sw[q] + (TS)fma(-wc, dp * iz2, t);
+    if (FLUID) {
+      w[q] = sw[q] + (TS)t;
+    } else {
+      T por = fma(dwz + dwz, gz, fma(dwy + dvz, gy, (dwx + duz) * gx)) * nu;
+      por = fma(lam * dc, gz, por);
+      t = fma(rv, por, t);
+      w[q] = sw[q] + (TS)fma(-wc, dp * iz2, t);
+    }
   }
   keep_ghosts<TS, DIM>(g, i, j, k, q, su, sv, sw, u, v, w);
 }

@@ -155,7 +155,29 @@ __global__ void __launch_bounds__(BX* BY) k_predictor(Geo g, Scal s, const T* __
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = (DIM == 3) ? blockIdx.z + 1 + k0 : 0;
-  if (i > g.m || j > g.n) return;
+  const bool in = i <= g.m && j <= g.n;
+  if (DIM == 3) {
+    // A warp is one x-row of BX = 32 cells.  Where every cell of it has zero
+    // porosity gradients and no non-slip damping (fluid away from the
+    // obstacles), the porosity terms of all three components vanish and the
+    // warp takes the shorter path: about a third fewer FP64 operations.  The
+    // vote runs before any lane leaves; lanes past the grid count as fluid.
+    bool fl = true;
+    if (in) {
+      const idx_t q = nat_idx(g, i, j, k);
+      fl = gxa[q] == T(0) && gya[q] == T(0) && gza[q] == T(0) && dampa[q] == T(0);
+    }
+    const bool all = __all_sync(0xffffffffu, fl);
+    if (!in) return;
+    if (all)
+      c_predictor<T, TS, DIM, true>(g, s, uo, vo, wo, div, gxa, gya, gza, rinva, dampa, su, sv, sw, u, v, w, i, j,
+                                    k);
+    else
+      c_predictor<T, TS, DIM, false>(g, s, uo, vo, wo, div, gxa, gya, gza, rinva, dampa, su, sv, sw, u, v, w, i, j,
+                                     k);
+    return;
+  }
+  if (!in) return;
   c_predictor<T, TS, DIM>(g, s, uo, vo, wo, div, gxa, gya, gza, rinva, dampa, su, sv, sw, u, v, w, i, j, k);
 }
 
