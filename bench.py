@@ -285,7 +285,7 @@ def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed:
 
 def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: int = 25,
                   baseline_steps: int = 20, large_cells: int = 100000, policy: str = "srpt_fill",
-                  plain_value: float = 0.0):
+                  plain_value: float = 0.0, schedule_bound: float = 0.0):
     """The serving form: `count` requests with Poisson arrivals (mean `rate`
     per second), 70 % 2D (128^2-1024^2) / 30 % 3D (64^3-192^3, 4-16 spheres),
     100-1000 steps each, admitted by a 150 GB HBM budget into one resident
@@ -297,14 +297,23 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
     from pixelflow_gb300 import geometry as G
     from pixelflow_gb300.serve import Server, summarize
     reqs = G.serving_requests(count=count, rate=rate, seed=seed)
-    t0 = time.perf_counter()
     with Server(chunk=chunk, cluster=8, threads=512, keep_state=False, large_cells=large_cells,
                 policy=policy) as srv:
+        tuned, tune_s = None, 0.0
+        if schedule_bound > 0:
+            # the autotuner's schedule per 3D size (set-up, before the stream starts)
+            tt = time.perf_counter()
+            tuned = srv.tune_schedules(reqs, schedule_bound)
+            tune_s = time.perf_counter() - tt
+        t0 = time.perf_counter()
         res = srv.run(reqs, realtime=True)
         wall = time.perf_counter() - t0
         summ = summarize(res, wall)
         summ.update(rounds=srv.rounds, device_ms=srv.device_ms, peak_device_bytes=srv.peak_bytes, policy=policy,
                     max_waiting=srv.max_waiting)
+        if tuned is not None:
+            summ["schedules"] = {"bound": schedule_bound, "tune_s": tune_s, "by_size": tuned,
+                                 "other_sizes": "4 x 25"}
     summ["workload"] = (f"{count} requests, Poisson {rate:g}/s, 70% 2D 128^2-1024^2 / 30% 3D 64^3-192^3, "
                         f"100-1000 steps, 150 GB budget, chunk {chunk}, large cases > {large_cells} cells "
                         f"on own streams, round policy {policy}")
@@ -317,7 +326,7 @@ def bench_serving(count: int = 32, rate: float = 200.0, seed: int = 0, chunk: in
     return summ
 
 
-def bench_serving_rates(rates=(0.5, 1.0, 2.0), count: int = 32, seed: int = 0):
+def bench_serving_rates(rates=(0.5, 1.0, 2.0), count: int = 32, seed: int = 0, schedule_bound: float = 0.0):
     """The serving form at sustainable arrival rates: per rate, `count`
     requests of the same mix; p50/p99 latency, the aggregate, the longest
     queue, and the latency growth (mean latency of the last quarter of the
@@ -328,8 +337,10 @@ def bench_serving_rates(rates=(0.5, 1.0, 2.0), count: int = 32, seed: int = 0):
         from pixelflow_gb300 import geometry as G
         from pixelflow_gb300.serve import Server, summarize
         reqs = G.serving_requests(count=count, rate=r, seed=seed)
-        t0 = time.perf_counter()
         with Server(chunk=25, cluster=8, threads=512, keep_state=False, policy="srpt_fill") as srv:
+            if schedule_bound > 0:
+                srv.tune_schedules(reqs, schedule_bound)  # cached from the first tuning
+            t0 = time.perf_counter()
             res = srv.run(reqs, realtime=True)
             wall = time.perf_counter() - t0
             summ = summarize(res, wall)
@@ -577,11 +588,14 @@ def run_ours(args):
         if not args.no_batch:
             line["forms"]["batch2d_512"] = bench_batch(steps=args.steps, plain_value=value,
                                                        schedule_bound=args.schedule_bound)
-            line["forms"]["serving"] = bench_serving(policy="srpt_fill", plain_value=value)
-            line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_steps=0)
+            line["forms"]["serving"] = bench_serving(policy="srpt_fill", plain_value=value,
+                                                     schedule_bound=args.schedule_bound)
+            line["forms"]["serving_round_robin"] = bench_serving(policy="rr", baseline_steps=0,
+                                                                 schedule_bound=args.schedule_bound)
             if args.serving_rates:
                 rates = tuple(float(x) for x in args.serving_rates.split(","))
-                line["forms"]["serving_rates"] = bench_serving_rates(rates, count=args.rate_requests)
+                line["forms"]["serving_rates"] = bench_serving_rates(rates, count=args.rate_requests,
+                                                                     schedule_bound=args.schedule_bound)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s.replace(precision="fp64"), shape, vals)
     barrier(world)

@@ -14,6 +14,8 @@
   rounding of the correction is carried until the next FP64 residual), the
   time with the passes.
 * `tune_batch_schedule`: the same for a batch, on a sample of its cases.
+  The serving loop (`serve.Server.tune_schedules`) runs `tune_schedule` once
+  per 3D grid size of its requests.
 
 Results are cached per machine and workload signature in a JSON file so
 later runs start tuned.
@@ -103,10 +105,17 @@ FUSED_PLANES: Tuple[int, ...] = (0, 32)
 SCHEDULES: Tuple[Tuple[int, int], ...] = ((1, 100), (2, 50), (4, 25), (5, 20), (10, 10), (20, 5))
 
 
-def _case_ms(settings, shape, vals, steps: int) -> float:
-    """Device ms per step of a precision-form case (after one untimed step)."""
+def _open_case(settings, shape, vals=None, shapes=None):
+    """A case from porosity values, or from analytic shapes (generated on the GPU)."""
     from .solver import Case
-    with Case(settings, shape, vals) as c:
+    if shapes is not None:
+        return Case.from_shapes(settings, shape, shapes)
+    return Case(settings, shape, vals)
+
+
+def _case_ms(settings, shape, vals, steps: int, shapes=None) -> float:
+    """Device ms per step of a precision-form case (after one untimed step)."""
+    with _open_case(settings, shape, vals, shapes) as c:
         c.initial_conditions()
         c.step(1)
         c.synchronize()
@@ -152,31 +161,32 @@ def _rel_l2(a, b) -> float:
 
 
 def tune_schedule(settings, shape, vals, bound: float = 1e-4, steps: int = 5, schedules=SCHEDULES,
-                  use_cache: bool = True) -> Tuple[Tuple[int, int], List[dict]]:
+                  use_cache: bool = True, shapes=None) -> Tuple[Tuple[int, int], List[dict]]:
     """The fastest outer x inner schedule of the precision form whose
     pressure (and velocity) error against the plain FP64 step after `steps`
     steps from the initial state stays within `bound` (relative L2).  When
-    no candidate meets the bound, the most accurate one is returned."""
-    from .solver import Case
+    no candidate meets the bound, the most accurate one is returned.  The
+    case comes from porosity values `vals` or, with `shapes`, from analytic
+    shapes generated on the GPU."""
     it = int(settings.iter_max)
     cands = [(o, i) for (o, i) in schedules if o * i == it]
-    sig = f"schedule:{tuple(shape)}:{it}:{bound:g}:{steps}"
+    sig = f"schedule:{tuple(shape)}:{it}:{bound:g}:{steps}:{cands}"
     cache = _load() if use_cache else {}
     if use_cache and sig in cache:
         return tuple(cache[sig]["best"]), cache[sig]["trials"]
-    with Case(settings.replace(precision="fp64"), shape, vals) as c:
+    with _open_case(settings.replace(precision="fp64"), shape, vals, shapes) as c:
         c.initial_conditions()
         c.step(steps)
         ref = c.get_state()
     trials = []
     for (o, i) in cands:
         s = settings.replace(precision="mixed", outer_max=o, inner_sweeps=i)
-        with Case(s, shape, vals) as c:
+        with _open_case(s, shape, vals, shapes) as c:
             c.initial_conditions()
             c.step(steps)
             got = c.get_state()
         err = {f: _rel_l2(got[f], ref[f]) for f in ref}
-        ms = _case_ms(s, shape, vals, 2)
+        ms = _case_ms(s, shape, vals, 2, shapes)
         trials.append({"outer": o, "inner": i, "ms": ms, "rel_l2": err, "within_bound": max(err.values()) <= bound})
     ok = [t for t in trials if t["within_bound"]]
     pick = min(ok, key=lambda t: t["ms"]) if ok else min(trials, key=lambda t: max(t["rel_l2"].values()))

@@ -80,6 +80,9 @@ class Server:
                  max_cases: int = 1024, keep_state: bool = True, edge: float = 1.0, large_cells: int = 100000,
                  policy: str = "rr", round_cells: int = 24_000_000, batch=None, round_ms: float = 200.0,
                  round_rate: float = 2.6e9):
+        # precision-form schedule (outer, inner) per (dim, shape), set by
+        # tune_schedules; requests of other sizes keep their own settings
+        self.schedules: Dict[Tuple[int, Tuple[int, ...]], Tuple[int, int]] = {}
         if policy not in ("rr", "srpt", "srpt_fill"):
             raise ValueError(f"unknown policy {policy!r}")
         self.large_cells = large_cells
@@ -107,6 +110,30 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
+    def tune_schedules(self, requests: List[Request], bound: float, steps: int = 5,
+                       schedules=((1, 100), (2, 50), (4, 25)), use_cache: bool = True) -> Dict[str, list]:
+        """The autotuner's outer x inner schedule for every 3D grid size among
+        `requests` (79 % of the serving mix's work; those cases run as
+        full-GPU step graphs): the fastest candidate whose error against the
+        plain FP64 step after `steps` steps stays within `bound`, tuned on the
+        first request of that size.  Later admissions of that size use it."""
+        from .autotune import tune_schedule
+        out = {}
+        for r in requests:
+            key = (r.dim, tuple(r.shape))
+            if r.dim != 3 or key in self.schedules:
+                continue
+            best, trials = tune_schedule(r.settings, r.shape, None, bound=bound, steps=steps, schedules=schedules,
+                                         use_cache=use_cache, shapes=to_pf_shapes(r.shapes, r.dim))
+            self.schedules[key] = tuple(best)
+            out[f"3D {r.shape[0]}"] = [list(best), [[t["outer"], t["inner"], round(t["ms"], 3),
+                                                     max(t["rel_l2"].values())] for t in trials]]
+        return out
+
+    def _settings(self, r: Request):
+        sch = self.schedules.get((r.dim, tuple(r.shape)))
+        return r.settings if sch is None else r.settings.replace(outer_max=sch[0], inner_sweeps=sch[1])
+
     def run(self, requests: List[Request], realtime: bool = True) -> List[Result]:
         """Serve `requests` (sorted by arrival).  With realtime=True arrivals
         follow the wall clock from the start of the call; otherwise every
@@ -131,7 +158,8 @@ class Server:
             while waiting:
                 r = waiting[0]
                 try:
-                    slot = self.batch.add_shapes(r.settings, r.shape, to_pf_shapes(r.shapes, r.dim), self.edge)
+                    slot = self.batch.add_shapes(self._settings(r), r.shape, to_pf_shapes(r.shapes, r.dim),
+                                                 self.edge)
                 except PfError as e:
                     if e.code in (-3, -7):  # over budget / no slot: wait for a case to finish
                         break
