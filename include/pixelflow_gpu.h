@@ -343,12 +343,6 @@ int pf_debug_step_host_plan(int l, int *slabs, int capacity);
  * colour c (either array may be NULL). */
 int pf_sor_info(pf_case *c, int *listed, int fluid[2], int total[2]);
 
-/* The precision form's FP32 split sweep (no reference counterpart): each
- * thread updates a chunk of 4 packed cells, and a chunk whose porosity
- * operands are all 1.0f skips their loads.  fluid[c] / chunks[c] = such
- * chunks and all chunks of colour c.  PF_E_STATE for a plain FP64 case. */
-int pf_dc_fluid_info(pf_case *c, int fluid[2], int chunks[2]);
-
 /* Testing of the exact six-term sum of the list sweep's fluid cells (no
  * reference counterpart): out[i] = x[6i] + ... + x[6i+5] rounded once to
  * FP64, ok[i] = 0 where an input is Inf/NaN or the sum is not a normal

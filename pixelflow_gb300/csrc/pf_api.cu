@@ -1120,20 +1120,4 @@ int pf_sor_info(pf_case* c, int* listed, int fluid[2], int total[2]) {
   return PF_OK;
 }
 
-int pf_dc_fluid_info(pf_case* c, int fluid[2], int chunks[2]) {
-  if (!c || !fluid || !chunks) return fail(PF_E_INVALID, "null argument");
-  if (c->opt.precision != PF_PREC_MIXED) return fail(PF_E_STATE, "pf_dc_fluid_info: not the precision form");
-  const int words = dc_fluid_words(c->g);
-  std::vector<unsigned> h((size_t)words);
-  for (int col = 0; col < 2; col++) {
-    PF_CUDA(cudaMemcpyAsync(h.data(), c->dcfl[col], (size_t)words * sizeof(unsigned), cudaMemcpyDeviceToHost, c->st));
-    PF_CUDA(cudaStreamSynchronize(c->st));
-    int n = 0;
-    for (unsigned w : h) n += __builtin_popcount(w);
-    fluid[col] = n;
-    chunks[col] = (int)(((long long)((c->g.m >> 1) / 4 + 1)) * c->g.n * (c->g.dim == 3 ? c->g.l : 1));
-  }
-  return PF_OK;
-}
-
 }  // extern "C"

@@ -567,9 +567,7 @@ int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
   const int d = g.dim;
   size_t b = nat8 * (6 + (d == 3) + 2 * d) + pk8 * (2 + 2 * (2 * d + 3));
   b += r256((size_t)(g.m + 2) * (g.n + 2) * g.Z * 8) + RED_TOTAL * sizeof(unsigned long long);
-  if (mixed)
-    b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * (mixed_fused(g, *opt) ? 8 : 6) + 256 +
-         2 * r256((size_t)dc_fluid_words(g) * sizeof(unsigned));
+  if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * (mixed_fused(g, *opt) ? 8 : 6) + 256;
   // the cell lists of the 3D sweep and residual: one 32-bit entry per cell
   if (sor_list_eligible(g) && (!opt || opt->sor_path == PF_SOR_AUTO)) b += sor_list_bytes(g);
   *bytes = b;

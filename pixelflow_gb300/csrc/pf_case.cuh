@@ -79,8 +79,6 @@ struct pf_case {
   float sweep_ms[2] = {0.f, 0.f};  // PF_SWEEP_AUTO: ms per sweep measured at creation (split, fused)
   float* rf[2] = {nullptr, nullptr};    // packed FP32 normalised residual (RHS of the sweeps)
   float* epsf[2] = {nullptr, nullptr};  // packed FP32 porosity (operator rebuilt on the fly)
-  // per colour, one bit per chunk of the split sweep: all its porosity operands are 1.0f
-  unsigned* dcfl[2] = {nullptr, nullptr};
   int* skip = nullptr;                  // device flag: defect correction converged
 
   int64_t sor_launches_per_step() const {

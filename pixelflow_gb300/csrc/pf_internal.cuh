@@ -163,15 +163,10 @@ void launch_zero_int(int* p, cudaStream_t st);
 void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cudaStream_t st);
 // The FP32 split sweep (one colour); early: its grid fits one wave (see
 // dc_one_wave), so its fixed operands load before the dependency wait.
-// `fluid` (nullable): the colour's bitmap of chunks whose porosity operands
-// are all 1.0f (launch_dc_fluid_bits, dc_fluid_words 32-bit words).
 bool dc_one_wave(const Geo& g, int sms);
-int dc_fluid_words(const Geo& g);
-void launch_dc_fluid_bits(const Geo& g, const float* epsc, const float* epso, int colour, unsigned* out,
-                          cudaStream_t st);
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
-                   const float* eo, int colour, const unsigned* fluid, unsigned long long* err, const int* skip,
-                   bool early, cudaStream_t st);
+                   const float* eo, int colour, unsigned long long* err, const int* skip, bool early,
+                   cudaStream_t st);
 // Fused full correction sweep (both colours in one launch, 3D with even n
 // and l): launch shape chosen once per case.
 struct FusedShape {

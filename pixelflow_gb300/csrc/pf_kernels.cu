@@ -579,89 +579,11 @@ __device__ __forceinline__ VecF<V> dc_chunk(const Geo& g, const DCConst& K, int 
   return out;
 }
 
-// The porosity operands of one chunk (own slots PC; the other colour's
-// same slots PO plus the slot before or after them px; rows north/south PN,
-// PS; planes top/bottom PT, PB).  A chunk whose bit is set in the case's
-// fluid bitmap had every one of these equal to 1.0f at set-up (the
-// operator is time-invariant), so it takes 1.0f without the loads: the same
-// arithmetic on the same values, 24 of the chunk's 44 loaded bytes per
-// update skipped.
-template <int DIM, int V>
-struct DCPoro {
-  VecF<V> PC, PO, PN, PS, PT, PB;
-  float px;
-};
-template <int DIM, int V>
-__device__ __forceinline__ void dc_poro_load(const Geo& g, const float* __restrict__ epsc,
-                                             const float* __restrict__ epso, idx_t q, int s, DCPoro<DIM, V>& P) {
-  const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
-  P.PC = ldv<V>(epsc + q);
-  P.PO = ldv<V>(epso + q);
-  P.px = s ? epso[q + V] : epso[q - 1];
-  P.PN = ldv<V>(epso + q + H);
-  P.PS = ldv<V>(epso + q - H);
-  if (DIM == 3) {
-    P.PT = ldv<V>(epso + q + HY);
-    P.PB = ldv<V>(epso + q - HY);
-  } else {
-    P.PT = VecF<V>{};
-    P.PB = VecF<V>{};
-  }
-}
-template <int DIM, int V>
-__device__ __forceinline__ void dc_poro_ones(DCPoro<DIM, V>& P) {
-#pragma unroll
-  for (int u = 0; u < V; u++) {
-    P.PC.a[u] = P.PO.a[u] = P.PN.a[u] = P.PS.a[u] = 1.f;
-    P.PT.a[u] = P.PB.a[u] = DIM == 3 ? 1.f : 0.f;
-  }
-  P.px = 1.f;
-}
-// Chunk t of a colour's launch (the mapping of k_sor_dc4): its row, first
-// slot h0, colour side s and packed index q.
-template <int DIM>
-__device__ __forceinline__ void dc_chunk_at(const Geo& g, int colour, int chunks, int t, int V, int& j, int& k,
-                                            int& h0, int& s, idx_t& q) {
-  const int row = t / chunks;
-  h0 = (t - row * chunks) * V;
-  k = DIM == 3 ? row / g.n + 1 : 0;
-  j = DIM == 3 ? row - (k - 1) * g.n + 1 : row + 1;
-  s = (colour + j + (DIM == 3 ? k : 1)) & 1;
-  q = pk_idx(g, h0, j, k);
-}
-
-// Set-up: bit t of word t/32 marks chunk t of colour `colour` whose
-// porosity operands (dc_poro_load) are all exactly 1.0f.
-template <int DIM, int V>
-__global__ void __launch_bounds__(DC4_THREADS) k_dc_fluid_bits(Geo g, const float* __restrict__ epsc,
-                                                               const float* __restrict__ epso, int colour,
-                                                               int chunks, int words, unsigned* __restrict__ out) {
-  const int t = blockIdx.x * DC4_THREADS + threadIdx.x;
-  const int rows = DIM == 3 ? g.n * g.l : g.n;
-  bool fl = false;
-  if (t < chunks * rows) {
-    int j, k, h0, s;
-    idx_t q;
-    dc_chunk_at<DIM>(g, colour, chunks, t, V, j, k, h0, s, q);
-    DCPoro<DIM, V> P;
-    dc_poro_load<DIM, V>(g, epsc, epso, q, s, P);
-    fl = P.px == 1.f;
-#pragma unroll
-    for (int u = 0; u < V; u++) {
-      fl = fl && P.PC.a[u] == 1.f && P.PO.a[u] == 1.f && P.PN.a[u] == 1.f && P.PS.a[u] == 1.f;
-      if (DIM == 3) fl = fl && P.PT.a[u] == 1.f && P.PB.a[u] == 1.f;
-    }
-  }
-  const unsigned b = __ballot_sync(0xffffffffu, fl);  // every lane reaches this (no early return)
-  if ((threadIdx.x & 31) == 0 && (t >> 5) < words) out[t >> 5] = b;
-}
-
 template <int DIM, bool TRACK, int V>
-__global__ void __launch_bounds__(DC4_THREADS, TRACK ? 3 : 4) k_sor_dc4(Geo g, DCConst K, const float* __restrict__ epsc,
+__global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const float* __restrict__ epsc,
                                                          const float* __restrict__ epso,
                                                          const float* __restrict__ r, float* __restrict__ ec,
                                                          const float* __restrict__ eo, int colour, int chunks,
-                                                         const unsigned* __restrict__ fluid,
                                                          unsigned long long* __restrict__ err,
                                                          const int* __restrict__ skip) {
   pdl_begin();
@@ -670,29 +592,31 @@ __global__ void __launch_bounds__(DC4_THREADS, TRACK ? 3 : 4) k_sor_dc4(Geo g, D
   const int rows = DIM == 3 ? g.n * g.l : g.n;
   unsigned e = 0;
   if (t < chunks * rows) {
-    int j, k, h0, s;
-    idx_t q;
-    dc_chunk_at<DIM>(g, colour, chunks, t, V, j, k, h0, s, q);
+    const int row = t / chunks;
+    const int h0 = (t - row * chunks) * V;
+    const int k = DIM == 3 ? row / g.n + 1 : 0;
+    const int j = DIM == 3 ? row - (k - 1) * g.n + 1 : row + 1;
+    const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
     const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
+    const idx_t q = pk_idx(g, h0, j, k);
     const idx_t qn = (j == g.n) ? pk_idx(g, h0, g.jn_n, k) : q + H;
     const idx_t qs = (j == 1) ? pk_idx(g, h0, g.js_1, k) : q - H;
-    const VecF<V> EC = ldv<V>(ec + q), R = ldv<V>(r + q), XO = ldv<V>(eo + q);
+    const VecF<V> EC = ldv<V>(ec + q), R = ldv<V>(r + q), PC = ldv<V>(epsc + q);
+    const VecF<V> XO = ldv<V>(eo + q), PO = ldv<V>(epso + q);
     const float xx = s ? eo[q + V] : eo[q - 1];
-    const VecF<V> XN = ldv<V>(eo + qn), XS = ldv<V>(eo + qs);
-    VecF<V> XT{}, XB{};
+    const float px = s ? epso[q + V] : epso[q - 1];
+    const VecF<V> XN = ldv<V>(eo + qn), XS = ldv<V>(eo + qs), PN = ldv<V>(epso + q + H), PS = ldv<V>(epso + q - H);
+    VecF<V> XT{}, XB{}, PT{}, PB{};
     if (DIM == 3) {
       const idx_t qt = (k == g.l) ? pk_idx(g, h0, j, g.kt_l) : q + HY;
       const idx_t qb = (k == 1) ? pk_idx(g, h0, j, g.kb_1) : q - HY;
       XT = ldv<V>(eo + qt);
       XB = ldv<V>(eo + qb);
+      PT = ldv<V>(epso + q + HY);
+      PB = ldv<V>(epso + q - HY);
     }
-    DCPoro<DIM, V> P;
-    if (fluid && ((fluid[t >> 5] >> (t & 31)) & 1u))
-      dc_poro_ones<DIM, V>(P);
-    else
-      dc_poro_load<DIM, V>(g, epsc, epso, q, s, P);
-    *reinterpret_cast<VecF<V>*>(ec + q) = dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, P.PC, XO, P.PO, xx, P.px, XN,
-                                                                  XS, P.PN, P.PS, XT, XB, P.PT, P.PB, e);
+    *reinterpret_cast<VecF<V>*>(ec + q) =
+        dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, PC, XO, PO, xx, px, XN, XS, PN, PS, XT, XB, PT, PB, e);
   }
   if (TRACK) warp_max_atomic(e, err);
 }
@@ -709,24 +633,31 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4_early(Geo g, DCConst K,
                                                                const float* __restrict__ epso,
                                                                const float* __restrict__ r, float* __restrict__ ec,
                                                                const float* __restrict__ eo, int colour, int chunks,
-                                                               const unsigned* __restrict__ fluid,
                                                                unsigned long long* __restrict__ err,
                                                                const int* __restrict__ skip) {
   const int t = blockIdx.x * DC4_THREADS + threadIdx.x;
   const int rows = DIM == 3 ? g.n * g.l : g.n;
   const bool act = t < chunks * rows;
-  int j, k, h0, s;
-  idx_t q;
-  dc_chunk_at<DIM>(g, colour, chunks, act ? t : 0, V, j, k, h0, s, q);
+  const int row = act ? t / chunks : 0;
+  const int h0 = (t - row * chunks) * V;
+  const int k = DIM == 3 ? row / g.n + 1 : 0;
+  const int j = DIM == 3 ? row - (k - 1) * g.n + 1 : row + 1;
+  const int s = (colour + j + (DIM == 3 ? k : 1)) & 1;
   const idx_t H = g.H, HY = (idx_t)g.H * g.Y;
-  VecF<V> R{};
-  DCPoro<DIM, V> P;
+  const idx_t q = pk_idx(g, h0, j, k);
+  VecF<V> R{}, PC{}, PO{}, PN{}, PS{}, PT{}, PB{};
+  float px = 0.f;
   if (act) {
     R = ldv<V>(r + q);
-    if (fluid && ((fluid[t >> 5] >> (t & 31)) & 1u))
-      dc_poro_ones<DIM, V>(P);
-    else
-      dc_poro_load<DIM, V>(g, epsc, epso, q, s, P);
+    PC = ldv<V>(epsc + q);
+    PO = ldv<V>(epso + q);
+    px = s ? epso[q + V] : epso[q - 1];
+    PN = ldv<V>(epso + q + H);
+    PS = ldv<V>(epso + q - H);
+    if (DIM == 3) {
+      PT = ldv<V>(epso + q + HY);
+      PB = ldv<V>(epso + q - HY);
+    }
   }
   pdl_begin();
   if (skip && *skip) return;
@@ -744,8 +675,8 @@ __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4_early(Geo g, DCConst K,
       XT = ldv<V>(eo + qt);
       XB = ldv<V>(eo + qb);
     }
-    *reinterpret_cast<VecF<V>*>(ec + q) = dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, P.PC, XO, P.PO, xx, P.px, XN,
-                                                                  XS, P.PN, P.PS, XT, XB, P.PT, P.PB, e);
+    *reinterpret_cast<VecF<V>*>(ec + q) =
+        dc_chunk<DIM, TRACK, V>(g, K, h0, s, EC, R, PC, XO, PO, xx, px, XN, XS, PN, PS, XT, XB, PT, PB, e);
   }
   if (TRACK) warp_max_atomic(e, err);
 }
@@ -1303,20 +1234,12 @@ static DCConst dc_const(const Geo& g, const Scal& sc) {
   return make_dc_const(sc.dt, sc.dx, sc.dy, sc.dz, g.dim, sc.omega);
 }
 
-// chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
-// 4 beat 2 and 8 per thread at 256^3 (1547 vs 1336 and 1508 Mcell-steps/s
-// for the step): the extra occupancy of narrower chunks does not pay for
-// their extra instructions, and 8 slots take 126 registers (two CTAs per SM)
-constexpr int DC_V = 4;
-static long long dc_threads(const Geo& g) {
-  const int chunks = (g.m >> 1) / DC_V + 1;
-  return (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
-}
-
 // Whether the FP32 split sweep's grid fits one wave of resident CTAs (its
 // fixed operands then load before the dependency wait).
 bool dc_one_wave(const Geo& g, int sms) {
-  const long long blocks = (dc_threads(g) + DC4_THREADS - 1) / DC4_THREADS;
+  const int chunks = (g.m >> 1) / 4 + 1;
+  const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
+  const long long blocks = (threads + DC4_THREADS - 1) / DC4_THREADS;
   int per_sm = 0;
   if (g.dim == 3)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sor_dc4_early<3, true, 4>, DC4_THREADS, 0);
@@ -1325,31 +1248,23 @@ bool dc_one_wave(const Geo& g, int sms) {
   return blocks <= (long long)per_sm * sms;
 }
 
-int dc_fluid_words(const Geo& g) { return (int)((dc_threads(g) + 31) / 32); }
-
-void launch_dc_fluid_bits(const Geo& g, const float* epsc, const float* epso, int colour, unsigned* out,
-                          cudaStream_t st) {
-  const int chunks = (g.m >> 1) / DC_V + 1;
-  const unsigned blocks = (unsigned)((dc_threads(g) + DC4_THREADS - 1) / DC4_THREADS);
-  const int words = dc_fluid_words(g);
-  if (g.dim == 3)
-    k_dc_fluid_bits<3, DC_V><<<blocks, DC4_THREADS, 0, st>>>(g, epsc, epso, colour, chunks, words, out);
-  else
-    k_dc_fluid_bits<2, DC_V><<<blocks, DC4_THREADS, 0, st>>>(g, epsc, epso, colour, chunks, words, out);
-}
-
 void launch_sor_dc(const Geo& g, const Scal& sc, const float* epsc, const float* epso, const float* r, float* ec,
-                   const float* eo, int colour, const unsigned* fluid, unsigned long long* err, const int* skip,
-                   bool early, cudaStream_t st) {
+                   const float* eo, int colour, unsigned long long* err, const int* skip, bool early,
+                   cudaStream_t st) {
   const DCConst K = dc_const(g, sc);
-  constexpr int V = DC_V;
+  // chunks of 4 slots covering h = 0 .. m/2 (the largest h of an interior cell);
+  // 4 beat 2 and 8 per thread at 256^3 (1547 vs 1336 and 1508 Mcell-steps/s
+  // for the step): the extra occupancy of narrower chunks does not pay for
+  // their extra instructions, and 8 slots take 126 registers (two CTAs per SM)
+  constexpr int V = 4;
   const int chunks = (g.m >> 1) / V + 1;
-  const unsigned blocks = (unsigned)((dc_threads(g) + DC4_THREADS - 1) / DC4_THREADS);
+  const long long threads = (long long)chunks * g.n * (g.dim == 3 ? g.l : 1);
+  const unsigned blocks = (unsigned)((threads + DC4_THREADS - 1) / DC4_THREADS);
 #define PF_DC(DIMV, TR)                                                                                          \
   (early ? launch_pdl(k_sor_dc4_early<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo, \
-                      colour, chunks, fluid, err, skip)                                                              \
+                      colour, chunks, err, skip)                                                                     \
          : launch_pdl(k_sor_dc4<DIMV, TR, V>, dim3(blocks), dim3(DC4_THREADS), st, g, K, epsc, epso, r, ec, eo,       \
-                      colour, chunks, fluid, err, skip))
+                      colour, chunks, err, skip))
   if (g.dim == 3) {
     if (err)
       PF_DC(3, true);

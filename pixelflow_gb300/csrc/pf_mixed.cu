@@ -6,9 +6,8 @@
 // residual r (normalised by omega/ap) and every norm.
 // FP32: the velocity stencils (divergence, the predictor's increment, read
 // from an FP32 copy of the state), and the correction sweeps on e, whose
-// operator is rebuilt on the fly from FP32 porosity (k_sor_dc4, 24 bytes per
-// update; chunks whose porosity operands are all 1.0f skip those loads, as
-// marked at set-up in a bitmap per colour).
+// operator is rebuilt on the fly from FP32 porosity (k_sor_dc, 24 bytes per
+// update).
 // Per step: outer_max passes of { r = bbn - w p - sum a p_nb (FP64);
 // inner_sweeps FP32 SOR iterations on e from e = 0; p += e (FP64) }.
 // With outer_max * inner_sweeps == iter_max the passes reproduce the plain
@@ -53,7 +52,7 @@ int mixed_choose_sweep(pf_case* c) {
     for (int it = 0; it < SWEEPS; it++)
       for (int col = 0; col < 2; col++)
         launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
-                      c->dcfl[col], col == 1 ? err : nullptr, nullptr, c->dc_early, st);
+                      col == 1 ? err : nullptr, nullptr, c->dc_early, st);
     cudaEventRecord(ev[1], st);
     for (int it = 0; it < SWEEPS; it++) {
       const float* ea[2] = {it & 1 ? c->e2[0] : c->e[0], it & 1 ? c->e2[1] : c->e[1]};
@@ -104,7 +103,6 @@ int mixed_alloc(pf_case* c) {
     req[nr++] = {&c->rf[col], pk};
     req[nr++] = {&c->epsf[col], pk};
     req[nr++] = {&c->e2[col], fused ? pk : 0};
-    req[nr++] = {reinterpret_cast<float**>(&c->dcfl[col]), (size_t)dc_fluid_words(g) * sizeof(unsigned)};
   }
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -144,8 +142,6 @@ void mixed_setup(pf_case* c) {
   launch_to_float(c->rinv, c->rinvf, n, c->st);
   launch_to_float(c->damp, c->dampf, n, c->st);
   launch_pack_eps(c->g, c->poro, c->epsf[0], c->epsf[1], c->st);
-  for (int col = 0; col < 2; col++)
-    launch_dc_fluid_bits(c->g, c->epsf[col], c->epsf[1 - col], col, c->dcfl[col], c->st);
 }
 
 // FP32 copy of the current FP64 velocity state, read by the stencils.
@@ -206,8 +202,8 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
         for (int col = 0; col < 2; col++) {
           if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
           unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
-          launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
-                        c->dcfl[col], err, skip, c->dc_early, st);
+          launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err,
+                        skip, c->dc_early, st);
         }
       }
     }

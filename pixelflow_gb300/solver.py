@@ -310,15 +310,6 @@ class Case:
         check(self.L.pf_sor_info(self.h, ctypes.byref(li), fl, tot))
         return {"listed": bool(li.value), "fluid": list(fl), "total": list(tot)}
 
-    def dc_fluid_info(self) -> Dict[str, list]:
-        """The precision form's split FP32 sweep: {"fluid": [c0, c1],
-        "chunks": [c0, c1]} -- chunks of 4 cells whose porosity operands are
-        all 1.0f (their loads skipped) and all chunks, per colour."""
-        fl = (ctypes.c_int * 2)()
-        ch = (ctypes.c_int * 2)()
-        check(self.L.pf_dc_fluid_info(self.h, fl, ch))
-        return {"fluid": list(fl), "chunks": list(ch)}
-
     def memory_bytes(self) -> int:
         b = ctypes.c_size_t()
         check(self.L.pf_memory_bytes(self.h, ctypes.byref(b)))

@@ -161,35 +161,3 @@ def test_auto_sweep_form_choice(shape):
         assert info == {"form": "split", "split_ms": 0.0, "fused_ms": 0.0}
     ref = _run(s.replace(sweep_form="split"), shape, vals, 2)[0]
     assert _same(got, ref)
-
-
-def test_split_sweep_fluid_chunks_match_fused_bit_for_bit():
-    """Chunks whose porosity operands are all 1.0f skip those loads in the
-    split sweep (a bitmap made at set-up).  With two small spheres most
-    chunks are such, warps mix both kinds near the spheres, and the fields
-    still equal the fused sweep's (which loads every operand) bit for bit."""
-    shape = (64, 48, 40)
-    vals = G.spheres_3d(*shape, count=2, seed=5)
-    s = G.settings_spheres_3d(precision="mixed", outer_max=2, inner_sweeps=5)
-    with Case(s.replace(sweep_form="split"), shape, vals) as c:
-        info = c.dc_fluid_info()
-    for col in (0, 1):
-        assert 0.3 * info["chunks"][col] < info["fluid"][col] < info["chunks"][col], info
-    split, nsplit, _, _ = _run(s.replace(sweep_form="split"), shape, vals, 4)
-    fused, nfused, _, _ = _run(s.replace(sweep_form="fused"), shape, vals, 4)
-    assert _same(fused, split)
-    assert nfused == nsplit
-
-
-def test_fluid_chunk_bitmap_2d_and_plain_rejected():
-    """The 2D sweep takes the bitmap too (its bits against the persistent
-    batch kernel, which loads every operand, are checked by the batch
-    tests); a plain FP64 case has none."""
-    s = G.settings_cylinder_2d(precision="mixed")
-    with Case(s, (512, 256), G.cylinder_2d()) as c:
-        info = c.dc_fluid_info()
-    assert info["chunks"][0] == (256 // 4 + 1) * 256
-    assert 0.5 * info["chunks"][0] < info["fluid"][0] < info["chunks"][0]
-    with Case(s.replace(precision="fp64"), (512, 256), G.cylinder_2d()) as c:
-        with pytest.raises(Exception):
-            c.dc_fluid_info()
