@@ -456,7 +456,8 @@ def run_ours(args):
     if args.precision == "fp64":
         kernel = "k_sor_list3" if listed else "k_sor_half"
     else:
-        kernel = "k_sor_fused3" if fused else "k_sor_dc4"
+        dc_listed = case.dc_list_info()["listed"]
+        kernel = "k_sor_fused3" if fused else ("k_sor_dc_list3" if dc_listed else "k_sor_dc4")
     form = "sor_fused" if fused else ("sor_list" if (listed and args.precision == "fp64") else "sor_half")
     kname = f"{form}_{args.precision}_{args.workload}"
     traffic = ncu_traffic(kname)

@@ -343,6 +343,13 @@ int pf_debug_step_host_plan(int l, int *slabs, int capacity);
  * colour c (either array may be NULL). */
 int pf_sor_info(pf_case *c, int *listed, int fluid[2], int total[2]);
 
+/* The precision form's split FP32 sweep (no reference counterpart): *listed
+ * = 1 when it walks chunk lists (PF_SOR_AUTO, 3D without walls, grids of
+ * more than one wave of CTAs); fluid[c] / total[c] = the chunks of four
+ * cells whose porosity operands are all 1.0f and all chunks of colour c
+ * (either array may be NULL). */
+int pf_dc_list_info(pf_case *c, int *listed, int fluid[2], int total[2]);
+
 /* Testing of the exact six-term sum of the list sweep's fluid cells (no
  * reference counterpart): out[i] = x[6i] + ... + x[6i+5] rounded once to
  * FP64, ok[i] = 0 where an input is Inf/NaN or the sum is not a normal

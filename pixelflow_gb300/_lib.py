@@ -111,6 +111,7 @@ _PROTOS = {
     "pf_sweep_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "pf_max_div_noalloc": (_I, [ctypes.POINTER(PfParams), _VP, _VP, _VP, _VP, _I, _I, _VP, _VP]),
     "pf_sor_info": (_I, [_VP, ctypes.POINTER(_I), _VP, _VP]),
+    "pf_dc_list_info": (_I, [_VP, ctypes.POINTER(_I), _VP, _VP]),
     "pf_debug_sum6": (_I, [_VP, _I, _VP, _VP]),
     "pf_batch_default_options": (None, [ctypes.POINTER(PfBatchOptions)]),
     "pf_batch_create": (_I, [ctypes.POINTER(PfBatchOptions), ctypes.POINTER(_VP)]),

@@ -261,6 +261,7 @@ static void case_free(pf_case* c) {
   if (c->st_io) cudaStreamDestroy(c->st_io);
   if (c->base) cudaFree(c->base);
   if (c->list_base) cudaFree(c->list_base);
+  if (c->dcl_base) cudaFree(c->dcl_base);
   mixed_free(c);
   if (c->hred) cudaFreeHost(c->hred);
   if (c->snap) cudaFree(c->snap);
@@ -485,6 +486,14 @@ static int finish_setup(pf_case* c) {
     rc = sor_list_setup(c);
     if (rc) return rc;
     c->use_list = true;
+  }
+  // the split FP32 sweep walks chunk lists where its grid is more than one
+  // wave (a one-wave grid loads its fixed operands ahead of the dependency
+  // wait instead, k_sor_dc4_early)
+  if (c->opt.precision == PF_PREC_MIXED && c->opt.sor_path == PF_SOR_AUTO && dc_list_eligible(g) && !c->dc_early) {
+    rc = dc_list_setup(c);
+    if (rc) return rc;
+    c->use_dcl = true;
   }
   if (c->opt.precision == PF_PREC_MIXED) return mixed_choose_sweep(c);
   return PF_OK;
@@ -1107,6 +1116,16 @@ int pf_debug_fused_drop_stage(pf_case* c, int stage) {
 int pf_memory_bytes(pf_case* c, size_t* bytes) {
   if (!c || !bytes) return fail(PF_E_INVALID, "null argument");
   *bytes = c->bytes + c->mixed_bytes + c->list_bytes + (c->iostage ? 3 * dense_bytes(c->g) : 0);
+  return PF_OK;
+}
+
+int pf_dc_list_info(pf_case* c, int* listed, int fluid[2], int total[2]) {
+  if (!c || !listed) return fail(PF_E_INVALID, "null argument");
+  *listed = c->use_dcl ? 1 : 0;
+  for (int col = 0; col < 2; col++) {
+    if (fluid) fluid[col] = c->dcl_fluid[col];
+    if (total) total[col] = c->dcl_total[col];
+  }
   return PF_OK;
 }
 

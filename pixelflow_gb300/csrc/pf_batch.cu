@@ -553,6 +553,13 @@ int pf_batch_destroy(pf_batch* b) {
   return PF_OK;
 }
 
+static int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  return sms;
+}
+
 // Bytes a case of these sizes takes on the device (admission control); the
 // same array list as case_alloc / mixed_alloc.
 int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
@@ -570,6 +577,9 @@ int pf_case_bytes(const pf_params* prm, const pf_options* opt, size_t* bytes) {
   if (mixed) b += nat4 * (d + 1 + 2 + (d == 3) + 2) + pk4 * (mixed_fused(g, *opt) ? 8 : 6) + 256;
   // the cell lists of the 3D sweep and residual: one 32-bit entry per cell
   if (sor_list_eligible(g) && (!opt || opt->sor_path == PF_SOR_AUTO)) b += sor_list_bytes(g);
+  // the chunk lists of the split FP32 sweep (grids of more than one wave)
+  if (mixed && opt->sor_path == PF_SOR_AUTO && dc_list_eligible(g) && !dc_one_wave(g, device_sms()))
+    b += dc_list_bytes(g);
   *bytes = b;
   return PF_OK;
 }

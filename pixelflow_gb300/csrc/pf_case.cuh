@@ -80,6 +80,14 @@ struct pf_case {
   float* rf[2] = {nullptr, nullptr};    // packed FP32 normalised residual (RHS of the sweeps)
   float* epsf[2] = {nullptr, nullptr};  // packed FP32 porosity (operator rebuilt on the fly)
   int* skip = nullptr;                  // device flag: defect correction converged
+  // the split FP32 sweep over chunk lists (3D, pf_dc_list.cu); their bytes
+  // are counted in list_bytes
+  bool use_dcl = false;
+  unsigned* dcl_base = nullptr;
+  unsigned* dcl[2] = {nullptr, nullptr};
+  int dcl_ngroups[2] = {0, 0};                           // groups of 32 entries per colour
+  int dcl_fluid[2] = {0, 0}, dcl_total[2] = {0, 0};      // all-fluid chunks, all chunks
+  int dcl_grid[2] = {0, 0};                              // persistent CTAs: untracked, tracked
 
   int64_t sor_launches_per_step() const {
     if (opt.precision == PF_PREC_MIXED) return (use_fused ? 1LL : 2LL) * opt.outer_max * opt.inner_sweeps;
@@ -107,6 +115,11 @@ size_t sor_list_bytes(const Geo& g);
 int sor_list_setup(pf_case* c);
 void launch_sor_list(const pf_case* c, int col, double omw, unsigned long long* err, bool early,
                      cudaStream_t st);
+// The precision form's split FP32 sweep over chunk lists (3D, no walls).
+bool dc_list_eligible(const Geo& g);
+size_t dc_list_bytes(const Geo& g);
+int dc_list_setup(pf_case* c);
+void launch_sor_dc_list(const pf_case* c, int col, unsigned long long* err, const int* skip, cudaStream_t st);
 // The precision form's FP64 residual over the same lists.
 void launch_residual_list(const pf_case* c, int col, float* rf, float* ec, unsigned long long* rmax, const int* skip,
                           cudaStream_t st);

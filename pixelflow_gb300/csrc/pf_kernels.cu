@@ -537,48 +537,6 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_residual(Geo g, Coef<double> 
 // outside 1 <= i <= m store their old value back.
 constexpr int DC4_THREADS = 256;
 
-// V consecutive floats loaded as one aligned vector access.
-template <int V>
-struct alignas(4 * V) VecF {
-  float a[V];
-};
-template <int V>
-__device__ __forceinline__ VecF<V> ldv(const float* p) {
-  return *reinterpret_cast<const VecF<V>*>(p);
-}
-
-// The V cells of one chunk from its loaded operand rows: own correction EC,
-// residual R and porosity PC; the other colour's correction XO and porosity
-// PO at the same slots plus the one slot before (s = 0) or after (s = 1)
-// them (xx, px); the other colour's rows north/south/top/bottom.  Lanes
-// outside 1 <= i <= m keep their old value.  Every chunked form of the sweep
-// calls this, so they agree bit for bit.
-template <int DIM, bool TRACK, int V>
-__device__ __forceinline__ VecF<V> dc_chunk(const Geo& g, const DCConst& K, int h0, int s, const VecF<V>& EC,
-                                            const VecF<V>& R, const VecF<V>& PC, const VecF<V>& XO,
-                                            const VecF<V>& PO, float xx, float px, const VecF<V>& XN,
-                                            const VecF<V>& XS, const VecF<V>& PN, const VecF<V>& PS,
-                                            const VecF<V>& XT, const VecF<V>& XB, const VecF<V>& PT,
-                                            const VecF<V>& PB, unsigned& e) {
-  VecF<V> out;
-#pragma unroll
-  for (int u = 0; u < V; u++) {
-    const int i = 2 * (h0 + u) + s;
-    const float eold = EC.a[u];
-    // east = other colour at h + s, west at h - 1 + s
-    const float xe = s ? (u < V - 1 ? XO.a[u + 1] : xx) : XO.a[u];
-    const float xw = s ? XO.a[u] : (u > 0 ? XO.a[u - 1] : xx);
-    const float pe = s ? (u < V - 1 ? PO.a[u + 1] : px) : PO.a[u];
-    const float pw = s ? PO.a[u] : (u > 0 ? PO.a[u - 1] : px);
-    const float v = dc_cell<DIM>(K, PC.a[u], pe, pw, PN.a[u], PS.a[u], PT.a[u], PB.a[u], xe, xw, XN.a[u], XS.a[u],
-                                 XT.a[u], XB.a[u], R.a[u], eold, i == 1, i == g.m);
-    const bool in = i >= 1 && i <= g.m;
-    out.a[u] = in ? v : eold;
-    if (TRACK && in) e = max(e, abs_bits(v - eold));
-  }
-  return out;
-}
-
 template <int DIM, bool TRACK, int V>
 __global__ void __launch_bounds__(DC4_THREADS) k_sor_dc4(Geo g, DCConst K, const float* __restrict__ epsc,
                                                          const float* __restrict__ epso,

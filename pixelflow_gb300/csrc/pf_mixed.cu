@@ -50,9 +50,13 @@ int mixed_choose_sweep(pf_case* c) {
   for (int rep = 0; rep < REPEATS; rep++) {
     cudaEventRecord(ev[0], st);
     for (int it = 0; it < SWEEPS; it++)
-      for (int col = 0; col < 2; col++)
-        launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
-                      col == 1 ? err : nullptr, nullptr, c->dc_early, st);
+      for (int col = 0; col < 2; col++) {
+        if (c->use_dcl)
+          launch_sor_dc_list(c, col, col == 1 ? err : nullptr, nullptr, st);
+        else
+          launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col,
+                        col == 1 ? err : nullptr, nullptr, c->dc_early, st);
+      }
     cudaEventRecord(ev[1], st);
     for (int it = 0; it < SWEEPS; it++) {
       const float* ea[2] = {it & 1 ? c->e2[0] : c->e[0], it & 1 ? c->e2[1] : c->e[1]};
@@ -202,8 +206,11 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
         for (int col = 0; col < 2; col++) {
           if (halo) launch_p_halo<float>(g, c->e[0], c->e[1], skip, st);
           unsigned long long* err = (track && (g.dim == 2 || col == 1)) ? &c->red[RED_ERRF] : nullptr;
-          launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err,
-                        skip, c->dc_early, st);
+          if (c->use_dcl)
+            launch_sor_dc_list(c, col, err, skip, st);
+          else
+            launch_sor_dc(g, s, c->epsf[col], c->epsf[1 - col], c->rf[col], c->e[col], c->e[1 - col], col, err,
+                          skip, c->dc_early, st);
         }
       }
     }

@@ -310,6 +310,17 @@ class Case:
         check(self.L.pf_sor_info(self.h, ctypes.byref(li), fl, tot))
         return {"listed": bool(li.value), "fluid": list(fl), "total": list(tot)}
 
+    def dc_list_info(self) -> Dict[str, object]:
+        """The precision form's split FP32 sweep: {"listed": bool, "fluid":
+        [c0, c1], "total": [c0, c1]} -- listed when it walks chunk lists with
+        the all-fluid chunks apart (3D, sor_path "auto", grids of more than
+        one wave)."""
+        li = ctypes.c_int()
+        fl = (ctypes.c_int * 2)()
+        tot = (ctypes.c_int * 2)()
+        check(self.L.pf_dc_list_info(self.h, ctypes.byref(li), fl, tot))
+        return {"listed": bool(li.value), "fluid": list(fl), "total": list(tot)}
+
     def memory_bytes(self) -> int:
         b = ctypes.c_size_t()
         check(self.L.pf_memory_bytes(self.h, ctypes.byref(b)))

@@ -161,3 +161,39 @@ def test_auto_sweep_form_choice(shape):
         assert info == {"form": "split", "split_ms": 0.0, "fused_ms": 0.0}
     ref = _run(s.replace(sweep_form="split"), shape, vals, 2)[0]
     assert _same(got, ref)
+
+
+def test_chunk_list_sweep_matches_fused_bit_for_bit():
+    """On grids of more than one wave of CTAs the split FP32 sweep walks
+    chunk lists (pf_dc_list.cu): the all-fluid chunks in warps of their own,
+    their porosity taken as 1.0f without loads.  Every field must still equal
+    the fused sweep's (which loads every operand) bit for bit, odd m
+    included (the last chunk of a row holds the outlet lane), and the bytes
+    must match the admission count."""
+    from pixelflow_gb300 import _lib
+    from pixelflow_gb300.solver import make_options, make_params
+    import ctypes
+    shape = (131, 128, 96)
+    vals = G.spheres_3d(*shape, count=4, seed=11)
+    s = G.settings_spheres_3d(precision="mixed", outer_max=2, inner_sweeps=5)
+    L = _lib.load()
+    for path in ("auto", "cells"):
+        ss = s.replace(sweep_form="split", sor_path=path)
+        with Case(ss, shape, vals) as c:
+            info = c.dc_list_info()
+            need = ctypes.c_size_t()
+            _lib.check(L.pf_case_bytes(ctypes.byref(make_params(ss, shape)), ctypes.byref(make_options(ss)),
+                                       ctypes.byref(need)))
+            assert c.memory_bytes() == need.value, path
+        assert info["listed"] == (path == "auto"), info
+    chunks = (131 // 2 // 4 + 1) * 128 * 96
+    with Case(s.replace(sweep_form="split"), shape, vals) as c:
+        info = c.dc_list_info()
+    for col in (0, 1):
+        assert 0.3 * chunks < info["fluid"][col] < info["total"][col] <= chunks, info
+    split, nsplit, _, _ = _run(s.replace(sweep_form="split"), shape, vals, 2)
+    fused, nfused, _, _ = _run(s.replace(sweep_form="fused"), shape, vals, 2)
+    assert _same(fused, split)
+    assert nfused == nsplit
+    eager, neager, _, _ = _run(s.replace(sweep_form="split"), shape, vals, 2, use_graph=False)
+    assert _same(eager, split) and neager == nsplit
