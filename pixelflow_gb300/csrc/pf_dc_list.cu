@@ -38,7 +38,10 @@ namespace pf {
 
 namespace {
 
-constexpr int DCL_THREADS = 256;
+// 128 threads per CTA: the tracked sweep holds 96 registers a thread, so
+// 5 CTAs of 4 warps fit an SM where 2 of 8 warps did (256^3: 41.7 -> 40.3 us
+// per launch; a register cap of 80 spills and gains nothing)
+constexpr int DCL_THREADS = 128;
 constexpr int DCL_V = 4;
 constexpr unsigned DCL_Q = 0x00ffffffu;  // chunk index: packed index / 4
 constexpr unsigned DCL_NONE = DCL_Q;     // padding entry: no chunk
