@@ -164,8 +164,9 @@ __global__ void __launch_bounds__(DCL_THREADS)
 }  // namespace
 
 bool dc_list_eligible(const Geo& g) {
-  // chunk index in 24 bits: packed index below 2^26
-  return g.dim == 3 && !g.wall && g.pk < (1LL << 26);
+  // chunk index in 24 bits, below the padding entry's DCL_Q: packed index
+  // below 2^26 - 4
+  return g.dim == 3 && !g.wall && g.pk < (1LL << 26) - 4;
 }
 
 // Device bytes of a case's chunk lists, fixed by the grid: every chunk of
