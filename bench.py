@@ -455,10 +455,11 @@ def run_ours(args):
     listed = case.sor_info()["listed"]
     if args.precision == "fp64":
         kernel = "k_sor_list3" if listed else "k_sor_half"
+        form = "sor_list" if listed else "sor_half"
     else:
         dc_listed = case.dc_list_info()["listed"]
         kernel = "k_sor_fused3" if fused else ("k_sor_dc_list3" if dc_listed else "k_sor_dc4")
-    form = "sor_fused" if fused else ("sor_list" if (listed and args.precision == "fp64") else "sor_half")
+        form = "sor_fused" if fused else ("sor_dc_list" if dc_listed else "sor_half")
     kname = f"{form}_{args.precision}_{args.workload}"
     traffic = ncu_traffic(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
