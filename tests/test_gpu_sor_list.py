@@ -195,3 +195,33 @@ def test_mixed_form_residual_over_lists():
         assert rel_l2(out["auto"][f], out["cells"][f]) < 1e-6, f
         for path in out:
             assert rel_l2(out[path][f], ref[f]) < 1e-4, (path, f)
+
+
+@pytest.mark.parametrize("shape", [(133, 129, 99), (130, 131, 97)])
+def test_mixed_chunk_lists_odd_periodic_sizes(shape):
+    """The precision form's FP32 sweep over chunk lists (pf_dc_list.cu) with
+    odd n or l: the periodic neighbours are ghost rows/planes refreshed before
+    each colour.  Against the per-cell sweep (sor_path "cells", whose FP64
+    residual rounds the fluid cells' neighbour sum differently) the fields
+    agree to FP32 level; both stay within the form's bound of the plain FP64
+    step; the lists are used and hold most chunks as all-fluid."""
+    s = G.settings_spheres_3d(iter_max=20, outer_max=4, inner_sweeps=5)
+    vals = G.spheres_3d(*shape, count=4, seed=13)
+    with Case(s, shape, vals) as c:
+        c.initial_conditions()
+        c.step(4)
+        ref = c.get_state()
+    out = {}
+    for path in ("auto", "cells"):
+        with Case(s.replace(precision="mixed", sor_path=path, sweep_form="split"), shape, vals) as c:
+            info = c.dc_list_info()
+            assert info["listed"] == (path == "auto"), info
+            if path == "auto":
+                assert all(0.3 * t < f < t for f, t in zip(info["fluid"], info["total"])), info
+            c.initial_conditions()
+            c.step(4)
+            out[path] = c.get_state()
+    for f in ("u", "v", "w", "p"):
+        assert rel_l2(out["auto"][f], out["cells"][f]) < 1e-6, f
+        for path in out:
+            assert rel_l2(out[path][f], ref[f]) < 1e-4, (path, f)
