@@ -1,7 +1,8 @@
 """Benchmark of the immersed-boundary step on GB300.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--workload spheres3d_256|spheres3d_384|cylinder2d] [--precision fp64|mixed]
+                [--workload spheres3d_256|spheres3d_384|cylinder2d|cylinder2d_slip]
+                [--precision fp64|mixed]
                 [--sweep-form auto|split|fused]
 
 One step = one time step of the whole case (snapshot, predictor, RHS,
@@ -53,11 +54,13 @@ def workload(name: str, precision: str):
         desc = dict(workload=f"3D ibm3 unit cube {nn}^3, 32 seeded spheres (seed 0), tanh edge 2 cells",
                     grid=list(shape), nu=s.xnue, dt=s.time / s.istep_max, iter_max=s.iter_max,
                     omega=s.relux_factor)
-    elif name == "cylinder2d":
-        s = G.settings_cylinder_2d(precision=precision)
+    elif name in ("cylinder2d", "cylinder2d_slip"):
+        slip = name.endswith("_slip")
+        s = G.settings_cylinder_2d(precision=precision, slip_y=slip)
         shape = (512, 256)
         vals = G.cylinder_2d()
-        desc = dict(workload="2D ibm2 cylinder 512x256, D=0.1 at (0.5,0.5), Re=100", grid=list(shape),
+        desc = dict(workload="2D ibm2 cylinder 512x256, D=0.1 at (0.5,0.5), Re=100"
+                    + (", symmetry (slip) rows top and bottom" if slip else ", periodic y"), grid=list(shape),
                     nu=s.xnue, dt=s.time / s.istep_max, iter_max=s.iter_max, omega=s.relux_factor)
     else:
         raise SystemExit(f"unknown workload {name}")

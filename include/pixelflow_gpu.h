@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 2
+#define PF_ABI_VERSION 3
 
 enum {
   PF_OK = 0,
@@ -64,6 +64,12 @@ typedef struct pf_params {
   int32_t walls[6];        /* wall table, faces top, bottom, east, west,
                               north, south (:10-15): 0 wall, 1 inlet (where
                               porosity >= 0.9), 2 outlet (where >= 0.9) */
+  int32_t slip_y;          /* 1 (2D, plain FP64 only): symmetry rows at j = 1
+                              and j = n (dp/dy = 0, v = 0, u mirrored) in
+                              place of the periodic wrap -- the option the
+                              reference keeps commented out in
+                              boundrary_matrix (ibm_2d_uniform_omp_cpu.f90:
+                              438-450) and boundary (:503-518); 0: periodic */
 } pf_params;
 
 /* Options that only this library reads (the &gpu_control group). */

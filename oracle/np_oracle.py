@@ -39,6 +39,9 @@ class NpCase:
         walls = getattr(s, "walls", None)
         self.wall_mode = self.dim == 3 and walls is not None
         self.walls = tuple(int(x) for x in walls) if self.wall_mode else None
+        # 2D symmetry rows at j = 1 and j = n (ibm_2d_uniform_omp_cpu.f90 keeps
+        # them commented out: :440-450, :512-526)
+        self.slip_y = self.dim == 2 and bool(getattr(s, "slip_y", False))
         # grid.f90:50-52 / :297-300
         self.dx = T(s.width) / T(m - 1)
         self.dy = T(s.height) / T(n - 1)
@@ -167,6 +170,16 @@ class NpCase:
             for a in (u, v, p):
                 a[0, :] = a[n, :]
                 a[n + 1, :] = a[1, :]
+            if self.slip_y:  # :512-526, j = 1 then j = n, columns 1..m
+                I = slice(1, m + 1)
+                u[0, I] = u[2, I]
+                v[1, I] = 0
+                v[0, I] = -v[2, I]
+                p[0, I] = p[2, I]
+                u[n + 1, I] = u[n - 1, I]
+                v[n, I] = 0
+                v[n + 1, I] = -v[n - 1, I]
+                p[n + 1, I] = p[n - 1, I]
         else:
             J, K = slice(1, n + 1), slice(1, l + 1)
             u[K, J, 1] = self.U * T(np.cos(self.aoa / T(1300.) * pi))
@@ -332,6 +345,11 @@ class NpCase:
         for key in ("ae", "aw", "an", "as", "at", "ab"):
             if key in C:
                 C[key][..., -1] = 0
+        if self.slip_y:  # :440-450, rows j = 1 then j = n
+            C["an"][0, :] = C["an"][0, :] + C["as"][0, :]
+            C["as"][0, :] = 0
+            C["as"][-1, :] = C["as"][-1, :] + C["an"][-1, :]
+            C["an"][-1, :] = 0
         return C
 
     def _wall_matrix(self, C):

@@ -33,7 +33,7 @@ class OrParams(ctypes.Structure):
         ("istep_max", ctypes.c_int32), ("iter_max", ctypes.c_int32),
         ("thickness", ctypes.c_double), ("threshold", ctypes.c_double),
         ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("inflow_porosity", ctypes.c_int32),
-        ("wall_mode", ctypes.c_int32), ("walls", ctypes.c_int32 * 6),
+        ("wall_mode", ctypes.c_int32), ("walls", ctypes.c_int32 * 6), ("slip_y", ctypes.c_int32),
     ]
 
 
@@ -44,7 +44,8 @@ def make_params(settings, m: int, n: int, l: int = 1, dim: int = 2) -> OrParams:
                     int(s.istep_max), int(s.iter_max), s.thickness, s.threshold, s.relux_factor,
                     1 if s.nonslip else 0, 1 if getattr(s, "inflow_porosity", False) else 0,
                     1 if getattr(s, "walls", None) is not None else 0,
-                    (ctypes.c_int32 * 6)(*(getattr(s, "walls", None) or (0,) * 6)))
+                    (ctypes.c_int32 * 6)(*(getattr(s, "walls", None) or (0,) * 6)),
+                    1 if getattr(s, "slip_y", False) else 0)
 
 
 def lib():

@@ -30,6 +30,8 @@
  *   3D: src/omp_parallel/ibm_3d_uniform_omp_cpu.f90
  *   3D with the wall table (wall_mode = 1):
  *       src/omp_parallel/ibm_3d_air_condition_omp_cpu.f90
+ *   2D with symmetry rows at j = 1 and j = n (slip_y = 1): the options the
+ *       2D file keeps commented out (:440-450, :512-526)
  *   grid: src/omp_parallel/lib/grid.f90, divergence: lib/output.f90
  */
 #include <math.h>
@@ -57,6 +59,7 @@ typedef struct or_params {
   int32_t nonslip, inflow_porosity;
   int32_t wall_mode;  /* 1: the air-condition program (3D) */
   int32_t walls[6];   /* top, bottom, east, west, north, south: 0 wall, 1 inlet, 2 outlet */
+  int32_t slip_y;     /* 1 (2D): the commented symmetry rows at j = 1 and j = n */
 } or_params;
 
 typedef struct F(or_ctx) {
@@ -67,6 +70,7 @@ typedef struct F(or_ctx) {
   int nonslip, iter_max, istep_max;
   int inflow_porosity;   /* backstep program: inflow/initial velocity x porosity */
   int wall_mode, walls[6];
+  int slip_y;            /* 2D symmetry rows (ibm_2d_uniform_omp_cpu.f90:440-450, 512-526) */
   const REAL *poro;      /* porosity of the case (set by or_grid_conditions) */
   size_t ncell; /* (m+2)(n+2)[(l+2)] */
   /* solve_p locals (static in the reference through -fno-automatic) */
@@ -106,6 +110,7 @@ CTX *F(or_create)(const or_params *P) {
   c->inflow_porosity = P->inflow_porosity;
   c->wall_mode = (P->dim == 3) ? P->wall_mode : 0;
   for (int f = 0; f < 6; f++) c->walls[f] = P->walls[f];
+  c->slip_y = (P->dim == 2) ? P->slip_y : 0;
   c->iter_max = P->iter_max;
   c->istep_max = P->istep_max;
   /* grid.f90:50-52 (2D), :297-300 (3D) */
@@ -330,6 +335,20 @@ void F(or_boundary)(CTX *c, REAL *p, REAL *u, REAL *v, REAL *w) {
       u[I2(i, n + 1)] = u[I2(i, 1)];
       v[I2(i, n + 1)] = v[I2(i, 1)];
       p[I2(i, n + 1)] = p[I2(i, 1)];
+    }
+    if (c->slip_y) { /* :512-526, the commented symmetry options at j = 1 and j = n */
+      for (int i = 1; i <= m; i++) {
+        u[I2(i, 0)] = u[I2(i, 2)];
+        v[I2(i, 1)] = R(0.);
+        v[I2(i, 0)] = -v[I2(i, 2)];
+        p[I2(i, 0)] = p[I2(i, 2)];
+      }
+      for (int i = 1; i <= m; i++) {
+        u[I2(i, n + 1)] = u[I2(i, n - 1)];
+        v[I2(i, n)] = R(0.);
+        v[I2(i, n + 1)] = -v[I2(i, n - 1)];
+        p[I2(i, n + 1)] = p[I2(i, n - 1)];
+      }
     }
   } else {
     const REAL pi = (REAL)atan(R(1.)) * R(4.);
@@ -804,6 +823,16 @@ void F(or_boundary_matrix)(CTX *c, const REAL *p) {
       c->aw[I2(m, j)] = R(0.);
       c->an[I2(m, j)] = R(0.);
       c->as[I2(m, j)] = R(0.);
+    }
+    if (c->slip_y) { /* :440-450, the commented symmetry rows (dp/dy = 0) */
+      for (int i = 1; i <= m; i++) {
+        c->an[I2(i, 1)] = c->an[I2(i, 1)] + c->as[I2(i, 1)];
+        c->as[I2(i, 1)] = R(0.);
+      }
+      for (int i = 1; i <= m; i++) {
+        c->as[I2(i, n)] = c->as[I2(i, n)] + c->an[I2(i, n)];
+        c->an[I2(i, n)] = R(0.);
+      }
     }
   } else {
     for (int k = 1; k <= l; k++)

@@ -32,7 +32,7 @@ class PfParams(ctypes.Structure):
         ("istep_max", ctypes.c_int32), ("iter_max", ctypes.c_int32),
         ("thickness", ctypes.c_double), ("threshold", ctypes.c_double),
         ("relux_factor", ctypes.c_double), ("nonslip", ctypes.c_int32), ("inflow_porosity", ctypes.c_int32),
-        ("wall_mode", ctypes.c_int32), ("walls", ctypes.c_int32 * 6),
+        ("wall_mode", ctypes.c_int32), ("walls", ctypes.c_int32 * 6), ("slip_y", ctypes.c_int32),
     ]
 
 

@@ -31,7 +31,7 @@ GROUPS = {
 }
 GPU_GROUP = "gpu_control"
 GPU_KEYS = ["precision", "outer_max", "inner_sweeps", "dc_tol", "track_sor_error", "inflow_porosity", "walls",
-            "sweep_form", "fused_rows", "fused_planes", "sor_path"]
+            "sweep_form", "fused_rows", "fused_planes", "sor_path", "slip_y"]
 WALL_FACES = ("top", "bottom", "east", "west", "north", "south")
 
 
@@ -89,6 +89,11 @@ class Settings:
     # programs' x inflow/outflow with periodic y and z.  In a namelist:
     # walls = "1,0,0,0,0,2".
     walls: Optional[Tuple[int, ...]] = None
+    # 2D, plain FP64: symmetry rows at j = 1 and j = n ("slip" top and bottom:
+    # dp/dy = 0, v = 0, u mirrored into the ghost row) in place of the periodic
+    # wrap, the option ibm_2d_uniform_omp_cpu.f90 keeps commented out
+    # (:438-450, :503-518)
+    slip_y: bool = False
 
     def replace(self, **kw) -> "Settings":
         return dataclasses.replace(self, **kw)

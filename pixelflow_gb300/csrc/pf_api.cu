@@ -56,6 +56,8 @@ int make_geo(const pf_params& p, Geo& g) {
   if (g.wall && p.dim != 3) return fail(PF_E_INVALID, "wall_mode: the air-condition program is 3D");
   for (int f = 0; g.wall && f < 6; f++)
     if (p.walls[f] < 0 || p.walls[f] > 2) return fail(PF_E_INVALID, "walls: each entry must be 0, 1 or 2");
+  g.slip = p.slip_y ? 1 : 0;
+  if (g.slip && (p.dim != 2 || g.wall)) return fail(PF_E_INVALID, "slip_y: the symmetry rows are a 2D option");
   if (g.wall) {  // non-periodic: the edge rows' neighbours are the ghost rows
     g.jn_n = g.n + 1;
     g.js_1 = 0;
@@ -321,7 +323,7 @@ static void enqueue_projection(pf_case* c) {
 
 static void enqueue_boundary(pf_case* c) {
   const int b = c->cur;
-  c->launches += c->g.wall ? 6 : (c->g.dim == 3 ? 3 : 2);
+  c->launches += boundary_launches(c->g);
   launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
 }
 
@@ -439,6 +441,8 @@ static int create_case(const pf_params* prm, const pf_options* opt, pf_case** ou
     rc = fail(PF_E_INVALID, "outer_max and inner_sweeps must be >= 0");
   if (rc == PF_OK && c->g.wall && c->opt.precision != PF_PREC_FP64)
     rc = fail(PF_E_INVALID, "wall_mode: the air-condition program runs in the plain FP64 form only");
+  if (rc == PF_OK && c->g.slip && c->opt.precision != PF_PREC_FP64)
+    rc = fail(PF_E_INVALID, "slip_y: the symmetry rows run in the plain FP64 form only");
   if (rc == PF_OK && c->opt.sweep_form != PF_SWEEP_AUTO && c->opt.sweep_form != PF_SWEEP_SPLIT &&
       c->opt.sweep_form != PF_SWEEP_FUSED)
     rc = fail(PF_E_INVALID, "unknown sweep_form");
@@ -555,7 +559,7 @@ int pf_initial_conditions(pf_case* c) {
   PF_CUDA(cudaMemsetAsync(c->p[1], 0, pk, c->st));
   launch_initial<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
   launch_boundary<double>(g, c->s, c->U[0], c->V[0], c->W[0], c->p[0], c->p[1], c->st);
-  c->launches += 1 + (g.wall ? 6 : (g.dim == 3 ? 3 : 2));
+  c->launches += 1 + boundary_launches(g);
   if (c->opt.precision == PF_PREC_MIXED) mixed_sync_from_fp64(c);
   return check_launch("pf_initial_conditions");
 }

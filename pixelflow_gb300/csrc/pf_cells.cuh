@@ -616,6 +616,23 @@ __device__ __forceinline__ void c_bnd_y(const Geo& g, T* u, T* v, T* w, double* 
   pref(g, p0, p1, i, g.n + 1, k) = pref(g, p0, p1, i, 1, k);
 }
 
+// boundary, the symmetry rows of the 2D slip option at column i (1..m), in
+// the order of the reference's commented blocks (ibm_2d_uniform_omp_cpu.f90
+// :512-526): j = 1 -- u mirrored into ghost row 0, v = 0 on the row and
+// odd into the ghost, p even; then j = n likewise.
+template <typename T>
+__device__ __forceinline__ void c_bnd_slip(const Geo& g, T* u, T* v, double* p0, double* p1, int i) {
+  const int n = g.n;
+  u[nat_idx(g, i, 0, 0)] = u[nat_idx(g, i, 2, 0)];
+  v[nat_idx(g, i, 1, 0)] = T(0);
+  v[nat_idx(g, i, 0, 0)] = -v[nat_idx(g, i, 2, 0)];
+  pref(g, p0, p1, i, 0, 0) = pref(g, p0, p1, i, 2, 0);
+  u[nat_idx(g, i, n + 1, 0)] = u[nat_idx(g, i, n - 1, 0)];
+  v[nat_idx(g, i, n, 0)] = T(0);
+  v[nat_idx(g, i, n + 1, 0)] = -v[nat_idx(g, i, n - 1, 0)];
+  pref(g, p0, p1, i, n + 1, 0) = pref(g, p0, p1, i, n - 1, 0);
+}
+
 // boundary, z faces (3D): periodic ghost planes at column i of row j.
 template <typename T>
 __device__ __forceinline__ void c_bnd_z(const Geo& g, T* u, T* v, T* w, double* p0, double* p1, int i, int j) {

@@ -37,7 +37,16 @@ struct Geo {
   // 1: the air-condition program -- walls on every face, no periodic wrap
   // (the edge neighbours are the ghost rows, which hold boundary values)
   int wall;
+  // 1 (2D): symmetry rows at j = 1 and j = n (the SOR's y coefficient across
+  // the edge folded into the inward one; the periodic neighbours it still
+  // addresses are multiplied by zero, as in the reference)
+  int slip;
 };
+
+// Kernels of the boundary stage (for the launch counts).
+__host__ __device__ inline int boundary_launches(const Geo& g) {
+  return g.wall ? 6 : (g.dim == 3 ? 3 : (g.slip ? 3 : 2));
+}
 
 // Ghost rows of p refreshed before each half-sweep (odd periodic sizes).
 __host__ __device__ inline bool periodic_halo(const Geo& g) {

@@ -108,6 +108,16 @@ __global__ void k_setup_coef(Geo g, Scal s, const double* __restrict__ po, Coef<
       oadd = a[0] * s.outlet_pressure;
       for (int d = 0; d < 6; d++) a[d] = 0.0;
     }
+    // the symmetry rows the reference keeps commented out (2D :440-450),
+    // applied after the inlet and outlet edits, as listed there
+    if (g.slip && j == 1) {
+      a[2] = a[2] + a[3];
+      a[3] = 0.0;
+    }
+    if (g.slip && j == g.n) {
+      a[3] = a[3] + a[2];
+      a[2] = 0.0;
+    }
   }
   const double wap = s.omega / ap;
   const int c = colour_of(g, i, j, k);
@@ -318,6 +328,15 @@ __global__ void k_bnd_y(Geo g, T* u, T* v, T* w, double* p0, double* p1) {
   pdl_begin();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= g.m + 1) c_bnd_y(g, u, v, w, p0, p1, i, blockIdx.y);  // k = 0 in 2D, 0..l+1 in 3D
+}
+
+// boundary, symmetry rows (2D slip option) over i = 1..m, after the periodic
+// ghost rows.
+template <typename T>
+__global__ void k_bnd_slip(Geo g, T* u, T* v, double* p0, double* p1) {
+  pdl_begin();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i <= g.m) c_bnd_slip(g, u, v, p0, p1, i);
 }
 
 // boundary, z faces (3D): periodic ghost planes over i = 0..m+1, j = 0..n+1.
@@ -1163,6 +1182,7 @@ void launch_boundary(const Geo& g, const Scal& s, TV* u, TV* v, TV* w, double* p
   launch_pdl(k_bnd_x<TV>, dim3((g.n + 127) / 128, g.dim == 3 ? g.l : 1), dim3(128), st, g, s, u, v, w, p0, p1);
   launch_pdl(k_bnd_y<TV>, dim3((g.m + 2 + 127) / 128, g.dim == 3 ? g.l + 2 : 1), dim3(128), st, g, u, v, w, p0, p1);
   if (g.dim == 3) launch_pdl(k_bnd_z<TV>, dim3((g.m + 2 + 127) / 128, g.n + 2), dim3(128), st, g, u, v, w, p0, p1);
+  if (g.slip) launch_pdl(k_bnd_slip<TV>, dim3((g.m + 127) / 128), dim3(128), st, g, u, v, p0, p1);
 }
 
 template <typename TV>

@@ -234,7 +234,7 @@ void enqueue_projection_mixed(pf_case* c) {
 
 void enqueue_boundary_mixed(pf_case* c) {
   const int b = c->cur;
-  c->launches += c->g.wall ? 6 : (c->g.dim == 3 ? 3 : 2);
+  c->launches += boundary_launches(c->g);
   launch_boundary<double>(c->g, c->s, c->U[b], c->V[b], c->W[b], c->p[0], c->p[1], c->st);
   mixed_sync_from_fp64(c);
 }

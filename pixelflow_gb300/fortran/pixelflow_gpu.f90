@@ -20,6 +20,7 @@ module pixelflow_gpu
     real(c_double) :: thickness, threshold, relux_factor
     integer(c_int32_t) :: nonslip, inflow_porosity
     integer(c_int32_t) :: wall_mode, walls(6)
+    integer(c_int32_t) :: slip_y
   end type pf_params
 
   type, bind(C) :: pf_options

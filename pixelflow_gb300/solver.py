@@ -35,7 +35,7 @@ def make_params(s: Settings, shape: Sequence[int]) -> PfParams:
                     s.inlet_velocity, s.outlet_pressure, s.aoa, int(s.istep_max), int(s.iter_max),
                     s.thickness, s.threshold, s.relux_factor, 1 if s.nonslip else 0,
                     1 if s.inflow_porosity else 0, 1 if s.walls is not None else 0,
-                    (ctypes.c_int32 * 6)(*(s.walls or (0,) * 6)))
+                    (ctypes.c_int32 * 6)(*(s.walls or (0,) * 6)), 1 if s.slip_y else 0)
 
 
 def make_options(s: Settings, use_graph: bool = True) -> PfOptions:

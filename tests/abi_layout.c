@@ -18,7 +18,7 @@ int main(int argc, char **argv) {
   F(pf_params, height); F(pf_params, depth); F(pf_params, time); F(pf_params, inlet_velocity);
   F(pf_params, outlet_pressure); F(pf_params, aoa); F(pf_params, istep_max); F(pf_params, iter_max);
   F(pf_params, thickness); F(pf_params, threshold); F(pf_params, relux_factor); F(pf_params, nonslip);
-  F(pf_params, inflow_porosity); F(pf_params, wall_mode); F(pf_params, walls);
+  F(pf_params, inflow_porosity); F(pf_params, wall_mode); F(pf_params, walls); F(pf_params, slip_y);
   F(pf_options, precision); F(pf_options, outer_max); F(pf_options, inner_sweeps);
   F(pf_options, track_sor_error); F(pf_options, dc_tol); F(pf_options, use_graph); F(pf_options, sweep_form);
   F(pf_options, fused_rows); F(pf_options, fused_planes); F(pf_options, sor_path); F(pf_options, reserved);

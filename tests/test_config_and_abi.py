@@ -126,7 +126,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(L, name), name
     assert set(_lib.exported_symbols()) >= set(declared)
-    assert L.pf_abi_version() == 2
+    assert L.pf_abi_version() == 3
 
 
 def test_invalid_arguments_fail_before_any_device_work():

@@ -392,3 +392,32 @@ def test_backstep_inflow_parity(shape, steps):
         b.step(3)
         a, bb = one.get_state(), b.get_state(slot)
         assert all(np.array_equal(a[k], bb[k]) for k in a)
+
+
+@pytest.mark.parametrize("shape,steps", [((64, 32), 60), ((63, 33), 40), ((96, 48), 30)])
+def test_slip_rows_parity(shape, steps):
+    """The 2D symmetry ("slip") rows at j = 1 and j = n, the option the
+    reference keeps commented out (ibm_2d_uniform_omp_cpu.f90:440-450 in
+    boundrary_matrix, :512-526 in boundary), against the oracle field by
+    field (odd n: the SOR's ghost rows are refreshed and multiplied by the
+    zeroed coefficients); v is 0 on both rows; the precision form refuses
+    the option."""
+    s = G.settings_cylinder_2d(iter_max=30, slip_y=True)
+    vals = G.cylinder_2d(*shape, radius=0.15, cx=0.6, cy=0.4)
+    ref, c = _pair(s, shape, vals)
+    with c:
+        c.initial_conditions()
+        c.step(steps)
+        got = c.get_state()
+        md, se = c.norms()
+    e_ref = ref.step(steps)
+    e = errors(got, ref, 2)
+    assert_each_field(e, 1e-11)
+    m, n = shape
+    assert not got["v"][1, 1:m + 1].any() and not got["v"][n, 1:m + 1].any()
+    assert abs(se - e_ref) <= 1e-8 * abs(e_ref)
+    assert abs(md - ref.divergence_diag()) <= 1e-8 * ref.divergence_diag()
+    with pytest.raises(Exception):
+        Case(s.replace(precision="mixed"), shape, vals)
+    with pytest.raises(Exception):
+        Case(G.settings_spheres_3d(slip_y=True), (16, 12, 10), G.spheres_3d(16, 12, 10, count=1))

@@ -222,6 +222,32 @@ def test_backstep_inflow_c_matches_numpy(shape):
     assert not np.array_equal(plain.u, a.u)
 
 
+@pytest.mark.parametrize("shape", [(12, 8), (9, 7), (10, 3)])
+def test_slip_rows_c_matches_numpy(shape):
+    """The 2D symmetry rows the reference keeps commented out
+    (ibm_2d_uniform_omp_cpu.f90:440-450, 512-526): both restatements agree
+    bit for bit; after a step v is 0 on rows 1 and n, the ghost rows mirror
+    u and p and negate v, and the run differs from the periodic one."""
+    s, vals = _case2d(shape)
+    s = s.replace(slip_y=True)
+    a, b = OracleCase(s, shape, vals), NpCase(s, shape, vals)
+    a.initialize()
+    b.initialize()
+    m, n = shape
+    I = slice(1, m + 1)
+    for _ in range(3):
+        assert a.step(1) == b.step(1)
+        for f in ("u", "v", "p"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        assert not a.v[1, I].any() and not a.v[n, I].any()
+        assert np.array_equal(a.u[0, I], a.u[2, I]) and np.array_equal(a.u[n + 1, I], a.u[n - 1, I])
+        assert np.array_equal(a.v[0, I], -a.v[2, I]) and np.array_equal(a.p[n + 1, I], a.p[n - 1, I])
+    periodic = OracleCase(s.replace(slip_y=False), shape, vals)
+    periodic.initialize()
+    periodic.step(3)
+    assert not np.array_equal(periodic.p, a.p)
+
+
 AIR_CONDITION_TABLE = (1, 0, 0, 0, 0, 2)  # ibm_3d_air_condition_omp_cpu.f90:10-15
 
 
