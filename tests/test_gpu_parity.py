@@ -246,6 +246,24 @@ def test_cylinder_512x256_1000_steps_parity():
 
 
 @pytest.mark.slow
+def test_cylinder_512x256_slip_1000_steps_parity():
+    """The 2D benchmark case as configured with slip top and bottom walls
+    (the reference's commented symmetry rows, slip_y) for 1000 steps against
+    the oracle: u, v, p each within 1e-10 relative L2."""
+    s = G.settings_cylinder_2d(slip_y=True)
+    vals = G.cylinder_2d()
+    ref, c = _pair(s, (512, 256), vals)
+    with c:
+        c.initial_conditions()
+        c.step(1000)
+        got = c.get_state()
+    ref.step(1000)
+    errs = errors(got, ref, 2)
+    print("1000-step slip relative L2 vs oracle:", errs)
+    assert_each_field(errs, 1e-10)
+
+
+@pytest.mark.slow
 def test_spheres_3d_reduced_parity():
     """The 3D benchmark geometry (32 seeded spheres) on a 64x64x64 grid for
     60 steps with iter_max=100."""
