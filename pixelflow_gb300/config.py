@@ -241,7 +241,10 @@ def read_porosity_csv(path: str) -> Tuple[Tuple[int, ...], np.ndarray]:
 
 
 def write_porosity_csv(path: str, values: np.ndarray) -> None:
-    """Write values (shape (n,m) or (l,n,m)) in the reference CSV format."""
+    """Write values (shape (n,m) or (l,n,m)) in the reference CSV format, as
+    the reference's own writer lays it out (tools/output/output_porosity.py:
+    header without spaces, records "i, j, k, value" with ten decimals, i
+    fastest): the same values give the same bytes."""
     if values.ndim == 2:
         n, m = values.shape
         jj, ii = np.meshgrid(np.arange(1, n + 1), np.arange(1, m + 1), indexing="ij")
@@ -255,4 +258,4 @@ def write_porosity_csv(path: str, values: np.ndarray) -> None:
     with open(path, "w") as f:
         f.write(header + "\n")
         for (a, b, c), v in zip(rec, values.ravel()):
-            f.write(f"{a},{b},{c},{v:.10f}\n")
+            f.write(f"{a}, {b}, {c}, {v:.10f}\n")
