@@ -11,6 +11,8 @@ from pixelflow_gb300 import geometry as G
 from oracle.np_oracle import NpCase
 from oracle.oracle import OracleCase
 
+from tests.golden.make_golden import CASES as GOLDEN_CASES
+
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
@@ -165,7 +167,7 @@ def test_sor_error_semantics():
     assert np.isfinite(e) and e > 0
 
 
-@pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
+@pytest.mark.parametrize("name", sorted(f + ".npz" for f in GOLDEN_CASES))
 def test_oracle_reproduces_golden(name):
     from tests.golden.make_golden import CASES, run_oracle
     spec = CASES[name[:-4]]
