@@ -366,6 +366,9 @@ def run_reference(args):
         barrier(world)
         return
     s, shape, vals, desc = workload(args.workload, "fp64")
+    # the same workload keys as the GPU arm's line
+    desc.update(parallelism=f"replicas{world}" if world > 1 else "single",
+                l2="working set > 129 MB L2 (no flush needed)")
     from oracle.oracle import OracleCase
     cells = int(np.prod(shape))
     c = OracleCase(s, shape, vals)
