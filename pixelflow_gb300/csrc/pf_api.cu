@@ -110,6 +110,7 @@ int make_scal(const pf_params& p, Scal& s) {
   s.ix2 = 1.0 / (s.dx * s.dx);
   s.iy2 = 1.0 / (s.dy * s.dy);
   s.iz2 = p.dim == 3 ? 1.0 / (s.dz * s.dz) : 0.0;
+  s.iso = p.dim == 3 && s.dx == s.dy && s.dx == s.dz;
   s.dtnu = s.dt * s.xnue;
   s.dtnl = s.dt * (s.xnue + s.xlambda);
   const double cdt = s.dt / s.density;

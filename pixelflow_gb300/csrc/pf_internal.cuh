@@ -87,6 +87,7 @@ struct Scal {
   // the device; the f-suffixed copies are those values rounded to float.
   double hx, hy, hz;     // 0.5/dx, 0.5/dy, 0.5/dz
   double ix2, iy2, iz2;  // 1/(dx*dx), ...
+  int iso;               // 3D with dx = dy = dz: the three Laplacian factors are one
   double dtnu, dtnl;     // dt*nu, dt*(nu+lambda)
   double pgx, pgy, pgz;  // dt/density*0.5/dx, ... (projection)
   float hxf, hyf, hzf, ix2f, iy2f, iz2f, dtf, nuf, lamf, dtnuf, dtnlf, pgxf, pgyf, pgzf;

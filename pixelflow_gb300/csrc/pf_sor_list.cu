@@ -59,68 +59,6 @@ namespace {
 // than 256 (256^3: 93.1 -> 92.1 us per launch; 64 threads: 93.7)
 constexpr int LIST_THREADS = 128;
 
-// Exact sum of six doubles, rounded once to nearest (ties to even when no
-// bits fell below the guard bits).  Each significand, with its implicit
-// bit, is shifted to the scale 2^(Emax - 1075 - G) of the largest exponent
-// with G = 7 guard bits; six terms below 2^60 add up without overflow in a
-// signed 64-bit integer.  A term more than G binades below the largest
-// loses the bits shifted out (truncated), an error below 2^-7 of the
-// largest term's last place.  Returns false (result unset) when an input
-// is Inf or NaN or the sum is not a normal number; the caller then adds in
-// FP64.
-__device__ __forceinline__ bool sum6_exact(const double (&x)[6], double& out) {
-  constexpr int G = 7;
-  unsigned long long mant[6];
-  int ex[6];
-  bool neg[6];
-  int emax = 1;
-  bool finite = true;
-#pragma unroll
-  for (int q = 0; q < 6; q++) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x[q]);
-    const int e = (int)((b >> 52) & 0x7ff);
-    finite = finite && e != 0x7ff;
-    mant[q] = (b & 0x000fffffffffffffULL) | (e ? (1ULL << 52) : 0ULL);
-    ex[q] = e ? e : 1;
-    neg[q] = (b >> 63) != 0;
-    emax = max(emax, ex[q]);
-  }
-  long long s = 0;
-#pragma unroll
-  for (int q = 0; q < 6; q++) {
-    const int d = emax - ex[q];
-    const unsigned long long a = d <= G ? (mant[q] << (G - d)) : (d - G < 64 ? mant[q] >> (d - G) : 0ULL);
-    s += neg[q] ? -(long long)a : (long long)a;
-  }
-  if (!finite) return false;
-  if (s == 0) {
-    out = 0.0;
-    return true;
-  }
-  const bool sn = s < 0;
-  unsigned long long u = sn ? (unsigned long long)(-s) : (unsigned long long)s;
-  const int lead = 63 - __clzll((long long)u);
-  int sh = lead - 52;
-  unsigned long long m;
-  if (sh > 0) {
-    m = u >> sh;
-    const unsigned long long rem = u & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
-    if (rem > half || (rem == half && (m & 1))) m++;
-    if (m == (1ULL << 53)) {
-      m >>= 1;
-      sh++;
-    }
-  } else {
-    m = u << (-sh);
-  }
-  const int eb = emax - G + sh;  // biased exponent of the result
-  if (eb <= 0 || eb >= 0x7ff) return false;
-  const unsigned long long bits =
-      (sn ? (1ULL << 63) : 0ULL) | ((unsigned long long)eb << 52) | (m & 0x000fffffffffffffULL);
-  out = __longlong_as_double((long long)bits);
-  return true;
-}
-
 // Per packed work item of one colour (the mapping of k_sor_half): 0 not a
 // cell (i = 0 or m+1), 1 pure fluid (all six normalised coefficients equal
 // the fluid constants, no outlet addend), 2 any other cell.  Block 0 also
