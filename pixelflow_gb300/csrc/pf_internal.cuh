@@ -202,6 +202,9 @@ void launch_pack_eps(const Geo& g, const double* poro, float* e0, float* e1, cud
 int launch_forces(const Geo& g, const Scal& s, const double* poro, const double* p0, const double* p1,
                   const double* u, const double* v, const double* w, double* scratch, double* out,
                   cudaStream_t st);
+// FP32 copies of nf (<= 3) FP64 arrays of n elements (n a multiple of 4,
+// 32-byte aligned arrays) in one launch.
+void launch_to_float3(const double* const* src, float* const* dst, int nf, long long n, cudaStream_t st);
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st);
 // staging (dense (m+2)(n+2)(l+2), i fastest) <-> device layouts

@@ -1081,6 +1081,23 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) b[q] = (float)a[q];
 }
+// FP32 copies of up to three FP64 arrays of n elements (n a multiple of 4,
+// arrays 32-byte aligned) in one launch, four elements per thread and
+// iteration: blockIdx.y selects the array.  The per-element conversion is
+// k_to_float's.
+struct Fields3 {
+  const double* src[3];
+  float* dst[3];
+};
+__global__ void k_to_float3(Fields3 f, long long n4) {
+  pdl_begin();
+  const double2* __restrict__ a = reinterpret_cast<const double2*>(f.src[blockIdx.y]);
+  float4* __restrict__ b = reinterpret_cast<float4*>(f.dst[blockIdx.y]);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+    const double2 x = a[2 * q], y = a[2 * q + 1];
+    b[q] = make_float4((float)x.x, (float)x.y, (float)y.x, (float)y.y);
+  }
+}
 __global__ void k_to_double(const float* __restrict__ a, double* __restrict__ b, long long n) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) b[q] = (double)a[q];
@@ -1395,6 +1412,20 @@ void launch_dc_check(const unsigned long long* rmax, double tol, int* skip, cuda
 
 void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st) {
   launch_pdl(k_to_float, dim3((unsigned)((n + 255) / 256)), dim3(256), st, src, dst, n);
+}
+void launch_to_float3(const double* const* src, float* const* dst, int nf, long long n, cudaStream_t st) {
+  Fields3 f{};
+  for (int i = 0; i < nf; i++) {
+    f.src[i] = src[i];
+    f.dst[i] = dst[i];
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long n4 = n / 4;
+  const long long want = (n4 + 255) / 256;
+  const unsigned blocks = (unsigned)std::max(1LL, std::min<long long>(want, 8LL * std::max(1, sms)));
+  launch_pdl(k_to_float3, dim3(blocks, nf), dim3(256), st, f, n4);
 }
 void launch_to_double(const float* src, double* dst, long long n, cudaStream_t st) {
   k_to_double<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);

@@ -151,11 +151,10 @@ void mixed_setup(pf_case* c) {
 // FP32 copy of the current FP64 velocity state, read by the stencils.
 void mixed_sync_from_fp64(pf_case* c) {
   const int b = c->cur;
-  const long long n = c->g.nat;
-  launch_to_float(c->U[b], c->Uf[0], n, c->st);
-  launch_to_float(c->V[b], c->Vf[0], n, c->st);
-  if (c->g.dim == 3) launch_to_float(c->W[b], c->Wf[0], n, c->st);
-  c->launches += c->g.dim;
+  const double* src[3] = {c->U[b], c->V[b], c->W[b]};
+  float* dst[3] = {c->Uf[0], c->Vf[0], c->Wf[0]};
+  launch_to_float3(src, dst, c->g.dim, c->g.nat, c->st);
+  c->launches += 1;
 }
 
 void mixed_sync_to_fp64(pf_case*) {}  // the state is FP64 already
