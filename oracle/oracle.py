@@ -3,8 +3,9 @@
 Wraps oracle/libpf_oracle.so (the C restatement of PixelFlow's OpenMP step in
 pf_oracle.c).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline / reference arm use it, always as the checker or the timed CPU
-baseline -- never as a product path.  Parity of this restatement with the
-reference is unpinned (see pf_oracle.c).
+baseline -- never as a product path.  This restatement reproduces the
+reference's own programs, executed from their Fortran source on small
+grids, bit for bit (see pf_oracle.c and tests/test_reference_pin.py).
 
 Arrays are numpy views in the reference's Fortran layout with ghosts:
 shape (n+2, m+2) for 2D and (l+2, n+2, m+2) for 3D, so that

@@ -6,11 +6,16 @@
  * bench.py as the checker and as the timed CPU baseline.  The product
  * (pixelflow_gb300, the CUDA C-ABI library) never links or calls this file.
  *
- * Parity status: UNPINNED.  The reference is Fortran 90 and has no tests,
- * golden vectors or expected outputs; no Fortran compiler exists in the
- * build container, so the reference itself cannot be run to pin this
- * restatement.  It is cross-checked instead against an independent numpy
- * restatement (oracle/np_oracle.py) and physical invariants (tests/).
+ * Parity status: pinned on small grids.  The reference is Fortran 90 and
+ * has no tests, golden vectors or expected outputs, and no Fortran compiler
+ * exists here.  Its own programs are instead executed from their source
+ * text by a translator for the Fortran subset they use
+ * (tests/golden/fortran_subset.py, gfortran plain-FP64 semantics; fixtures
+ * tests/golden/refpin_*.npz): this restatement reproduces their fields bit
+ * for bit (uniform 2D and 3D on even and odd grids, backstep,
+ * air-condition; tests/test_reference_pin.py).  It is also cross-checked
+ * against an independent numpy restatement (oracle/np_oracle.py) and
+ * physical invariants (tests/).
  *
  * Every routine below follows one reference subroutine statement for
  * statement, with the same loop nests, the same red-black linear-index

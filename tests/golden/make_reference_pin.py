@@ -1,0 +1,137 @@
+"""Golden vectors made by the reference itself: PixelFlow's OpenMP programs
+(src/omp_parallel/*.f90 and lib/global.f90, lib/grid.f90), executed from
+their own source text by tests/golden/fortran_subset.py with gfortran's
+plain-FP64 semantics, on small grids for a few steps.
+
+Each case writes tests/golden/refpin_<name>.npz with the porosity values the
+program read (its CSV, written by this repository's writer, which produces
+the reference writer's bytes), the settings, and the fields u, v, [w,] p the
+program holds after `steps` time steps (ghost layers included,
+[(k,) j, i] order).  The runs replace only what is not arithmetic: the
+namelist reader (`read_settings` returns the settings below), the output
+routines, `get_now_time` and `system`; the static array sizes md, nd, ld
+are shrunk to the grid (they size storage only).  The main program, the
+grid set-up (which reads the CSV with list-directed input), the initial and
+boundary conditions, solve_p, the matrix edits and the SOR run unchanged.
+
+Run from the repository root (the reference is not needed afterwards):
+
+    PF_REFERENCE_DIR=<reference checkout> python -m tests.golden.make_reference_pin
+"""
+import os
+import re
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from pixelflow_gb300 import config as C  # noqa: E402
+from pixelflow_gb300 import geometry as G  # noqa: E402
+from tests.golden.fortran_subset import Program  # noqa: E402
+
+AIR_CONDITION_TABLE = (1, 0, 0, 0, 0, 2)  # top, bottom, east, west, north, south
+
+# name -> (program file, dim, shape, settings builder, steps)
+CASES = {
+    "uniform2d_12x8": ("ibm_2d_uniform_omp_cpu.f90", (12, 8), "cyl", 3),
+    "uniform2d_13x9": ("ibm_2d_uniform_omp_cpu.f90", (13, 9), "cyl", 3),
+    "uniform2d_9x8": ("ibm_2d_uniform_omp_cpu.f90", (9, 8), "cyl", 3),
+    "backstep2d_12x8": ("ibm_2d_backstep_omp_cpu.f90", (12, 8), "step", 3),
+    "uniform3d_8x6x5": ("ibm_3d_uniform_omp_cpu.f90", (8, 6, 5), "sph", 3),
+    "uniform3d_7x6x5": ("ibm_3d_uniform_omp_cpu.f90", (7, 6, 5), "sph", 3),
+    "uniform3d_8x7x6": ("ibm_3d_uniform_omp_cpu.f90", (8, 7, 6), "sph", 2),
+    "aircon3d_8x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (8, 7, 6), "room", 3),
+}
+
+NAMES = ["xnue", "xlambda", "density", "width", "height", "depth", "time", "inlet_velocity", "outlet_pressure",
+         "aoa", "istep_max", "istep_out", "thickness", "threshold", "radius", "center_x", "center_y", "center_z",
+         "nonslip", "output_folder", "csv_file", "iter_max", "relux_factor"]
+
+
+def case_inputs(name):
+    """(settings, shape, porosity values before the CSV round trip, steps)."""
+    prog, shape, kind, steps = CASES[name]
+    if kind in ("cyl", "step"):
+        m, n = shape
+        s = G.settings_cylinder_2d(iter_max=7)
+        vals = G.cylinder_2d(m, n, radius=0.2, cx=0.6, cy=0.45)
+        if kind == "step":  # an obstacle across the inlet: a non-uniform inflow profile
+            vals = np.minimum(vals, G.cylinder_2d(m, n, radius=0.3, cx=0.0, cy=0.3))
+            s = s.replace(inflow_porosity=True)
+        dt = 2e-4
+    else:
+        m, n, l = shape
+        if kind == "room":
+            s = G.settings_spheres_3d(iter_max=5, walls=AIR_CONDITION_TABLE, inlet_velocity=0.5)
+            vals = G.spheres_3d(m, n, l, spheres=np.array([[0.5, 0.5, 0.4, 0.2]]))
+            vals[-1, : n // 2, : m // 2] = 0.05
+            vals[:, 0, m // 2:] = 0.05
+        else:
+            s = G.settings_spheres_3d(iter_max=5)
+            vals = G.spheres_3d(m, n, l, spheres=np.array([[0.4, 0.5, 0.5, 0.2], [0.7, 0.3, 0.6, 0.15]]))
+        dt = 1e-4
+    # time / istep_max is dt for the program and the oracle alike
+    s = s.replace(time=dt * steps, istep_max=steps)
+    return s, shape, vals, steps
+
+
+def run_reference(ref_dir, name):
+    prog, shape, kind, steps = CASES[name]
+    s, shape, vals, steps = case_inputs(name)
+    src = os.path.join(ref_dir, "src", "omp_parallel")
+    files = [os.path.join(src, "lib", "global.f90"), os.path.join(src, "lib", "grid.f90"), os.path.join(src, prog)]
+    texts = [open(f).read() for f in files]
+    with tempfile.TemporaryDirectory() as tmp:
+        csv = os.path.join(tmp, "porosity.csv")
+        C.write_porosity_csv(csv, vals)
+        csv_text = open(csv).read()
+        _, vals_read = C.read_porosity_csv(csv)
+    settings = dict(xnue=s.xnue, xlambda=s.xlambda, density=s.density, width=s.width, height=s.height,
+                    depth=s.depth, time=s.time, inlet_velocity=s.inlet_velocity, outlet_pressure=s.outlet_pressure,
+                    aoa=s.aoa, istep_max=int(s.istep_max), istep_out=10 ** 6, thickness=s.thickness,
+                    threshold=s.threshold, radius=0.0, center_x=0.0, center_y=0.0, center_z=0.0,
+                    nonslip=bool(s.nonslip), output_folder="out", csv_file="porosity.csv",
+                    iter_max=int(s.iter_max), relux_factor=s.relux_factor)
+
+    def read_settings(P, *args):
+        return [settings[k] for k in NAMES]
+
+    def noop(P, *args):
+        return None
+
+    called = set(re.findall(r"\bcall\s+(\w+)", "\n".join(t.lower() for t in texts)))
+    probe = Program(texts, overrides=_sizes(shape))
+    stubs = {nm: noop for nm in called - set(probe.subs)}
+    stubs.update({nm: noop for nm in called if nm.startswith("output_") or nm in ("get_now_time", "system")})
+    stubs["read_settings"] = read_settings
+    P = Program(texts, overrides=_sizes(shape), stubs=stubs)
+    P.vfs["porosity.csv"] = csv_text
+    S = P.run_main()
+    out = {}
+    for f in ("u", "v", "w", "p") if len(shape) == 3 else ("u", "v", "p"):
+        a = S[f]
+        out[f] = np.array(a.data, dtype=np.float64).reshape(a.ext[::-1])
+    return s, shape, vals_read, steps, out
+
+
+def _sizes(shape):
+    if len(shape) == 2:
+        return {"md": shape[0] + 1, "nd": shape[1] + 1}
+    return {"md": shape[0] + 1, "nd": shape[1] + 1, "ld": shape[2] + 1}
+
+
+def main():
+    ref = os.environ.get("PF_REFERENCE_DIR")
+    if not ref:
+        raise SystemExit("set PF_REFERENCE_DIR to a checkout of the reference")
+    for name in CASES:
+        s, shape, vals_read, steps, out = run_reference(ref, name)
+        np.savez(os.path.join(HERE, f"refpin_{name}.npz"), porosity=vals_read, steps=steps, **out)
+        print(name, {k: float(np.abs(v).max()) for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main()

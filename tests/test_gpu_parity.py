@@ -22,6 +22,7 @@ from pixelflow_gb300.solver import Case
 from oracle.oracle import OracleCase
 from tests.conftest import rel_l2, rel_vel
 from tests.golden.make_golden import CASES, case_inputs
+from tests.golden.make_reference_pin import CASES as REFPIN_CASES, case_inputs as refpin_inputs
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -439,3 +440,20 @@ def test_slip_rows_parity(shape, steps):
         Case(s.replace(precision="mixed"), shape, vals)
     with pytest.raises(Exception):
         Case(G.settings_spheres_3d(slip_y=True), (16, 12, 10), G.spheres_3d(16, 12, 10, count=1))
+
+
+@pytest.mark.parametrize("name", sorted(REFPIN_CASES))
+def test_gpu_matches_the_reference_programs(name):
+    """The fields of PixelFlow's own OpenMP programs, executed from their
+    Fortran source (tests/golden/refpin_*.npz, see make_reference_pin.py),
+    against the GPU step on the same settings and porosity: every field
+    within 1e-12 relative L2 after the programs' few steps."""
+    s, shape, _, steps = refpin_inputs(name)
+    ref = np.load(os.path.join(GOLDEN, f"refpin_{name}.npz"))
+    with Case(s, shape, ref["porosity"]) as c:
+        c.initial_conditions()
+        c.step(steps)
+        got = c.get_state()
+    dim = len(shape)
+    errs = errors(got, {f: ref[f] for f in fields(dim)}, dim)
+    assert_each_field(errs, 1e-12)
