@@ -11,9 +11,10 @@
  * exists here.  Its own programs are instead executed from their source
  * text by a translator for the Fortran subset they use
  * (tests/golden/fortran_subset.py, gfortran plain-FP64 semantics; fixtures
- * tests/golden/refpin_*.npz): this restatement reproduces their fields bit
- * for bit (uniform 2D and 3D on even and odd grids, backstep,
- * air-condition; tests/test_reference_pin.py).  It is also cross-checked
+ * tests/golden/refpin_*.npz): this restatement reproduces their fields,
+ * their divergence output and the drag program's force log bit for bit
+ * (uniform 2D and 3D on even and odd grids, backstep, air-condition, drag;
+ * tests/test_reference_pin.py).  It is also cross-checked
  * against an independent numpy restatement (oracle/np_oracle.py) and
  * physical invariants (tests/).
  *

@@ -446,6 +446,7 @@ class Program:
             self._collect(u)
         self.M: Dict[str, Dict[str, object]] = {}
         self.files: Dict[int, List[str]] = {}
+        self.writes: Dict[object, List[list]] = {}
         self.vfs: Dict[str, str] = {}
         self.compiled = {}
         for m in [u for u in self._walk() if u.kind == "module"]:
@@ -511,13 +512,17 @@ class Program:
 
     @staticmethod
     def _split_top(s):
-        out, depth, cur = [], 0, ""
+        out, depth, cur, quote = [], 0, "", None
         for ch in s:
-            if ch == "(":
+            if quote:
+                quote = None if ch == quote else quote
+            elif ch in "'\"":
+                quote = ch
+            elif ch == "(":
                 depth += 1
             elif ch == ")":
                 depth -= 1
-            if ch == "," and depth == 0:
+            if ch == "," and depth == 0 and not quote:
                 out.append(cur)
                 cur = ""
             else:
@@ -641,7 +646,10 @@ class Program:
 
     def _stmt(self, ctx, ln):
         """Yield (python_line, indent_change)."""
-        if ln.startswith(("write", "print", "close", "flush")):
+        m = re.match(r"write\s*\(", ln)
+        if m:
+            return self._write(ctx, ln)
+        if ln.startswith(("print", "close", "flush")):
             return [("pass", 0)]
         m = re.match(r"do\s+(\w+)\s*=\s*(.*)$", ln)
         if m:
@@ -721,6 +729,45 @@ class Program:
                     return ln[i + 1:k], rest
         return None
 
+    def _write(self, ctx, ln):
+        """write(unit, fmt) items: the values are recorded (P.writes[unit],
+        one list per record) instead of formatted; implied-do items
+        (expr, v = a, b) expand in order."""
+        depth, k0 = 0, ln.index("(")
+        for k in range(k0, len(ln)):
+            if ln[k] == "(":
+                depth += 1
+            elif ln[k] == ")":
+                depth -= 1
+                if depth == 0:
+                    break
+        spec = Program._split_top(ln[k0 + 1:k])
+        unit = spec[0].strip()
+        unit_src = repr("*") if unit == "*" else ctx.expr(unit)[0]
+        items = Program._split_top(ln[k + 1:]) if ln[k + 1:].strip() else []
+        parts = []
+        for it in items:
+            parts.append(self._write_item(ctx, it.strip()))
+        return [(f"P.record({unit_src}, [{', '.join(parts)}])", 0)]
+
+    def _write_item(self, ctx, it):
+        m = re.match(r"\((.*)\)$", it)
+        if m:
+            inner = Program._split_top(m.group(1))
+            # (items..., v = a, b[, s])
+            for q in range(len(inner)):
+                mm = re.match(r"(\w+)\s*=\s*(.*)$", inner[q])
+                if mm:
+                    v = mm.group(1)
+                    lo = ctx.expr(mm.group(2))[0]
+                    rest = inner[q + 1:]
+                    hi = ctx.expr(rest[0])[0]
+                    st = ctx.expr(rest[1])[0] if len(rest) > 1 else "1"
+                    vs, _ = ctx.var(v)
+                    body = ", ".join(self._write_item(ctx, x.strip()) for x in inner[:q])
+                    return f"*[_x for {vs} in _range({lo}, {hi}, {st}) for _x in ({body},)]"
+        return ctx.expr(it)[0]
+
     def _lhs(self, ctx, s):
         s = s.strip()
         m = re.match(r"(\w+)\s*\((.*)\)$", s)
@@ -760,8 +807,14 @@ class Program:
         return [ret.get(a) for a in u.args]
 
     def _open(self, unit, fname):
-        text = self.vfs[fname.strip()]
-        self.files[int(unit)] = text.splitlines()
+        name = fname.strip()
+        if name in self.vfs:
+            self.files[int(unit)] = self.vfs[name].splitlines()
+        else:  # a file the program writes
+            self.writes.setdefault(int(unit), [])
+
+    def record(self, unit, values):
+        self.writes.setdefault(unit if unit == "*" else int(unit), []).append(list(values))
 
     def _read(self, unit, kinds):
         lines = self.files[int(unit)]

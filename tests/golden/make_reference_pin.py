@@ -1,18 +1,24 @@
 """Golden vectors made by the reference itself: PixelFlow's OpenMP programs
-(src/omp_parallel/*.f90 and lib/global.f90, lib/grid.f90), executed from
-their own source text by tests/golden/fortran_subset.py with gfortran's
-plain-FP64 semantics, on small grids for a few steps.
+(src/omp_parallel/*.f90 and lib/global.f90, lib/grid.f90, lib/output.f90),
+executed from their own source text by tests/golden/fortran_subset.py with
+gfortran's plain-FP64 semantics, on small grids for a few steps.
 
 Each case writes tests/golden/refpin_<name>.npz with the porosity values the
 program read (its CSV, written by this repository's writer, which produces
-the reference writer's bytes), the settings, and the fields u, v, [w,] p the
+the reference writer's bytes), the settings, the fields u, v, [w,] p the
 program holds after `steps` time steps (ghost layers included,
-[(k,) j, i] order).  The runs replace only what is not arithmetic: the
-namelist reader (`read_settings` returns the settings below), the output
-routines, `get_now_time` and `system`; the static array sizes md, nd, ld
-are shrunk to the grid (they size storage only).  The main program, the
-grid set-up (which reads the CSV with list-directed input), the initial and
-boundary conditions, solve_p, the matrix edits and the SOR run unchanged.
+[(k,) j, i] order), the porosity-weighted divergence field `div`
+([(k,) j, i], interior only) that output_divergent_2d/3d writes at the end
+of the run, and, for the drag program, the pressure and friction force sums
+`fp`, `fv` (one row per step) that output_force_log_2d prints after every
+step.  The runs replace only what is not arithmetic: the namelist reader
+(`read_settings` returns the settings below), the file and image writers,
+`get_now_time` and `system`; the static array sizes md, nd, ld are shrunk to
+the grid (they size storage only).  The main program, the grid set-up (which
+reads the CSV with list-directed input), the initial and boundary
+conditions, solve_p, the matrix edits, the SOR, the divergence output and
+the force log run unchanged; their `write` statements are recorded as values
+rather than formatted.
 
 Run from the repository root (the reference is not needed afterwards):
 
@@ -44,7 +50,11 @@ CASES = {
     "uniform3d_7x6x5": ("ibm_3d_uniform_omp_cpu.f90", (7, 6, 5), "sph", 3),
     "uniform3d_8x7x6": ("ibm_3d_uniform_omp_cpu.f90", (8, 7, 6), "sph", 2),
     "aircon3d_8x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (8, 7, 6), "room", 3),
+    "drag2d_12x8": ("ibm_2d_drag_omp_cpu.f90", (12, 8), "cyl", 4),
 }
+
+# output routines that run as written (their records are captured)
+INTERPRETED = ("output_divergent_2d", "output_divergent_3d", "output_force_log_2d", "output_force_log_3d")
 
 NAMES = ["xnue", "xlambda", "density", "width", "height", "depth", "time", "inlet_velocity", "outlet_pressure",
          "aoa", "istep_max", "istep_out", "thickness", "threshold", "radius", "center_x", "center_y", "center_z",
@@ -82,7 +92,8 @@ def run_reference(ref_dir, name):
     prog, shape, kind, steps = CASES[name]
     s, shape, vals, steps = case_inputs(name)
     src = os.path.join(ref_dir, "src", "omp_parallel")
-    files = [os.path.join(src, "lib", "global.f90"), os.path.join(src, "lib", "grid.f90"), os.path.join(src, prog)]
+    files = [os.path.join(src, "lib", f) for f in ("global.f90", "grid.f90", "output.f90")]
+    files.append(os.path.join(src, prog))
     texts = [open(f).read() for f in files]
     with tempfile.TemporaryDirectory() as tmp:
         csv = os.path.join(tmp, "porosity.csv")
@@ -92,7 +103,7 @@ def run_reference(ref_dir, name):
     settings = dict(xnue=s.xnue, xlambda=s.xlambda, density=s.density, width=s.width, height=s.height,
                     depth=s.depth, time=s.time, inlet_velocity=s.inlet_velocity, outlet_pressure=s.outlet_pressure,
                     aoa=s.aoa, istep_max=int(s.istep_max), istep_out=10 ** 6, thickness=s.thickness,
-                    threshold=s.threshold, radius=0.0, center_x=0.0, center_y=0.0, center_z=0.0,
+                    threshold=s.threshold, radius=s.radius, center_x=0.0, center_y=0.0, center_z=0.0,
                     nonslip=bool(s.nonslip), output_folder="out", csv_file="porosity.csv",
                     iter_max=int(s.iter_max), relux_factor=s.relux_factor)
 
@@ -105,7 +116,8 @@ def run_reference(ref_dir, name):
     called = set(re.findall(r"\bcall\s+(\w+)", "\n".join(t.lower() for t in texts)))
     probe = Program(texts, overrides=_sizes(shape))
     stubs = {nm: noop for nm in called - set(probe.subs)}
-    stubs.update({nm: noop for nm in called if nm.startswith("output_") or nm in ("get_now_time", "system")})
+    stubs.update({nm: noop for nm in called
+                  if (nm.startswith("output_") and nm not in INTERPRETED) or nm in ("get_now_time", "system")})
     stubs["read_settings"] = read_settings
     P = Program(texts, overrides=_sizes(shape), stubs=stubs)
     P.vfs["porosity.csv"] = csv_text
@@ -114,7 +126,23 @@ def run_reference(ref_dir, name):
     for f in ("u", "v", "w", "p") if len(shape) == 3 else ("u", "v", "p"):
         a = S[f]
         out[f] = np.array(a.data, dtype=np.float64).reshape(a.ext[::-1])
+    out["div"] = _divergence_records(P.writes[63 if len(shape) == 2 else 62], shape)
+    fp = [r[1:] for r in P.writes["*"] if r and r[0] == "Fp ="]
+    fv = [r[1:] for r in P.writes["*"] if r and r[0] == "Fv ="]
+    if fp:
+        out["fp"] = np.array(fp, dtype=np.float64)
+        out["fv"] = np.array(fv, dtype=np.float64)
+        assert len(fp) == steps
     return s, shape, vals_read, steps, out
+
+
+def _divergence_records(recs, shape):
+    """The rows after the 'divergent velocity' record, one per (k,) j."""
+    k = [q for q, r in enumerate(recs) if r == ["divergent velocity"]][-1]
+    rows = int(np.prod(shape[1:]))
+    body = recs[k + 1:k + 1 + rows]
+    assert all(len(r) == shape[0] for r in body)
+    return np.array(body, dtype=np.float64).reshape(shape[::-1])
 
 
 def _sizes(shape):

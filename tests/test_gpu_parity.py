@@ -447,13 +447,31 @@ def test_gpu_matches_the_reference_programs(name):
     """The fields of PixelFlow's own OpenMP programs, executed from their
     Fortran source (tests/golden/refpin_*.npz, see make_reference_pin.py),
     against the GPU step on the same settings and porosity: every field
-    within 1e-12 relative L2 after the programs' few steps."""
+    within 1e-12 relative L2 after the programs' few steps, max|div u|
+    against the divergence the program writes within 1e-8 relative, and the
+    drag program's force log (printed after every step) against pf_forces
+    within 1e-10 of the largest component (the GPU sums in another order)."""
     s, shape, _, steps = refpin_inputs(name)
     ref = np.load(os.path.join(GOLDEN, f"refpin_{name}.npz"))
+    dim = len(shape)
+    fp, fv = [], []
     with Case(s, shape, ref["porosity"]) as c:
         c.initial_conditions()
-        c.step(steps)
+        if "fp" in ref.files:
+            for _ in range(steps):
+                c.step(1)
+                f = c.forces()
+                fp.append(f["Fp"])
+                fv.append(f["Fv"])
+        else:
+            c.step(steps)
         got = c.get_state()
-    dim = len(shape)
+        max_div, _ = c.norms()
     errs = errors(got, {f: ref[f] for f in fields(dim)}, dim)
     assert_each_field(errs, 1e-12)
+    want = float(np.abs(ref["div"]).max())
+    assert abs(max_div - want) <= 1e-8 * want, (max_div, want)
+    if "fp" in ref.files:
+        for got_f, want_f in ((np.array(fp), ref["fp"]), (np.array(fv), ref["fv"])):
+            scale = np.abs(want_f).max(axis=1, keepdims=True)
+            assert np.all(np.abs(got_f - want_f) <= 1e-10 * scale), (got_f, want_f)

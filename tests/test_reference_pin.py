@@ -5,9 +5,12 @@ compute (their Fortran source executed by tests/golden/fortran_subset.py,
 gfortran plain-FP64 semantics, made by tests/golden/make_reference_pin.py):
 the uniform 2D program on even and odd grids (the linear-index colour map's
 odd-m shift included), the backstep program, the uniform 3D program on even
-and odd grids and the air-condition program with its wall table.  The C
-oracle (oracle/pf_oracle.c), given the same settings and the porosity the
-program read, must reproduce every field bit for bit."""
+and odd grids, the air-condition program with its wall table and the drag
+program, with the divergence field each program writes at the end
+(output_divergent_2d/3d) and the drag program's force log after every step
+(output_force_log_2d).  The C oracle (oracle/pf_oracle.c), given the same
+settings and the porosity the program read, must reproduce every field, the
+divergence and the force sums bit for bit."""
 import os
 
 import numpy as np
@@ -30,12 +33,23 @@ def test_oracle_reproduces_the_reference_bit_for_bit(name):
     assert int(ref["steps"]) == steps
     o = OracleCase(s, shape, ref["porosity"])
     o.initialize()
-    o.step(steps)
+    fp, fv = [], []
+    for _ in range(steps):  # the drag program logs the forces after every step
+        o.step(1)
+        a, b = o.forces()
+        fp.append(a[:len(shape)])
+        fv.append(b[:len(shape)])
     fields = ("u", "v", "w", "p") if len(shape) == 3 else ("u", "v", "p")
     for f in fields:
         got = getattr(o, f)
         assert got.shape == ref[f].shape, f
         assert np.array_equal(got, ref[f]), (f, float(np.abs(got - ref[f]).max()))
+    mx, div = o.divergence_diag(want_field=True)
+    interior = div[tuple(slice(1, -1) for _ in shape)]
+    assert np.array_equal(interior, ref["div"]), float(np.abs(interior - ref["div"]).max())
+    assert mx == np.abs(ref["div"]).max()
+    if "fp" in ref.files:
+        assert np.array_equal(np.array(fp), ref["fp"]) and np.array_equal(np.array(fv), ref["fv"])
 
 
 def test_fixture_translator_reproduces_itself():
@@ -47,5 +61,6 @@ def test_fixture_translator_reproduces_itself():
     from tests.golden.make_reference_pin import run_reference
     _, _, _, _, out = run_reference(ref_dir, "uniform2d_9x8")
     ref = load("uniform2d_9x8")
+    assert set(out) == set(ref.files) - {"porosity", "steps"}
     for f, a in out.items():
         assert np.array_equal(a, ref[f]), f
