@@ -238,12 +238,13 @@ def _plain_sequential(items, steps: int):
 
 def bench_batch(ncases: int = 512, steps: int = 20, warmup_steps: int = 2, seed: int = 0,
                 baseline_steps: int = 20, large_cells: int = 100000, plain_value: float = 0.0,
-                schedule_bound: float = 5e-5):
+                schedule_bound: float = 1e-6):
     """The batched form: `ncases` independent 2D cases of uneven size (nx, ny in
     {64, 96, ..., 512}, 1-4 circles/ellipses, Re 50-400 capped at cell
     Reynolds number 2, dt at CFL 0.2 of the predictor's stability limit,
     porosity threshold 0.1), precision form (FP32 sweeps in FP64 defect
-    correction, 4 x 25), advanced by the persistent batch kernel.  Reports
+    correction, the schedule from the autotuner), advanced by the
+    persistent batch kernel.  Reports
     device-timed aggregate Mcell-steps/s over the cases that stay finite and,
     as the comparison, the plain FP64 single-case step run on every case, one
     after another."""
@@ -562,14 +563,15 @@ def run_ours(args):
     line["clocks"] = clocks
     case.close()
     if args.forms and args.precision == "fp64" and args.workload.startswith("spheres3d"):
-        # the precision form on the same case (config 3's 4 x 25 schedule; the
-        # FP32 sweep's form and tile from the autotuner, which also reports
-        # the schedules' speed and error), and the batched form (2D batch)
+        # the precision form on the same case (the FP32 sweep's form and tile
+        # and the outer x inner schedule, at most 4 passes of 25 sweeps, from
+        # the autotuner, which also reports every candidate's speed and
+        # error), and the batched form (2D batch)
         from pixelflow_gb300.autotune import tune_fused, tune_schedule
         ms_ = s.replace(precision="mixed")
         tile, tile_trials = tune_fused(ms_, shape, vals, use_cache=False)
         sched, sched_trials = tune_schedule(ms_, shape, vals, bound=args.schedule_bound, use_cache=False)
-        mc = Case(ms_.replace(**tile), shape, vals)
+        mc = Case(ms_.replace(outer_max=sched[0], inner_sweeps=sched[1], **tile), shape, vals)
         mc.initial_conditions()
         mc.step(args.warmup)
         mc.synchronize()
@@ -591,7 +593,8 @@ def run_ours(args):
         line["forms"] = {"mixed_same_case": {"value": mval, "unit": UNIT, "max_div": mdiv,
                                              "speedup_vs_plain_fp64": mval / value,
                                              "rel_l2_vs_fp64": err, "after_steps": args.warmup + args.steps,
-                                             "schedule": "4 passes x 25 FP32 sweeps, FP64 residual/accumulation",
+                                             "schedule": f"{sched[0]} passes x {sched[1]} FP32 sweeps, "
+                                                         "FP64 residual/accumulation",
                                              "sweep": msweep,
                                              "autotune": {"tile": tile, "tile_trials": tile_trials,
                                                           "schedule_bound": args.schedule_bound,
@@ -632,7 +635,7 @@ def main():
     ap.add_argument("--serving-rates", default="0.5,1,2",
                     help="serving form at these arrival rates (requests/s); empty to skip")
     ap.add_argument("--rate-requests", type=int, default=32, help="requests per arrival rate")
-    ap.add_argument("--schedule-bound", type=float, default=5e-5,
+    ap.add_argument("--schedule-bound", type=float, default=1e-6,
                     help="precision form: the autotuner's bound on the relative L2 error against FP64 when it "
                          "picks the outer x inner schedule")
     args = ap.parse_args()

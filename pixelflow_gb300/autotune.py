@@ -10,9 +10,10 @@
   defect-correction passes x FP32 sweeps per pass, product = iter_max):
   every candidate runs the case for a few steps beside the plain FP64 step,
   and the fastest schedule whose pressure error against FP64 (relative L2)
-  stays within `bound` wins.  The error grows with the sweeps per pass (FP32
-  rounding of the correction is carried until the next FP64 residual), the
-  time with the passes.
+  stays within `bound` wins.  The time grows with the passes; the error,
+  since the FP32 sweep keeps its operator's row sum (pf_cells.cuh), hardly
+  depends on the schedule, so when no candidate meets the bound the fastest
+  of those within twice the smallest error is taken.
 * `tune_batch_schedule`: the same for a batch, on a sample of its cases.
   The serving loop (`serve.Server.tune_schedules`) runs `tune_schedule` once
   per 3D grid size of its requests.
@@ -160,14 +161,25 @@ def _rel_l2(a, b) -> float:
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def _pick(trials, error) -> Tuple[int, int]:
+    """The fastest trial within the bound, else the fastest of those within
+    twice the smallest error (schedules of one accuracy class)."""
+    ok = [t for t in trials if t["within_bound"]]
+    if not ok:
+        floor = min(error(t) for t in trials)
+        ok = [t for t in trials if error(t) <= 2.0 * floor]
+    pick = min(ok, key=lambda t: t["ms"])
+    return pick["outer"], pick["inner"]
+
+
 def tune_schedule(settings, shape, vals, bound: float = 1e-4, steps: int = 5, schedules=SCHEDULES,
                   use_cache: bool = True, shapes=None) -> Tuple[Tuple[int, int], List[dict]]:
     """The fastest outer x inner schedule of the precision form whose
     pressure (and velocity) error against the plain FP64 step after `steps`
     steps from the initial state stays within `bound` (relative L2).  When
-    no candidate meets the bound, the most accurate one is returned.  The
-    case comes from porosity values `vals` or, with `shapes`, from analytic
-    shapes generated on the GPU."""
+    no candidate meets the bound, the fastest of those within twice the
+    smallest error is returned.  The case comes from porosity values `vals`
+    or, with `shapes`, from analytic shapes generated on the GPU."""
     it = int(settings.iter_max)
     cands = [(o, i) for (o, i) in schedules if o * i == it]
     sig = f"schedule:{tuple(shape)}:{it}:{bound:g}:{steps}:{cands}"
@@ -188,9 +200,7 @@ def tune_schedule(settings, shape, vals, bound: float = 1e-4, steps: int = 5, sc
         err = {f: _rel_l2(got[f], ref[f]) for f in ref}
         ms = _case_ms(s, shape, vals, 2, shapes)
         trials.append({"outer": o, "inner": i, "ms": ms, "rel_l2": err, "within_bound": max(err.values()) <= bound})
-    ok = [t for t in trials if t["within_bound"]]
-    pick = min(ok, key=lambda t: t["ms"]) if ok else min(trials, key=lambda t: max(t["rel_l2"].values()))
-    best = (pick["outer"], pick["inner"])
+    best = _pick(trials, lambda t: max(t["rel_l2"].values()))
     if use_cache:
         cache[sig] = {"best": list(best), "trials": trials}
         _save(cache)
@@ -204,7 +214,8 @@ def tune_batch_schedule(cases, bound: float = 1e-4, steps: int = 20, sample: int
     with .settings, .m, .n and .porosity()): on a sample of them, each
     candidate's error against the plain FP64 single-case step after `steps`
     steps, and its device time in the persistent kernel (a batch of the
-    sample); the fastest within `bound` wins (else the most accurate)."""
+    sample); the fastest within `bound` wins (else the fastest within twice
+    the smallest error)."""
     from .batch import Batch
     from .solver import Case
     rng = np.random.default_rng(seed)
@@ -233,9 +244,7 @@ def tune_batch_schedule(cases, bound: float = 1e-4, steps: int = 20, sample: int
         worst = float(max(errs))
         trials.append({"outer": o, "inner": i, "ms": ms, "mcell_steps_per_s": cell_steps / (ms / 1e3) / 1e6,
                        "max_rel_l2": worst, "within_bound": worst <= bound})
-    ok = [t for t in trials if t["within_bound"]]
-    pick = min(ok, key=lambda t: t["ms"]) if ok else min(trials, key=lambda t: t["max_rel_l2"])
-    best = (pick["outer"], pick["inner"])
+    best = _pick(trials, lambda t: t["max_rel_l2"])
     if use_cache:
         cache[sig] = {"best": list(best), "trials": trials}
         _save(cache)

@@ -738,6 +738,16 @@ __device__ __forceinline__ void c_bnd_z(const Geo& g, T* u, T* v, T* w, double* 
 //   a_f = dt/h^2 * max(small, (eps_a+eps_b)/2), ap = -sum a_f (before the
 //   inlet/outlet edits), inlet: a_e += a_w, a_w = 0; outlet: all a_f = 0,
 //   e = (1-w) e + r - (w/ap) sum a_f e_f.
+// Away from the outlet the update is evaluated as
+//   e = e + r + (w/sigma) sum a_f (e_f - e),   sigma = sum a_f = -ap,
+// the same value in exact arithmetic (the inlet edit keeps the sum).  In
+// floats the two differ in what the rounding does to the operator's row sum:
+// with (1-w) and w/ap rounded separately, a correction that is constant
+// across a cell's neighbours is not reproduced, and that relative error of
+// a few 1e-8 in the operator's diagonal acts on the smooth pressure modes
+// that the 100 sweeps of a step never damp (the pressure error against the
+// plain FP64 step is ~100x larger); here a constant correction gives
+// e + r exactly.
 struct DCConst {
   // half face factors 0.5*dt/dx^2 etc. (exact halves of the float dt/dx^2)
   // and twice the porosity floor: kx*max(small, (a+b)*0.5) is computed as
@@ -772,24 +782,21 @@ template <int DIM>
 __device__ __forceinline__ float dc_cell_faces(const DCConst& K, float ae, float aw, float an, float as, float at,
                                                float ab, float xe, float xw, float xn, float xs, float xt,
                                                float xb, float rr, float eold, bool inlet, bool outlet) {
-  const float ap = -ae - aw - an - as - at - ab;
-  float enew = fmaf(K.omw, eold, rr);
-  if (!outlet) {
-    if (inlet) {
-      ae += aw;
-      aw = 0.f;
-    }
-    float t = ae * xe;
-    t = fmaf(aw, xw, t);
-    t = fmaf(an, xn, t);
-    t = fmaf(as, xs, t);
-    if (DIM == 3) {
-      t = fmaf(at, xt, t);
-      t = fmaf(ab, xb, t);
-    }
-    enew = fmaf(-__fdividef(K.omega, ap), t, enew);
+  if (outlet) return fmaf(K.omw, eold, rr);
+  const float sigma = ae + aw + an + as + at + ab;
+  if (inlet) {
+    ae += aw;
+    aw = 0.f;
   }
-  return enew;
+  float t = ae * (xe - eold);
+  t = fmaf(aw, xw - eold, t);
+  t = fmaf(an, xn - eold, t);
+  t = fmaf(as, xs - eold, t);
+  if (DIM == 3) {
+    t = fmaf(at, xt - eold, t);
+    t = fmaf(ab, xb - eold, t);
+  }
+  return fmaf(__fdividef(K.omega, sigma), t, eold + rr);
 }
 
 // One cell of the correction sweep from its loaded operands.  Every form of

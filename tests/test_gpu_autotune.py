@@ -31,11 +31,15 @@ def test_tune_schedule_respects_the_bound():
     fastest = min(trials, key=lambda t: t["ms"])
     assert loose == (fastest["outer"], fastest["inner"])
     tight, trials = A.tune_schedule(s, shape, vals, bound=0.0, steps=3, schedules=scheds, use_cache=False)
-    # nothing meets a zero bound: the most accurate schedule is returned
+    # nothing meets a zero bound: the fastest of the schedules within twice
+    # the smallest error (one accuracy class) is returned
     worst = {(t["outer"], t["inner"]): max(t["rel_l2"].values()) for t in trials}
-    assert tight == min(worst, key=worst.get)
-    # more FP64 corrections, smaller error: the FP32 rounding carried between them shrinks
-    assert worst[(20, 1)] < worst[(1, 20)]
+    ms = {(t["outer"], t["inner"]): t["ms"] for t in trials}
+    floor = min(worst.values())
+    assert tight == min((k for k in worst if worst[k] <= 2 * floor), key=ms.get)
+    print("schedule errors", worst)
+    # the FP32 sweep keeps its operator's row sum, so every schedule stays close to FP64
+    assert max(worst.values()) < 1e-5
 
 
 def test_tune_batch_schedule_on_a_sample():
