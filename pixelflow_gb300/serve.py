@@ -112,21 +112,21 @@ class Server:
 
     def tune_schedules(self, requests: List[Request], bound: float, steps: int = 5,
                        schedules=((1, 100), (2, 50), (4, 25)), use_cache: bool = True) -> Dict[str, list]:
-        """The autotuner's outer x inner schedule for every 3D grid size among
-        `requests` (79 % of the serving mix's work; those cases run as
-        full-GPU step graphs): the fastest candidate whose error against the
-        plain FP64 step after `steps` steps stays within `bound`, tuned on the
-        first request of that size.  Later admissions of that size use it."""
+        """The autotuner's outer x inner schedule for every grid size among
+        `requests`: the fastest candidate whose error against the plain FP64
+        step after `steps` steps stays within `bound` (else the fastest of
+        the most accurate class), tuned as a single-case step on the first
+        request of that size.  Later admissions of that size use it."""
         from .autotune import tune_schedule
         out = {}
         for r in requests:
             key = (r.dim, tuple(r.shape))
-            if r.dim != 3 or key in self.schedules:
+            if key in self.schedules:
                 continue
             best, trials = tune_schedule(r.settings, r.shape, None, bound=bound, steps=steps, schedules=schedules,
                                          use_cache=use_cache, shapes=to_pf_shapes(r.shapes, r.dim))
             self.schedules[key] = tuple(best)
-            out[f"3D {r.shape[0]}"] = [list(best), [[t["outer"], t["inner"], round(t["ms"], 3),
+            out[f"{r.dim}D {r.shape[0]}"] = [list(best), [[t["outer"], t["inner"], round(t["ms"], 3),
                                                      max(t["rel_l2"].values())] for t in trials]]
         return out
 

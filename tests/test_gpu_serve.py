@@ -56,25 +56,23 @@ def test_served_results_equal_single_runs(policy):
     assert summ["requests"] == len(reqs) and summ["p99_latency_s"] >= summ["p50_latency_s"]
 
 
-def test_tuned_schedules_apply_to_3d_admissions():
-    """tune_schedules picks an outer x inner schedule per 3D grid size (2D
-    sizes keep their own); every served 3D result then equals the single run
-    under the tuned schedule, bit for bit."""
+def test_tuned_schedules_apply_to_admissions():
+    """tune_schedules picks an outer x inner schedule per grid size, 2D and
+    3D; every served result then equals the single run under the tuned
+    schedule, bit for bit."""
     reqs = _small_requests()
     cands = ((1, 20), (2, 10), (4, 5))
     with Server(chunk=4, policy="srpt_fill", round_cells=20_000, round_ms=2.0) as srv:
         tuned = srv.tune_schedules(reqs, bound=1e-2, steps=3, schedules=cands, use_cache=False)
-        sizes3 = {tuple(q.shape) for q in reqs if q.dim == 3}
-        assert sizes3 and set(k[1] for k in srv.schedules) == sizes3
-        assert all(k[0] == 3 and v in cands for k, v in srv.schedules.items())
-        assert len(tuned) == len(sizes3)
+        sizes = {(q.dim, tuple(q.shape)) for q in reqs}
+        assert {d for d, _ in sizes} == {2, 3} and set(srv.schedules) == sizes
+        assert all(v in cands for v in srv.schedules.values())
+        assert len(tuned) == len(sizes)
         res = srv.run(reqs, realtime=False)
         chosen = dict(srv.schedules)
     for r, q in zip(res, reqs):
-        s = q.settings
-        if q.dim == 3:
-            o, i = chosen[(3, tuple(q.shape))]
-            s = s.replace(outer_max=o, inner_sweeps=i)
+        o, i = chosen[(q.dim, tuple(q.shape))]
+        s = q.settings.replace(outer_max=o, inner_sweeps=i)
         with Case.from_shapes(s, q.shape, q.shapes) as c:
             c.initial_conditions()
             c.step(q.steps)
