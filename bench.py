@@ -422,6 +422,10 @@ def run_ours(args):
     s, shape, vals, desc = workload(args.workload, args.precision)
     if args.precision == "mixed":
         s = s.replace(sweep_form=args.sweep_form)
+        if args.schedule:
+            o, i = (int(x) for x in args.schedule.lower().split("x"))
+            s = s.replace(outer_max=o, inner_sweeps=i)
+            desc.update(outer_passes=o, inner_sweeps=i)
     cells = int(np.prod(shape))
     case = Case(s, shape, vals)
     case.initial_conditions()
@@ -628,6 +632,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--sweep-form", default="auto", choices=["auto", "split", "fused"],
                     help="precision form: the FP32 sweep's form (auto: timed on the case at creation)")
+    ap.add_argument("--schedule", default="",
+                    help="precision form: outer passes x FP32 sweeps per pass, e.g. 1x100 (default: 4x25)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", type=int, default=1, help="also measure the precision and batched forms")
     ap.add_argument("--no-batch", action="store_true")
