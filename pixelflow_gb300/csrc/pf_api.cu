@@ -113,6 +113,9 @@ int make_scal(const pf_params& p, Scal& s) {
   s.iso = p.dim == 3 && s.dx == s.dy && s.dx == s.dz;
   s.dtnu = s.dt * s.xnue;
   s.dtnl = s.dt * (s.xnue + s.xlambda);
+  s.mdt_h = -s.dt * s.hx;
+  s.dtnu_i2 = s.dtnu * s.ix2;
+  s.dtnl_h = s.dtnl * s.hx;
   const double cdt = s.dt / s.density;
   s.pgx = cdt * 0.5 / s.dx;
   s.pgy = cdt * 0.5 / s.dy;

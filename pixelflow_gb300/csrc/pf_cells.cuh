@@ -403,6 +403,26 @@ __device__ __forceinline__ void c_predictor(Geo g, Scal s, const T* __restrict__
     const T ut = uo[q + XY], ub = uo[q - XY], vt = vo[q + XY], vb = vo[q - XY];
     const T wc = wo[q], we = wo[q + 1], ww = wo[q - 1], wn = wo[q + X], ws = wo[q - X];
     const T wt = wo[q + XY], wb = wo[q - XY];
+    if (FLUID && sizeof(T) == sizeof(double) && s.iso) {
+      // Fluid warps of an isotropic FP64 grid: with hx = hy = hz the
+      // convective differences share one factor, folded with -dt into one
+      // constant, as are dt*nu with 1/dx^2 and dt*(nu+lambda) with 0.5/dx
+      // (computed once on the host): 12 FP64 operations per component
+      // instead of 17 on the FP64-bound predictor.  Different roundings
+      // than the factored form only in the last bits.
+      const T a = (T)s.mdt_h, b = (T)s.dtnu_i2, d = (T)s.dtnl_h;
+      T conv = fma(wc, ut - ub, fma(vc, un - us, uc * (ue - uw)));
+      T t = fma(b, lap6_iso<T>(uc, ue, uw, un, us, ut, ub), a * conv);
+      u[q] = su[q] + (TS)fma(d, dE - dW, t);
+      conv = fma(wc, vt - vb, fma(vc, vn - vs, uc * (ve - vw)));
+      t = fma(b, lap6_iso<T>(vc, ve, vw, vn, vs, vt, vb), a * conv);
+      v[q] = sv[q] + (TS)fma(d, dN - dS, t);
+      conv = fma(wc, wt - wb, fma(vc, wn - ws, uc * (we - ww)));
+      t = fma(b, lap6_iso<T>(wc, we, ww, wn, ws, wt, wb), a * conv);
+      w[q] = sw[q] + (TS)fma(d, dT - dB, t);
+      keep_ghosts<TS, DIM>(g, i, j, k, q, su, sv, sw, u, v, w);
+      return;
+    }
     const T duz = (ut - ub) * hz, dvz = (vt - vb) * hz;
     const T dwx = (we - ww) * hx, dwy = (wn - ws) * hy, dwz = (wt - wb) * hz;
     const T luz = fma(-two, uc, ut + ub), lvz = fma(-two, vc, vt + vb);

@@ -89,6 +89,9 @@ struct Scal {
   double ix2, iy2, iz2;  // 1/(dx*dx), ...
   int iso;               // 3D with dx = dy = dz: the three Laplacian factors are one
   double dtnu, dtnl;     // dt*nu, dt*(nu+lambda)
+  // iso only (hx = hy = hz, ix2 = iy2 = iz2): -dt*hx, dtnu*ix2, dtnl*hx, the
+  // factors of the fluid warps' predictor with the constants folded
+  double mdt_h, dtnu_i2, dtnl_h;
   double pgx, pgy, pgz;  // dt/density*0.5/dx, ... (projection)
   float hxf, hyf, hzf, ix2f, iy2f, iz2f, dtf, nuf, lamf, dtnuf, dtnlf, pgxf, pgyf, pgzf;
   // non-null (the case's natural porosity array): inflow and initial
