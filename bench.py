@@ -547,9 +547,9 @@ def run_ours(args):
            "d2h_bytes_per_step": nbytes, "call": "pf_step_host", "calls": ncalls,
            "three_calls": world * cells * ncalls / three_s / 1e6,
            "per_call_ms": {"pf_step_host": {"median": statistics.median(calls_a), "min": min(calls_a),
-                                            "max": max(calls_a)},
+                                            "max": max(calls_a), "all": [round(x, 2) for x in calls_a]},
                            "three_calls": {"median": statistics.median(calls_b), "min": min(calls_b),
-                                           "max": max(calls_b)}}}
+                                           "max": max(calls_b), "all": [round(x, 2) for x in calls_b]}}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms / args.steps, "higher_is_better": True,
