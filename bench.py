@@ -26,6 +26,7 @@ on all host cores for the same workload and metric.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -519,10 +520,17 @@ def run_ours(args):
         case.get_state(out)
     barrier(world)
     calls_a, calls_b = [], []
-    # at least 40 calls (~1 s at 256^3): a single stall of the shared host
-    # (50-125 ms, seen in either form at random) then moves the mean by a few
-    # per cent instead of a third; the per-call statistics are reported too
+    # at least 40 calls (~1 s at 256^3); the per-call times are reported too
+    # (on the shared box a call now and then stalls for 75-150 ms in either
+    # form, the host side; the device-timed steps show no such outliers).
+    # Python's cyclic garbage collector is off while the calls are timed: a
+    # full collection of this process's heap (torch loaded) takes ~30 ms on
+    # the machine's host, a pause of the measuring harness that the library's
+    # own callers (a Fortran program through the C ABI) do not have.
+    # Reference counting still frees everything the loop allocates.
     ncalls = max(args.steps, 40)
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     for _ in range(ncalls):
         ta = time.perf_counter()
@@ -540,6 +548,7 @@ def run_ours(args):
         calls_b.append(1e3 * (time.perf_counter() - ta))
     t1 = time.perf_counter()
     three_s = reduce_max(t1 - t0, world)
+    gc.enable()
     for a in list(host.values()) + list(out.values()):
         host_unregister(a)
     nbytes = sum(a.nbytes for a in host.values())
