@@ -170,6 +170,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def stage_roofline(stage_ms, steps, cells, dim, s, precision, peak, peak_kind):
+    """HBM roofline of every stage of the step: device time per step (CUDA
+    events between the stages), the stage's algorithmic bytes per step
+    (words per cell: predictor 7 (2D 5), RHS 5 (4), SOR 5 per iteration,
+    projection + boundary 7 (5); FP64 words of 8 B, and in the precision
+    form FP32 words of 4 B for the predictor's stencils and the sweeps), and
+    the achieved fraction of the measured HBM copy peak."""
+    sweeps = s.iter_max if precision == "fp64" else s.outer_max * s.inner_sweeps
+    w8, w4 = 8, (8 if precision == "fp64" else 4)
+    words = {"predictor": ((7 if dim == 3 else 5), w4), "rhs": ((5 if dim == 3 else 4), w8),
+             "sor": (5 * sweeps, w4), "projection_boundary": ((7 if dim == 3 else 5), w8)}
+    out = {}
+    for k, ms in stage_ms.items():
+        per_step = ms / max(steps, 1)
+        nw, wsz = words[k]
+        alg = cells * nw * wsz
+        gbs = alg / (per_step / 1e3) / 1e9 if per_step > 0 else 0.0
+        out[k] = {"ms_per_step": per_step, "alg_bytes_per_step": alg, "achieved_gbs": gbs,
+                  "frac": gbs / peak if peak else None}
+    out["peak_gbs"] = peak
+    out["peak_source"] = peak_kind
+    return out
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -447,6 +471,7 @@ def run_ours(args):
     clocks = sampler.stop()
     step_ms = reduce_max(prof["step_ms"], world)
     per_step = case.profile_step_times()
+    stage_ms = case.profile_stages()
     value = world * cells * args.steps / (step_ms / 1e3) / 1e6
     max_div, sor_err = case.norms()
     # the plain state after warmup + steps, for the precision form's error below
@@ -571,6 +596,7 @@ def run_ours(args):
     line["max_div"] = max_div
     line["sor_error"] = sor_err
     line["roofline"] = roofline
+    line["stages"] = stage_roofline(stage_ms, prof["steps"], cells, len(shape), s, args.precision, peak, peak_kind)
     line["e2e"] = e2e
     line["gpu_launches"] = launches
     line["clocks"] = clocks

@@ -224,6 +224,14 @@ int pf_profile_end(pf_case *c, double *sor_ms, int64_t *sor_launches, double *st
  * values; *n receives the count written. */
 int pf_profile_step_times(pf_case *c, double *ms, int64_t max_steps, int64_t *n);
 
+/* The last profiling session's device time (ms, summed over its steps) of
+ * the step's four stages, in the order of the reference's loop body:
+ * ms[0] divergence + predictor, ms[1] the Poisson right-hand side (and, in
+ * the precision form, nothing else), ms[2] the SOR (every half-sweep with
+ * its halo updates; the precision form's passes of FP64 residual, FP32
+ * sweeps and FP64 accumulation), ms[3] projection + boundary. */
+int pf_profile_stages(pf_case *c, double ms[4]);
+
 /* Number of kernels this case has launched (graph replays count every
  * kernel node), for accounting in benchmarks. */
 int pf_kernel_launches(pf_case *c, int64_t *count);

@@ -104,6 +104,7 @@ _PROTOS = {
     "pf_profile_end": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_D),
                             ctypes.POINTER(ctypes.c_int64)]),
     "pf_profile_step_times": (_I, [_VP, _VP, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "pf_profile_stages": (_I, [_VP, _VP]),
     "pf_kernel_launches": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "pf_memory_bytes": (_I, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     "pf_debug_fused_drop_stage": (_I, [_VP, _I]),

@@ -295,6 +295,7 @@ static void enqueue_solve_p(pf_case* c, bool prof, bool head) {
     launch_predictor<double, double>(g, s, c->U[o], c->V[o], c->W[o], c->div, c->gx, c->gy, c->gz, c->rinv,
                                      c->damp, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
   }
+  if (prof) cudaEventRecord(c->ev_cur[4], st);
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);
@@ -954,9 +955,11 @@ int pf_step(pf_case* c, int nsteps) {
   if (nsteps < 0) return fail(PF_E_INVALID, "nsteps < 0");
   for (int s = 0; s < nsteps; s++) {
     if (c->profiling) {
-      int rc = ensure_events(c, (size_t)(c->prof_steps + 1) * 4);
+      // per step: [0] start, [4] after the predictor, [1] after the RHS,
+      // [2] after the SOR, [3] end
+      int rc = ensure_events(c, (size_t)(c->prof_steps + 1) * pf_case::PROF_EVENTS);
       if (rc) return rc;
-      cudaEvent_t* ev = &c->events[(size_t)c->prof_steps * 4];
+      cudaEvent_t* ev = &c->events[(size_t)c->prof_steps * pf_case::PROF_EVENTS];
       c->ev_cur = ev;
       cudaEventRecord(ev[0], c->st);
       enqueue_step(c, true);
@@ -1057,13 +1060,21 @@ int pf_profile_end(pf_case* c, double* sor_ms, int64_t* sor_launches, double* st
   PF_CUDA(cudaStreamSynchronize(c->st));
   double sor = 0, step = 0;
   c->step_times.clear();
+  for (double& x : c->stage_ms) x = 0.0;
   for (int64_t s = 0; s < c->prof_steps; s++) {
-    float a = 0, b = 0;
-    cudaEvent_t* ev = &c->events[(size_t)s * 4];
+    float a = 0, b = 0, t0 = 0, t1 = 0, t3 = 0;
+    cudaEvent_t* ev = &c->events[(size_t)s * pf_case::PROF_EVENTS];
     PF_CUDA(cudaEventElapsedTime(&a, ev[1], ev[2]));
     PF_CUDA(cudaEventElapsedTime(&b, ev[0], ev[3]));
+    PF_CUDA(cudaEventElapsedTime(&t0, ev[0], ev[4]));
+    PF_CUDA(cudaEventElapsedTime(&t1, ev[4], ev[1]));
+    PF_CUDA(cudaEventElapsedTime(&t3, ev[2], ev[3]));
     sor += a;
     step += b;
+    c->stage_ms[0] += t0;
+    c->stage_ms[1] += t1;
+    c->stage_ms[2] += a;
+    c->stage_ms[3] += t3;
     c->step_times.push_back(b);
   }
   if (sor_ms) *sor_ms = sor;
@@ -1071,6 +1082,12 @@ int pf_profile_end(pf_case* c, double* sor_ms, int64_t* sor_launches, double* st
   if (steps) *steps = c->prof_steps;
   if (sor_launches) *sor_launches = c->prof_steps * c->sor_launches_per_step();
   c->profiling = false;
+  return PF_OK;
+}
+
+int pf_profile_stages(pf_case* c, double* ms) {
+  if (!c || !ms) return fail(PF_E_INVALID, "null argument");
+  for (int k = 0; k < 4; k++) ms[k] = c->stage_ms[k];
   return PF_OK;
 }
 

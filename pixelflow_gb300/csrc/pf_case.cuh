@@ -28,12 +28,14 @@ struct pf_case {
   // step graphs [part][buffer]: part 0 the whole step, part 1 the step after
   // the predictor (pf_step_host issues the divergence and predictor itself)
   cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  // profiling
+  // profiling: PROF_EVENTS events per profiled step
+  static constexpr int PROF_EVENTS = 5;
   bool profiling = false;
   int64_t prof_steps = 0;
   std::vector<cudaEvent_t> events;
   cudaEvent_t* ev_cur = nullptr;
   std::vector<double> step_times;  // ms, last profiling session
+  double stage_ms[4] = {0, 0, 0, 0};  // predictor, RHS, SOR, projection + boundary (pf_profile_stages)
   int64_t launches = 0;            // kernels launched so far
   // asynchronous snapshots (pf_snapshot_begin / _wait), allocated on first use:
   // dense (m+2)(n+2)[(l+2)] copies of u, v, [w,] p on the device and pinned

@@ -172,6 +172,7 @@ void enqueue_solve_p_mixed(pf_case* c, bool prof) {
   launch_divergence<float>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, st);
   launch_predictor<float, double>(g, s, c->Uf[0], c->Vf[0], c->Wf[0], c->divf, c->gxf, c->gyf, c->gzf, c->rinvf,
                                   c->dampf, c->U[o], c->V[o], c->W[o], c->U[nw], c->V[nw], c->W[nw], st);
+  if (prof) cudaEventRecord(c->ev_cur[4], st);
   launch_rhs<double>(g, s, c->U[nw], c->V[nw], c->W[nw], c->poro, c->gx, c->gy, c->gz, c->C[0], c->C[1], st);
   if (prof) cudaEventRecord(c->ev_cur[1], st);
   const bool halo = periodic_halo(g);

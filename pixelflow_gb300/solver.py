@@ -336,6 +336,14 @@ class Case:
         check(self.L.pf_profile_end(self.h, ctypes.byref(sor), ctypes.byref(nl), ctypes.byref(st), ctypes.byref(ns)))
         return dict(sor_ms=sor.value, sor_launches=nl.value, step_ms=st.value, steps=ns.value)
 
+    def profile_stages(self) -> Dict[str, float]:
+        """Device time (ms, summed over the last profiling session's steps)
+        of the step's stages: divergence + predictor, RHS, SOR (all passes),
+        projection + boundary."""
+        ms = np.zeros(4)
+        check(self.L.pf_profile_stages(self.h, _ptr(ms)))
+        return dict(zip(("predictor", "rhs", "sor", "projection_boundary"), ms.tolist()))
+
 
 def host_register(a: np.ndarray):
     check(_lib.load().pf_host_register(_ptr(a), a.nbytes))

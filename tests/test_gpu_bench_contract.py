@@ -1,8 +1,8 @@
 """bench.py's JSON line on a small workload: every key of the contract
 (metric, value, unit, n_gpus, steps, warmup, ms_per_step, higher_is_better,
 scaling, vs_baseline, dtype, data, config, e2e with its byte counts,
-gpu_launches, clocks, roofline with traffic and peak, cpu_baseline) with
-sane values, for the plain and the precision form."""
+gpu_launches, clocks, roofline with traffic and peak, cpu_baseline, and the
+per-stage roofline) with sane values, for the plain and the precision form."""
 import json
 import os
 import subprocess
@@ -45,6 +45,11 @@ def test_bench_line_contract(args):
     assert rf["bound"] in ("hbm", "tensor") and rf["unit"] == "GB/s"
     assert rf["achieved"] > 0 and rf["peak"] > 0 and abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-9
     assert "traffic" in rf
+    st = d["stages"]
+    stages = ("predictor", "rhs", "sor", "projection_boundary")
+    assert all(st[k]["ms_per_step"] > 0 and st[k]["achieved_gbs"] > 0 for k in stages)
+    assert abs(sum(st[k]["ms_per_step"] for k in stages) - d["ms_per_step"]) <= 0.01 * d["ms_per_step"] + 0.01
+    assert st["peak_gbs"] == rf["peak"]
     if "--precision" in args:
         assert d["dtype"] == "f32+f64" and rf["kernel"] == "k_sor_fused3"
         assert rf["cell_updates_per_launch"] == 64 ** 3  # one launch per full sweep
