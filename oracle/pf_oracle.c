@@ -13,7 +13,8 @@
  * (tests/golden/fortran_subset.py, gfortran plain-FP64 semantics; fixtures
  * tests/golden/refpin_*.npz): this restatement reproduces their fields,
  * their divergence output and the drag program's force log bit for bit
- * (uniform 2D and 3D on even and odd grids, backstep, air-condition, drag;
+ * (uniform 2D and 3D on even and odd grids, backstep, air-condition, drag,
+ * and the uniform 2D program with its commented symmetry rows enabled;
  * tests/test_reference_pin.py).  It is also cross-checked
  * against an independent numpy restatement (oracle/np_oracle.py) and
  * physical invariants (tests/).

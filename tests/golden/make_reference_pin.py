@@ -18,7 +18,9 @@ the grid (they size storage only).  The main program, the grid set-up (which
 reads the CSV with list-directed input), the initial and boundary
 conditions, solve_p, the matrix edits, the SOR, the divergence output and
 the force log run unchanged; their `write` statements are recorded as values
-rather than formatted.
+rather than formatted.  The slip cases run the uniform 2D program with the
+symmetry rows its source keeps commented out enabled (enable_slip), the
+option this repository exposes as `slip_y`.
 
 Run from the repository root (the reference is not needed afterwards):
 
@@ -51,7 +53,18 @@ CASES = {
     "uniform3d_8x7x6": ("ibm_3d_uniform_omp_cpu.f90", (8, 7, 6), "sph", 2),
     "aircon3d_8x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (8, 7, 6), "room", 3),
     "drag2d_12x8": ("ibm_2d_drag_omp_cpu.f90", (12, 8), "cyl", 4),
+    # the uniform 2D program with its commented symmetry ("slip") rows enabled
+    "slip2d_12x8": ("ibm_2d_uniform_omp_cpu.f90", (12, 8), "cyl_slip", 3),
+    "slip2d_13x9": ("ibm_2d_uniform_omp_cpu.f90", (13, 9), "cyl_slip", 3),
 }
+
+# The commented blocks that make up the 2D symmetry option, by the comment
+# line that heads each (ibm_2d_uniform_omp_cpu.f90: boundrary_matrix :440-450,
+# boundary :512-526); enable_slip() removes the leading "!" of the block's
+# statements.
+SLIP_HEADS = ("! symmetry or wall (dp/dy=0. at j=1)", "! symmetry or wall  (dp/dy=0. at j=n)",
+              "! option: symmetry (du/dy=0., v=0., dp/dy=0. at j=1)",
+              "! option: symmetry  (du/dy=0., v=0., dp/dy=0. at j=n)")
 
 # output routines that run as written (their records are captured)
 INTERPRETED = ("output_divergent_2d", "output_divergent_3d", "output_force_log_2d", "output_force_log_3d")
@@ -64,9 +77,9 @@ NAMES = ["xnue", "xlambda", "density", "width", "height", "depth", "time", "inle
 def case_inputs(name):
     """(settings, shape, porosity values before the CSV round trip, steps)."""
     prog, shape, kind, steps = CASES[name]
-    if kind in ("cyl", "step"):
+    if kind in ("cyl", "step", "cyl_slip"):
         m, n = shape
-        s = G.settings_cylinder_2d(iter_max=7)
+        s = G.settings_cylinder_2d(iter_max=7, slip_y=kind == "cyl_slip")
         vals = G.cylinder_2d(m, n, radius=0.2, cx=0.6, cy=0.45)
         if kind == "step":  # an obstacle across the inlet: a non-uniform inflow profile
             vals = np.minimum(vals, G.cylinder_2d(m, n, radius=0.3, cx=0.0, cy=0.3))
@@ -88,6 +101,26 @@ def case_inputs(name):
     return s, shape, vals, steps
 
 
+def enable_slip(text):
+    """The program text with the commented statements under each SLIP_HEADS
+    comment enabled (up to the next line that is not a commented statement)."""
+    lines = text.splitlines()
+    out, on, found = [], False, 0
+    for ln in lines:
+        st = ln.strip()
+        if any(st.startswith(h) for h in SLIP_HEADS):
+            on, found = True, found + 1
+            out.append(ln)
+            continue
+        if on and st.startswith("!") and not st.startswith("! -") and len(st) > 1:
+            out.append(ln.replace("!", "", 1))
+            continue
+        on = False
+        out.append(ln)
+    assert found == len(SLIP_HEADS), found
+    return "\n".join(out) + "\n"
+
+
 def run_reference(ref_dir, name):
     prog, shape, kind, steps = CASES[name]
     s, shape, vals, steps = case_inputs(name)
@@ -95,6 +128,8 @@ def run_reference(ref_dir, name):
     files = [os.path.join(src, "lib", f) for f in ("global.f90", "grid.f90", "output.f90")]
     files.append(os.path.join(src, prog))
     texts = [open(f).read() for f in files]
+    if kind == "cyl_slip":
+        texts[-1] = enable_slip(texts[-1])
     with tempfile.TemporaryDirectory() as tmp:
         csv = os.path.join(tmp, "porosity.csv")
         C.write_porosity_csv(csv, vals)

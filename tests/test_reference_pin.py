@@ -5,8 +5,9 @@ compute (their Fortran source executed by tests/golden/fortran_subset.py,
 gfortran plain-FP64 semantics, made by tests/golden/make_reference_pin.py):
 the uniform 2D program on even and odd grids (the linear-index colour map's
 odd-m shift included), the backstep program, the uniform 3D program on even
-and odd grids, the air-condition program with its wall table and the drag
-program, with the divergence field each program writes at the end
+and odd grids, the air-condition program with its wall table, the drag
+program and the uniform 2D program with its commented symmetry ("slip")
+rows enabled, with the divergence field each program writes at the end
 (output_divergent_2d/3d) and the drag program's force log after every step
 (output_force_log_2d).  The C oracle (oracle/pf_oracle.c), given the same
 settings and the porosity the program read, must reproduce every field, the
