@@ -41,6 +41,13 @@ from pixelflow_gb300 import geometry as G  # noqa: E402
 from tests.golden.fortran_subset import Program  # noqa: E402
 
 AIR_CONDITION_TABLE = (1, 0, 0, 0, 0, 2)  # top, bottom, east, west, north, south
+# other wall tables of the air-condition program, set through its integer
+# parameters top_wall .. north_wall (0 wall, 1 inlet, 2 outlet); the second
+# has outlets on the top (its bb starts from plane 1) and west faces and
+# inlets on the east and north faces
+WALL_TABLES = {"aircon3d_bottom_in_east_out_8x7x6": (0, 1, 2, 0, 0, 0),
+               "aircon3d_mixed_faces_9x7x6": (2, 0, 1, 2, 1, 0)}
+WALL_PARAMS = ("top_wall", "bottom_wall", "east_wall", "west_wall", "north_wall", "south_wall")
 
 # name -> (program file, dim, shape, settings builder, steps)
 CASES = {
@@ -52,6 +59,8 @@ CASES = {
     "uniform3d_7x6x5": ("ibm_3d_uniform_omp_cpu.f90", (7, 6, 5), "sph", 3),
     "uniform3d_8x7x6": ("ibm_3d_uniform_omp_cpu.f90", (8, 7, 6), "sph", 2),
     "aircon3d_8x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (8, 7, 6), "room", 3),
+    "aircon3d_bottom_in_east_out_8x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (8, 7, 6), "room", 3),
+    "aircon3d_mixed_faces_9x7x6": ("ibm_3d_air_condition_omp_cpu.f90", (9, 7, 6), "room", 3),
     "drag2d_12x8": ("ibm_2d_drag_omp_cpu.f90", (12, 8), "cyl", 4),
     # the uniform 2D program with its commented symmetry ("slip") rows enabled
     "slip2d_12x8": ("ibm_2d_uniform_omp_cpu.f90", (12, 8), "cyl_slip", 3),
@@ -88,7 +97,8 @@ def case_inputs(name):
     else:
         m, n, l = shape
         if kind == "room":
-            s = G.settings_spheres_3d(iter_max=5, walls=AIR_CONDITION_TABLE, inlet_velocity=0.5)
+            s = G.settings_spheres_3d(iter_max=5, walls=WALL_TABLES.get(name, AIR_CONDITION_TABLE),
+                                      inlet_velocity=0.5)
             vals = G.spheres_3d(m, n, l, spheres=np.array([[0.5, 0.5, 0.4, 0.2]]))
             vals[-1, : n // 2, : m // 2] = 0.05
             vals[:, 0, m // 2:] = 0.05
@@ -148,13 +158,16 @@ def run_reference(ref_dir, name):
     def noop(P, *args):
         return None
 
+    overrides = _sizes(shape)
+    if kind == "room":
+        overrides.update(zip(WALL_PARAMS, WALL_TABLES.get(name, AIR_CONDITION_TABLE)))
     called = set(re.findall(r"\bcall\s+(\w+)", "\n".join(t.lower() for t in texts)))
-    probe = Program(texts, overrides=_sizes(shape))
+    probe = Program(texts, overrides=overrides)
     stubs = {nm: noop for nm in called - set(probe.subs)}
     stubs.update({nm: noop for nm in called
                   if (nm.startswith("output_") and nm not in INTERPRETED) or nm in ("get_now_time", "system")})
     stubs["read_settings"] = read_settings
-    P = Program(texts, overrides=_sizes(shape), stubs=stubs)
+    P = Program(texts, overrides=overrides, stubs=stubs)
     P.vfs["porosity.csv"] = csv_text
     S = P.run_main()
     out = {}

@@ -5,7 +5,8 @@ compute (their Fortran source executed by tests/golden/fortran_subset.py,
 gfortran plain-FP64 semantics, made by tests/golden/make_reference_pin.py):
 the uniform 2D program on even and odd grids (the linear-index colour map's
 odd-m shift included), the backstep program, the uniform 3D program on even
-and odd grids, the air-condition program with its wall table, the drag
+and odd grids, the air-condition program with its own wall table and two
+others (set through its wall parameters), the drag
 program and the uniform 2D program with its commented symmetry ("slip")
 rows enabled, with the divergence field each program writes at the end
 (output_divergent_2d/3d) and the drag program's force log after every step
