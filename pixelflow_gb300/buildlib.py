@@ -3,11 +3,17 @@
 Each .cu file under csrc/ is compiled in parallel to an object file, then the
 objects are linked into pixelflow_gb300/libpixelflow_gb300.so.  No torch, no
 cmake: plain nvcc, so the same recipe runs on x86-64 and aarch64 hosts.
+
+The C++ host program host/pf_run.cpp (the reference's main program over the
+C ABI) is then linked against that library as pixelflow_gb300/pf_run, with
+-ffp-contract=off so that its text output has the same bits on x86-64 and
+aarch64.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import shutil
 import subprocess
 import sys
 
@@ -15,6 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpixelflow_gb300.so")
+HOST_SRC = os.path.join(HERE, "host", "pf_run.cpp")
+HOST_BIN = os.path.join(HERE, "pf_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
            "--expt-relaxed-constexpr"]
@@ -51,7 +59,36 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in sources() + _headers())
 
 
+def build_host(force: bool = False, verbose: bool = False) -> str:
+    """Link host/pf_run.cpp against libpixelflow_gb300.so (g++, C++17)."""
+    header = os.path.join(os.path.dirname(HERE), "include", "pixelflow_gpu.h")
+    if (not force and os.path.exists(HOST_BIN)
+            and all(os.path.getmtime(f) <= os.path.getmtime(HOST_BIN) for f in (HOST_SRC, header, LIB))):
+        return HOST_BIN
+    cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
+    tmp = HOST_BIN + ".tmp"
+    common = ["-O2", "-std=c++17", "-I", os.path.dirname(header), HOST_SRC, "-o", tmp, "-L", HERE,
+              "-lpixelflow_gb300"]
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if cxx:
+        cmd = [cxx, *common, "-Wall", "-ffp-contract=off", "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath-link,{cuda_lib}"]
+    else:  # nvcc hands a .cpp file to its own host compiler
+        cmd = [_nvcc(), *common, "-Xcompiler", "-Wall,-ffp-contract=off", "-Xlinker", "-rpath,$ORIGIN",
+               "-Xlinker", f"-rpath-link,{cuda_lib}"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.check_call(cmd)
+    os.replace(tmp, HOST_BIN)
+    return HOST_BIN
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
+    lib = build_lib(force=force, verbose=verbose)
+    build_host(force=force, verbose=verbose)
+    return lib
+
+
+def build_lib(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
         return LIB
     os.makedirs(OBJDIR, exist_ok=True)
