@@ -9,12 +9,14 @@
 // lib/grid.f90:36-47, 281-294), set the initial and boundary conditions, write
 // the legacy-VTK file of step 0, then run istep_max steps, writing the VTK file
 // every istep_out steps (output_paraview_temp_2d/_3d, lib/output.f90:421-537,
-// 968-1088).  This program does the same from a project directory:
+// 968-1088), and end with the same file of the final state as
+// output_paraview.vtk (output_paraview_2d/_3d, :307-419, :800-910).  This
+// program does the same from a project directory:
 //
 //   pf_run [--project DIR] [--steps N] [--device D] [--force-log]
 //          [--save-state FILE] [--restart STATE] [--no-vtk]
 //   pf_run [--project DIR] --print-config [--dump-porosity FILE]
-//   pf_run [--project DIR] --vtk-from STATE [--istep K]
+//   pf_run [--project DIR] --vtk-from STATE [--istep K | --final]
 //
 // The step runs on the GPU through libpixelflow_gb300.so; VTK output uses the
 // asynchronous snapshots (pf_snapshot_begin/_wait), so a file is written while
@@ -634,7 +636,11 @@ std::vector<double> node_coords(int count, double length, double centre) {
   return x;
 }
 
-void write_vtk(const std::string& path, const State& st, const std::vector<double>& poro, const Settings& s) {
+// final: the file of the end of the run (output_paraview_2d/_3d,
+// output.f90:307-419, :793-910), whose 3D form writes porosity after
+// VelocityDivergent instead of before pressure; the 2D form is the same text.
+void write_vtk(const std::string& path, const State& st, const std::vector<double>& poro, const Settings& s,
+               bool final = false) {
   const int dim = st.dim, m = st.m, n = st.n, l = dim == 3 ? st.l : 1;
   const size_t X = m + 2, Y = n + 2;
   const std::vector<double> xs = node_coords(m, s.width, s.center_x);
@@ -695,9 +701,13 @@ void write_vtk(const std::string& path, const State& st, const std::vector<doubl
       w.record(r, 3);
     });
   }
-  w.text("SCALARS porosity float\n");
-  w.text("LOOKUP_TABLE default\n");
-  each([&](int i, int j, int k) { w.record(&poro[at(i, j, k)], 1); });
+  auto porosity_section = [&]() {
+    w.text("SCALARS porosity float\n");
+    w.text("LOOKUP_TABLE default\n");
+    each([&](int i, int j, int k) { w.record(&poro[at(i, j, k)], 1); });
+  };
+  const bool porosity_last = final && dim == 3;
+  if (!porosity_last) porosity_section();
   w.text("SCALARS pressure float\n");
   w.text("LOOKUP_TABLE default\n");
   each([&](int i, int j, int k) { w.record(&st.p[at(i, j, k)], 1); });
@@ -710,6 +720,7 @@ void write_vtk(const std::string& path, const State& st, const std::vector<doubl
     if (dim == 3) d = d + (st.w[at(i, j, k + 1)] - st.w[at(i, j, k - 1)]) / (zs[k + 1] - zs[k - 1]);
     w.record(&d, 1);
   });
+  if (porosity_last) porosity_section();
   if (dim == 2) {
     w.text("SCALARS abs_dimless_v float\n");
     w.text("LOOKUP_TABLE default\n");
@@ -833,7 +844,7 @@ struct Args {
   std::string project = ".";
   long long steps = -1;
   int device = 0;
-  bool print_config = false, force_log = false, no_vtk = false;
+  bool print_config = false, force_log = false, no_vtk = false, final = false;
   std::string dump_porosity, save_state, vtk_from, restart;
   long long istep = -1;
 };
@@ -843,7 +854,7 @@ void usage() {
                "usage: pf_run [--project DIR] [--steps N] [--device D] [--force-log] [--save-state FILE] "
                "[--restart STATE] [--no-vtk]\n"
                "       pf_run [--project DIR] --print-config [--dump-porosity FILE]\n"
-               "       pf_run [--project DIR] --vtk-from STATE [--istep K]\n");
+               "       pf_run [--project DIR] --vtk-from STATE [--istep K | --final]\n");
 }
 
 Args parse_args(int argc, char** argv) {
@@ -874,6 +885,8 @@ Args parse_args(int argc, char** argv) {
       a.restart = next();
     else if (s == "--vtk-from")
       a.vtk_from = next();
+    else if (s == "--final")
+      a.final = true;
     else if (s == "--istep")
       a.istep = std::stoll(next());
     else if (s == "-h" || s == "--help") {
@@ -921,7 +934,8 @@ int run(const Args& a) {
     if (st.dim != g.dim || st.m != g.m || st.n != g.n || (g.dim == 3 && st.l != g.l))
       die("--vtk-from: the state's grid does not match the project's porosity file");
     mkdir_p(folder);
-    write_vtk(vtk_path(folder, a.istep >= 0 ? a.istep : st.istep), st, clamped_porosity(g, s.threshold), s);
+    const std::string out = a.final ? folder + "/output_paraview.vtk" : vtk_path(folder, a.istep >= 0 ? a.istep : st.istep);
+    write_vtk(out, st, clamped_porosity(g, s.threshold), s, a.final);
     return 0;
   }
   if (s.istep_max <= 0 || s.istep_out <= 0) die("istep_max and istep_out must be > 0");
@@ -1006,11 +1020,14 @@ int run(const Args& a) {
     const int rc = pf_norms(c, &max_div, &sor_err);
     std::printf("# steps %lld  max|div u| %.17g  SOR error %.17g\n", done, max_div, sor_err);
     check(rc, "pf_norms");
-    if (!a.save_state.empty()) {
+    if (vtk || !a.save_state.empty()) {
       check(pf_get_state(c, buf.u.data(), buf.v.data(), g.dim == 3 ? buf.w.data() : nullptr, buf.p.data(), ld1, ld2),
             "pf_get_state");
       buf.istep = done;
-      write_state(a.save_state, buf);
+      // the main programs end with output_paraview_2d/_3d: the same file for
+      // the final state, named output_paraview.vtk (output.f90:323, :816)
+      if (vtk) write_vtk(folder + "/output_paraview.vtk", buf, poro, s, true);
+      if (!a.save_state.empty()) write_state(a.save_state, buf);
     }
   } catch (...) {
     pf_destroy(c);

@@ -55,7 +55,12 @@ def _rows(cols: List[np.ndarray]) -> str:
     return "\n".join(line.tolist()) + "\n"
 
 
-def write_vtk(path: str, state: Dict[str, np.ndarray], porosity: np.ndarray, settings: Settings) -> None:
+def write_vtk(path: str, state: Dict[str, np.ndarray], porosity: np.ndarray, settings: Settings,
+              final: bool = False) -> None:
+    """final=True: the file the main programs write at the end of the run,
+    output_paraview_2d/_3d (output.f90:307-419, :793-910).  In 2D it is the
+    same text; in 3D its porosity section comes after VelocityDivergent
+    instead of before pressure."""
     s = settings
     u, v, p = state["u"], state["v"], state["p"]
     dim = u.ndim
@@ -93,9 +98,11 @@ def write_vtk(path: str, state: Dict[str, np.ndarray], porosity: np.ndarray, set
         if dim == 2:
             f.write("VECTORS dimless_v float\n")
             f.write(_rows([u[I] * po / s.inlet_velocity, v[I] * po / s.inlet_velocity, zero]))
-        f.write("SCALARS porosity float\n")
-        f.write("LOOKUP_TABLE default\n")
-        f.write(_rows([po]))
+        porosity_last = final and dim == 3
+        if not porosity_last:
+            f.write("SCALARS porosity float\n")
+            f.write("LOOKUP_TABLE default\n")
+            f.write(_rows([po]))
         f.write("SCALARS pressure float\n")
         f.write("LOOKUP_TABLE default\n")
         f.write(_rows([p[I]]))
@@ -112,6 +119,10 @@ def write_vtk(path: str, state: Dict[str, np.ndarray], porosity: np.ndarray, set
         f.write("SCALARS VelocityDivergent float\n")
         f.write("LOOKUP_TABLE default\n")
         f.write(_rows([div]))
+        if porosity_last:
+            f.write("SCALARS porosity float\n")
+            f.write("LOOKUP_TABLE default\n")
+            f.write(_rows([po]))
         if dim == 2:
             f.write("SCALARS abs_dimless_v float\n")
             f.write("LOOKUP_TABLE default\n")

@@ -52,6 +52,7 @@ def test_pf_run_matches_python_host(tmp_path, name):
         write_vtk(vtk_path(py_dir, 0), c.get_state(), c.porosity(), c.settings)  # the step-0 file
         run_with_output(c, s.istep_max, s.istep_out, py_dir)
         want = c.get_state()
+        porosity = c.porosity()
         max_div, sor_err = c.norms()
     got, istep = read_state_file(final)
     assert istep == s.istep_max
@@ -61,11 +62,15 @@ def test_pf_run_matches_python_host(tmp_path, name):
 
     written = sorted(f for f in os.listdir(os.path.join(root, s.output_folder)) if f.endswith(".vtk"))
     steps = [0] + list(range(s.istep_out, s.istep_max + 1, s.istep_out))
-    assert written == [os.path.basename(vtk_path("", k)) for k in steps]
+    assert written == sorted([os.path.basename(vtk_path("", k)) for k in steps] + ["output_paraview.vtk"])
     for k in steps:
         a = open(vtk_path(os.path.join(root, s.output_folder), k), "rb").read()
         b = open(vtk_path(py_dir, k), "rb").read()
         assert a == b, k
+    # the final file: the same writer on the final state
+    write_vtk(os.path.join(py_dir, "final.vtk"), want, porosity, s, final=True)
+    assert open(os.path.join(root, s.output_folder, "output_paraview.vtk"), "rb").read() == \
+        open(os.path.join(py_dir, "final.vtk"), "rb").read()
 
 
 def test_pf_run_force_log_matches_pf_forces(tmp_path):
@@ -108,7 +113,7 @@ def test_pf_run_restart_continues_bit_for_bit(tmp_path, name):
     # the restarted run writes the files of the steps after its first one
     after = [k for k in range(s.istep_out, s.istep_max + 1, s.istep_out) if k > 3]
     assert sorted(os.listdir(os.path.join(split, s.output_folder))) == \
-        [os.path.basename(vtk_path("", k)) for k in after]
+        sorted([os.path.basename(vtk_path("", k)) for k in after] + ["output_paraview.vtk"])
     for k in after:
         assert open(vtk_path(os.path.join(whole, s.output_folder), k), "rb").read() == \
             open(vtk_path(os.path.join(split, s.output_folder), k), "rb").read(), k

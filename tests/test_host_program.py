@@ -190,10 +190,12 @@ def _padded_porosity(vals, threshold):
     return out
 
 
+@pytest.mark.parametrize("final", [False, True])
 @pytest.mark.parametrize("shape", [(11, 7), (6, 5, 4)])
-def test_vtk_from_state_matches_python_writer(pf_run, tmp_path, shape):
+def test_vtk_from_state_matches_python_writer(pf_run, tmp_path, shape, final):
     """--vtk-from writes the same bytes as write_vtk for the same state: the
-    coordinates, the seven arrays and their f16.4 text, i fastest."""
+    coordinates, the seven arrays and their f16.4 text, i fastest; with
+    --final the end-of-run file output_paraview.vtk."""
     dim = len(shape)
     s = (G.settings_cylinder_2d(center_x=0.3, inlet_velocity=1.3) if dim == 2
          else G.settings_spheres_3d(center_x=0.5, center_y=0.25, center_z=0.75))
@@ -205,13 +207,15 @@ def test_vtk_from_state_matches_python_writer(pf_run, tmp_path, shape):
     state["u"].flat[5] = -0.0
     state["p"].flat[7] = -1e-7  # prints as -0.0000
     write_state_file(str(tmp_path / "state.bin"), state, shape, istep=42)
-    r = _run(pf_run, "--project", root, "--vtk-from", str(tmp_path / "state.bin"))  # the file's own step
+    r = _run(pf_run, "--project", root, "--vtk-from", str(tmp_path / "state.bin"),  # the file's own step
+             *(["--final"] if final else []))
     assert r.returncode == 0, r.stderr
-    got = open(os.path.join(root, s.output_folder, "output_00042.vtk"), "rb").read()
+    name = "output_paraview.vtk" if final else "output_00042.vtk"
+    got = open(os.path.join(root, s.output_folder, name), "rb").read()
     s_py = read_settings(os.path.join(root, "config", "controlDict.txt"))
     _, raw = read_porosity_csv(os.path.join(root, s.csv_file))
     want_path = str(tmp_path / "want.vtk")
-    write_vtk(want_path, state, _padded_porosity(raw, s_py.threshold), s_py)
+    write_vtk(want_path, state, _padded_porosity(raw, s_py.threshold), s_py, final=final)
     want = open(want_path, "rb").read()
     assert got == want
 

@@ -14,8 +14,10 @@ def _f(x):
     return "%16.4f" % x
 
 
-def _reference_text(st, po, s, dim):
-    """Loop-by-loop statement of the Fortran writer (records of 3(f16.4,1x))."""
+def _reference_text(st, po, s, dim, final=False):
+    """Loop-by-loop statement of the Fortran writer (records of 3(f16.4,1x)).
+    final: output_paraview_2d/_3d (output.f90:307-419, :793-910), the file of
+    the end of the run, whose 3D form writes porosity last."""
     u, v, p = st["u"], st["v"], st["p"]
     if dim == 2:
         n, m = u.shape[0] - 2, u.shape[1] - 2
@@ -46,7 +48,9 @@ def _reference_text(st, po, s, dim):
         for c in cells:
             e = U(po, *c)
             out.append(rec((U(u, *c) * e / s.inlet_velocity, U(v, *c) * e / s.inlet_velocity, 0.0)))
-    out += ["SCALARS porosity float", "LOOKUP_TABLE default"] + [rec((U(po, *c),)) for c in cells]
+    porosity = ["SCALARS porosity float", "LOOKUP_TABLE default"] + [rec((U(po, *c),)) for c in cells]
+    if not (final and dim == 3):
+        out += porosity
     out += ["SCALARS pressure float", "LOOKUP_TABLE default"] + [rec((U(p, *c),)) for c in cells]
     out += ["SCALARS VelocityDivergent float", "LOOKUP_TABLE default"]
     x, y = xs[0], xs[1]
@@ -59,6 +63,8 @@ def _reference_text(st, po, s, dim):
                  + (v[k, j + 1, i] - v[k, j - 1, i]) / (y[j + 1] - y[j - 1])
                  + (w[k + 1, j, i] - w[k - 1, j, i]) / (z[k + 1] - z[k - 1]))
         out.append(rec((d,)))
+    if final and dim == 3:
+        out += porosity
     if dim == 2:
         out += ["SCALARS abs_dimless_v float", "LOOKUP_TABLE default"]
         for c in cells:
@@ -68,8 +74,9 @@ def _reference_text(st, po, s, dim):
     return "\n".join(out) + "\n"
 
 
+@pytest.mark.parametrize("final", [False, True])
 @pytest.mark.parametrize("dim", [2, 3])
-def test_vtk_writer_matches_reference_layout(dim, tmp_path):
+def test_vtk_writer_matches_reference_layout(dim, final, tmp_path):
     rng = np.random.default_rng(3)
     shape = (5, 4) if dim == 2 else (4, 3, 3)
     fshape = tuple(x + 2 for x in reversed(shape))
@@ -77,5 +84,5 @@ def test_vtk_writer_matches_reference_layout(dim, tmp_path):
     po = rng.uniform(0, 1, size=fshape)
     s = Settings(width=2.0, height=1.0, depth=1.5, inlet_velocity=0.7, center_x=0.25, center_y=0.5, center_z=0.4)
     path = tmp_path / "output_00010.vtk"
-    write_vtk(str(path), st, po, s)
-    assert path.read_text() == _reference_text(st, po, s, dim)
+    write_vtk(str(path), st, po, s, final=final)
+    assert path.read_text() == _reference_text(st, po, s, dim, final=final)
