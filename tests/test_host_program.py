@@ -237,3 +237,26 @@ def test_state_file_of_another_grid_is_rejected(pf_run, tmp_path):
         f.write(b"\0")
     r = _run(pf_run, "--project", root, "--restart", str(tmp_path / "s.bin"))
     assert r.returncode == 1 and "size does not match" in r.stderr, r.stderr
+
+
+# The reference's own example project (test/cylinder-2d.zip of PixelFlow):
+# PF_REFERENCE_CYLINDER_ZIP names its path; the test is skipped without it.
+REF_ZIP = os.environ.get("PF_REFERENCE_CYLINDER_ZIP", "")
+
+
+@pytest.mark.skipif(not REF_ZIP or not os.path.exists(REF_ZIP),
+                    reason="PF_REFERENCE_CYLINDER_ZIP not set to the reference's test/cylinder-2d.zip")
+def test_reference_cylinder_project_reads_as_in_python(pf_run, tmp_path):
+    """The reference's example project, its controlDict and 1024 x 512
+    porosity file as shipped: the same settings and values bit for bit."""
+    import zipfile
+    with zipfile.ZipFile(REF_ZIP) as z:
+        z.extractall(tmp_path)
+    proj = str(tmp_path / "cylinder-2d")
+    raw = str(tmp_path / "poro.bin")
+    r = _run(pf_run, "--project", proj, "--print-config", "--dump-porosity", raw)
+    assert r.returncode == 0, r.stderr
+    py = read_settings(os.path.join(proj, "config", "controlDict.txt"))
+    shape, vals = read_porosity_csv(os.path.join(proj, py.csv_file))
+    _same_settings(json.loads(r.stdout), py, shape)
+    assert np.fromfile(raw, dtype=np.float64).tobytes() == vals.ravel().tobytes()
