@@ -12,9 +12,13 @@ arguments (arrays passed as objects; scalars copied in and out), `real`,
 `integer`, `logical`, `character` declarations with `dimension` bounds,
 `do` loops with steps, block and one-line `if`, `call`, assignment,
 `return`, `exit`, `cycle`, list-directed `read` from files opened with
-`open`, and the intrinsics the programs use.  `!$omp` directives are
-comments (the parallel loops are order-independent, as the reference
-requires); `write`, `print` and `close` are ignored.  Expressions are
+`open`, namelist `read`s (the caller supplies the group's values in
+`Program.nml_values`), and the intrinsics the programs use.  `!$omp`
+directives are comments (the parallel loops are order-independent, as the
+reference requires).  `write` records its values, unformatted, one list per
+record in `Program.writes[unit]` (an internal write into a character
+variable under "internal", the variable left unchanged); `print` and
+`close` are ignored.  Expressions are
 evaluated left to right as written, one IEEE operation per Fortran operator
 (no fused multiply-add), `x**2` as `x*x`, integer `/` truncating toward zero,
 `mod` with the sign of its first argument.
@@ -570,8 +574,13 @@ class Program:
         uses = [ln.split()[1].rstrip(",") for ln in u.body if ln.startswith("use ") and "omp_lib" not in ln]
         u.uses = uses + [x for x in u.uses if x not in uses]
         body = []
+        ctx.namelists = {}
         for ln in u.body:
-            if ln.startswith(("use ", "implicit", "namelist")):
+            m = re.match(r"namelist\s*/\s*(\w+)\s*/\s*(.*)$", ln)
+            if m:  # namelist /group/ a, b: the members a namelist read sets
+                ctx.namelists.setdefault(m.group(1), []).extend(x.strip() for x in m.group(2).split(","))
+                continue
+            if ln.startswith(("use ", "implicit")):
                 continue
             if self._decl(ctx, ln):
                 continue
@@ -694,6 +703,14 @@ class Program:
             unit = ctx.expr(parts[0])[0]
             fname = [p for p in parts if p.replace(" ", "").startswith("file=")][0].split("=", 1)[1]
             return [(f"P._open({unit}, {ctx.expr(fname)[0]})", 0)]
+        m = re.match(r"read\s*\(\s*(\w+)\s*,\s*nml\s*=\s*(\w+)\s*\)$", ln)
+        if m:  # a namelist read: the members the caller supplied (P.nml_values)
+            group = m.group(2)
+            out = [(f"_nl = P.nml({group!r})", 0)]
+            for member in ctx.namelists.get(group, []):
+                vs, _ = ctx.var(member)
+                out.append((f"{vs} = _nl.get({member!r}, {vs})", 0))
+            return out
         m = re.match(r"read\s*\((\w+)\s*,\s*\*\s*\)\s*(.*)$", ln)
         if m:
             unit = m.group(1)
@@ -813,7 +830,16 @@ class Program:
         else:  # a file the program writes
             self.writes.setdefault(int(unit), [])
 
+    def nml(self, group):
+        """Values of namelist group `group` for a `read(u, nml=group)`."""
+        return getattr(self, "nml_values", {}).get(group, {})
+
     def record(self, unit, values):
+        if isinstance(unit, str) and unit != "*":
+            # an internal write into a character variable (a file name's
+            # step number): recorded, the variable itself is left unchanged
+            self.writes.setdefault("internal", []).append(list(values))
+            return
         self.writes.setdefault(unit if unit == "*" else int(unit), []).append(list(values))
 
     def _read(self, unit, kinds):

@@ -9,16 +9,21 @@ the reference writer's bytes), the settings, the fields u, v, [w,] p the
 program holds after `steps` time steps (ghost layers included,
 [(k,) j, i] order), the porosity-weighted divergence field `div`
 ([(k,) j, i], interior only) that output_divergent_2d/3d writes at the end
-of the run, and, for the drag program, the pressure and friction force sums
+of the run, for the drag program the pressure and friction force sums
 `fp`, `fv` (one row per step) that output_force_log_2d prints after every
-step.  The runs replace only what is not arithmetic: the namelist reader
-(`read_settings` returns the settings below), the file and image writers,
+step, and the records of the two VTK writers on the final state: the
+istep_out file of the last step (output_paraview_temp_2d/_3d) and the
+end-of-run file (output_paraview_2d/_3d), as `vtk_temp_vals`/`_lens` and
+`vtk_final_vals`/`_lens` (every value written, in order, and the number of
+values of each record; a record of literal text only has none).  The runs replace only what is not arithmetic: the namelist reader
+(`read_settings` returns the settings below), the other file writers,
 `get_now_time` and `system`; the static array sizes md, nd, ld are shrunk to
 the grid (they size storage only).  The main program, the grid set-up (which
 reads the CSV with list-directed input), the initial and boundary
 conditions, solve_p, the matrix edits, the SOR, the divergence output and
-the force log run unchanged; their `write` statements are recorded as values
-rather than formatted.  The slip cases run the uniform 2D program with the
+the force log and the VTK writers run unchanged (istep_out = the run's
+steps); their `write` statements are recorded as values rather than
+formatted.  The slip cases run the uniform 2D program with the
 symmetry rows its source keeps commented out enabled (enable_slip), the
 option this repository exposes as `slip_y`.
 
@@ -76,7 +81,9 @@ SLIP_HEADS = ("! symmetry or wall (dp/dy=0. at j=1)", "! symmetry or wall  (dp/d
               "! option: symmetry  (du/dy=0., v=0., dp/dy=0. at j=n)")
 
 # output routines that run as written (their records are captured)
-INTERPRETED = ("output_divergent_2d", "output_divergent_3d", "output_force_log_2d", "output_force_log_3d")
+INTERPRETED = ("output_divergent_2d", "output_divergent_3d", "output_force_log_2d", "output_force_log_3d",
+               "output_paraview_temp_2d", "output_paraview_temp_3d", "output_paraview_2d", "output_paraview_3d")
+VTK_TEMP_UNIT, VTK_FINAL_UNIT = 65, 50  # output.f90:441, :994 and :323, :816
 
 NAMES = ["xnue", "xlambda", "density", "width", "height", "depth", "time", "inlet_velocity", "outlet_pressure",
          "aoa", "istep_max", "istep_out", "thickness", "threshold", "radius", "center_x", "center_y", "center_z",
@@ -147,7 +154,7 @@ def run_reference(ref_dir, name):
         _, vals_read = C.read_porosity_csv(csv)
     settings = dict(xnue=s.xnue, xlambda=s.xlambda, density=s.density, width=s.width, height=s.height,
                     depth=s.depth, time=s.time, inlet_velocity=s.inlet_velocity, outlet_pressure=s.outlet_pressure,
-                    aoa=s.aoa, istep_max=int(s.istep_max), istep_out=10 ** 6, thickness=s.thickness,
+                    aoa=s.aoa, istep_max=int(s.istep_max), istep_out=int(s.istep_max), thickness=s.thickness,
                     threshold=s.threshold, radius=s.radius, center_x=0.0, center_y=0.0, center_z=0.0,
                     nonslip=bool(s.nonslip), output_folder="out", csv_file="porosity.csv",
                     iter_max=int(s.iter_max), relux_factor=s.relux_factor)
@@ -169,12 +176,23 @@ def run_reference(ref_dir, name):
     stubs["read_settings"] = read_settings
     P = Program(texts, overrides=overrides, stubs=stubs)
     P.vfs["porosity.csv"] = csv_text
+    # the 3D VTK writers read &directory_control themselves (output.f90:811-814)
+    P.nml_values = {"directory_control": {"csv_file": settings["csv_file"],
+                                          "output_folder": settings["output_folder"]}}
     S = P.run_main()
     out = {}
     for f in ("u", "v", "w", "p") if len(shape) == 3 else ("u", "v", "p"):
         a = S[f]
         out[f] = np.array(a.data, dtype=np.float64).reshape(a.ext[::-1])
     out["div"] = _divergence_records(P.writes[63 if len(shape) == 2 else 62], shape)
+    final = P.writes.get(VTK_FINAL_UNIT, [])
+    temp = P.writes.get(VTK_TEMP_UNIT, [])
+    if final:  # the VTK records: the end-of-run file and the istep_out file of the last step
+        assert len(temp) == 2 * len(final)  # step 0 and step `steps`
+        for key, recs in (("vtk_final", final), ("vtk_temp", temp[len(final):])):
+            assert all(isinstance(x, (int, float)) for r in recs for x in r)
+            out[key + "_vals"] = np.array([x for r in recs for x in r], dtype=np.float64)
+            out[key + "_lens"] = np.array([len(r) for r in recs], dtype=np.int64)
     fp = [r[1:] for r in P.writes["*"] if r and r[0] == "Fp ="]
     fv = [r[1:] for r in P.writes["*"] if r and r[0] == "Fv ="]
     if fp:
@@ -205,7 +223,7 @@ def main():
         raise SystemExit("set PF_REFERENCE_DIR to a checkout of the reference")
     for name in CASES:
         s, shape, vals_read, steps, out = run_reference(ref, name)
-        np.savez(os.path.join(HERE, f"refpin_{name}.npz"), porosity=vals_read, steps=steps, **out)
+        np.savez_compressed(os.path.join(HERE, f"refpin_{name}.npz"), porosity=vals_read, steps=steps, **out)
         print(name, {k: float(np.abs(v).max()) for k, v in out.items()})
 
 

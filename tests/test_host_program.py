@@ -260,3 +260,28 @@ def test_reference_cylinder_project_reads_as_in_python(pf_run, tmp_path):
     shape, vals = read_porosity_csv(os.path.join(proj, py.csv_file))
     _same_settings(json.loads(r.stdout), py, shape)
     assert np.fromfile(raw, dtype=np.float64).tobytes() == vals.ravel().tobytes()
+
+
+def _refpin_cases():
+    from tests.golden.make_reference_pin import CASES
+    return sorted(CASES)
+
+
+@pytest.mark.parametrize("name", _refpin_cases())
+def test_vtk_from_reproduces_the_reference_records(pf_run, tmp_path, name):
+    """The host program's VTK writer against the records the reference's own
+    writers produced for the final state of each pinned program run
+    (tests/golden/refpin_*.npz): the istep_out file and, with --final, the
+    end-of-run file."""
+    from tests.test_reference_pin import check_vtk_records, load, pinned_vtk_inputs
+    ref = load(name)
+    state, _, s = pinned_vtk_inputs(name)
+    shape = tuple(reversed(ref["porosity"].shape))
+    root = _project(str(tmp_path), s, porosity=ref["porosity"])
+    write_state_file(str(tmp_path / "state.bin"), state, shape, istep=int(ref["steps"]))
+    for final, key in ((False, "vtk_temp"), (True, "vtk_final")):
+        r = _run(pf_run, "--project", root, "--vtk-from", str(tmp_path / "state.bin"), *(["--final"] if final else []))
+        assert r.returncode == 0, r.stderr
+        out = os.path.join(root, s.output_folder,
+                           "output_paraview.vtk" if final else "output_%05d.vtk" % int(ref["steps"]))
+        check_vtk_records(open(out).read(), ref[key + "_vals"], ref[key + "_lens"])
