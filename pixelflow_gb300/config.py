@@ -119,12 +119,28 @@ def _convert(value: str):
         raise ValueError(f"namelist: cannot parse value {value!r}") from exc
 
 
+def _outside_quotes(line: str, ch: str) -> int:
+    """Index of the first `ch` outside a quoted string, or -1."""
+    q = None
+    for k, c in enumerate(line):
+        if q:
+            if c == q:
+                q = None
+        elif c in "\"'":
+            q = c
+        elif c == ch:
+            return k
+    return -1
+
+
 def parse_namelists(text: str) -> Dict[str, Dict[str, object]]:
-    """Parse Fortran namelist groups (``&name ... /``) ignoring ``!`` comments."""
+    """Parse Fortran namelist groups (``&name ... /``): ``!`` starts a
+    comment and ``/`` ends the group, both outside quoted strings."""
     groups: Dict[str, Dict[str, object]] = {}
     current: Optional[str] = None
     for raw in text.splitlines():
-        line = raw.split("!", 1)[0]
+        bang = _outside_quotes(raw, "!")
+        line = raw if bang < 0 else raw[:bang]
         if not line.strip():
             continue
         stripped = line.strip()
@@ -137,8 +153,9 @@ def parse_namelists(text: str) -> Dict[str, Dict[str, object]]:
             else:
                 continue
         end = False
-        if "/" in line and not re.search(r"[\"'][^\"']*/[^\"']*[\"']", line):
-            line, end = line.split("/", 1)[0], True
+        slash = _outside_quotes(line, "/")
+        if slash >= 0:
+            line, end = line[:slash], True
         for m in _TOKEN.finditer(line):
             groups[current][m.group(1).lower()] = _convert(m.group(2))
         if end:

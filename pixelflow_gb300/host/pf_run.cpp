@@ -162,9 +162,25 @@ using Groups = std::map<std::string, std::map<std::string, Value>>;
 bool ident_start(char ch) { return std::isalpha(static_cast<unsigned char>(ch)) || ch == '_'; }
 bool ident_char(char ch) { return std::isalnum(static_cast<unsigned char>(ch)) || ch == '_'; }
 
-// Fortran namelist groups (&name ... /), `!` comments ignored.  Members are
-// `name = value` pairs separated by blanks or commas; a `/` outside quotes
-// ends the group.
+// Position of the first `ch` outside a quoted string (npos if none).
+size_t outside_quotes(const std::string& line, char ch) {
+  char q = 0;
+  for (size_t k = 0; k < line.size(); k++) {
+    const char c = line[k];
+    if (q) {
+      if (c == q) q = 0;
+    } else if (c == '"' || c == '\'') {
+      q = c;
+    } else if (c == ch) {
+      return k;
+    }
+  }
+  return std::string::npos;
+}
+
+// Fortran namelist groups (&name ... /): `!` starts a comment and `/` ends
+// the group, both outside quoted strings.  Members are `name = value` pairs
+// separated by blanks or commas.
 Groups parse_namelists(const std::string& text) {
   Groups groups;
   std::string current;
@@ -175,7 +191,7 @@ Groups parse_namelists(const std::string& text) {
     if (nl == std::string::npos) nl = text.size();
     std::string line = text.substr(pos, nl - pos);
     pos = nl + 1;
-    const size_t bang = line.find('!');
+    const size_t bang = outside_quotes(line, '!');
     if (bang != std::string::npos) line.resize(bang);
     if (trim(line).empty()) continue;
     if (!in_group) {

@@ -109,6 +109,17 @@ istep_max = 12
 """
 
 
+def test_quotes_hold_comment_and_slash_characters(pf_run, tmp_path):
+    """`!` and `/` inside a quoted value are characters of the value; a `/`
+    after it on the same line still ends the group."""
+    text = NAMELIST.replace("""  output_folder = 'results', csv_file = "data/porosity.csv"
+/""", """  output_folder = 'out/run!1', csv_file = "data/porosity.csv" /""")
+    root = _project(str(tmp_path), text=text, porosity=np.full((5, 6), 0.5))
+    py = read_settings(os.path.join(root, "config", "controlDict.txt"))
+    assert py.output_folder == "out/run!1" and py.csv_file == "data/porosity.csv" and py.iter_max == 25
+    _same_settings(_config(pf_run, root), py, (6, 5))
+
+
 def test_print_config_hand_written_namelist(pf_run, tmp_path):
     root = _project(str(tmp_path), text=NAMELIST, porosity=np.full((5, 6), 0.5))
     py = read_settings(os.path.join(root, "config", "controlDict.txt"))
