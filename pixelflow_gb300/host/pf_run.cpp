@@ -404,6 +404,8 @@ Grid read_porosity_csv(const std::string& path) {
       char* end = nullptr;
       const double v = std::strtod(a, &end);
       if (end == a) die(path + ": bad header");
+      // the library's own limit on each extent (pf_create rejects larger)
+      if (!(v >= 1.0 && v <= double(1 << 20))) die(path + ": grid size in the header out of range");
       dims.push_back(static_cast<long long>(v));
       k += static_cast<size_t>(end - a);
     }
@@ -420,8 +422,8 @@ Grid read_porosity_csv(const std::string& path) {
   }
   g.m = static_cast<int>(dims[0]);
   g.n = static_cast<int>(dims[1]);
-  if (g.m < 1 || g.n < 1 || g.l < 1) die(path + ": bad grid size in the header");
   const size_t cells = static_cast<size_t>(g.m) * g.n * g.l;
+  if (cells >= (size_t(1) << 31)) die(path + ": grid too large (the library's arrays hold < 2^31 cells)");
   g.values.assign(cells, 0.0);
   size_t pos = nl + 1;
   const int nidx = g.dim;
@@ -446,6 +448,8 @@ Grid read_porosity_csv(const std::string& path) {
       a = c + 1;
     }
     if ((int)cols.size() < nidx + 1) die(path + ": record with too few columns '" + line + "'");
+    for (int q = 0; q < nidx; q++)
+      if (!(cols[q] >= 1.0 && cols[q] < double(1 << 21))) die(path + ": index out of range in '" + line + "'");
     const long long i = static_cast<long long>(cols[0]), j = static_cast<long long>(cols[1]);
     const long long k = g.dim == 3 ? static_cast<long long>(cols[2]) : 1;
     if (i < 1 || i > g.m || j < 1 || j > g.n || k < 1 || k > g.l) die(path + ": index out of range in '" + line + "'");
@@ -873,6 +877,14 @@ void usage() {
                "       pf_run [--project DIR] --vtk-from STATE [--istep K | --final]\n");
 }
 
+long long int_arg(const std::string& flag, const std::string& text) {
+  if (!is_int_text(text)) die(flag + " needs an integer, got '" + text + "'");
+  errno = 0;
+  const long long v = std::strtoll(text.c_str(), nullptr, 10);
+  if (errno == ERANGE || v < 0 || v > INT_MAX) die(flag + " out of range: " + text);
+  return v;
+}
+
 Args parse_args(int argc, char** argv) {
   Args a;
   for (int k = 1; k < argc; k++) {
@@ -884,9 +896,9 @@ Args parse_args(int argc, char** argv) {
     if (s == "--project" || s == "-C")
       a.project = next();
     else if (s == "--steps")
-      a.steps = std::stoll(next());
+      a.steps = int_arg(s, next());
     else if (s == "--device")
-      a.device = std::stoi(next());
+      a.device = static_cast<int>(int_arg(s, next()));
     else if (s == "--print-config")
       a.print_config = true;
     else if (s == "--dump-porosity")
@@ -904,7 +916,7 @@ Args parse_args(int argc, char** argv) {
     else if (s == "--final")
       a.final = true;
     else if (s == "--istep")
-      a.istep = std::stoll(next());
+      a.istep = int_arg(s, next());
     else if (s == "-h" || s == "--help") {
       usage();
       std::exit(0);

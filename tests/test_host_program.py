@@ -161,12 +161,22 @@ def test_bad_settings_are_errors(pf_run, tmp_path, text, needle):
     assert r.returncode == 1 and needle in r.stderr, r.stderr
 
 
-def test_bad_porosity_file_is_an_error(pf_run, tmp_path):
+@pytest.mark.parametrize("edit,needle", [
+    (lambda t: t + "6, 1, 1, 0.5\n", "index out of range"),  # i beyond m = 5
+    (lambda t: t + "nan, 1, 1, 0.5\n", "index out of range"),
+    (lambda t: t + "1, 1\n", "too few columns"),
+    (lambda t: t + "1, 1, 1, x\n", "bad record"),
+    (lambda t: "5,4000000,1\n" + t.split("\n", 1)[1], "out of range"),
+    (lambda t: "1048576,1048576,1048576\n" + t.split("\n", 1)[1], "grid too large"),
+], ids=["index", "nan-index", "columns", "value", "extent", "cells"])
+def test_bad_porosity_file_is_an_error(pf_run, tmp_path, edit, needle):
     root = _project(str(tmp_path), G.settings_cylinder_2d(), porosity=np.full((4, 5), 0.5))
-    with open(os.path.join(root, "data", "porosity.csv"), "a") as f:
-        f.write("6, 1, 1, 0.5\n")  # i beyond m = 5
+    csv = os.path.join(root, "data", "porosity.csv")
+    text = open(csv).read()
+    with open(csv, "w") as f:
+        f.write(edit(text))
     r = _run(pf_run, "--project", root, "--print-config")
-    assert r.returncode == 1 and "index out of range" in r.stderr, r.stderr
+    assert r.returncode == 1 and needle in r.stderr, r.stderr
 
 
 def write_state_file(path, state, shape, istep=0):
@@ -296,3 +306,16 @@ def test_vtk_from_reproduces_the_reference_records(pf_run, tmp_path, name):
         out = os.path.join(root, s.output_folder,
                            "output_paraview.vtk" if final else "output_%05d.vtk" % int(ref["steps"]))
         check_vtk_records(open(out).read(), ref[key + "_vals"], ref[key + "_lens"])
+
+
+@pytest.mark.parametrize("args,needle", [
+    (["--steps", "ten"], "--steps needs an integer"),
+    (["--steps", "-3"], "--steps out of range"),
+    (["--device", "99999999999"], "--device out of range"),
+    (["--frobnicate"], "unknown argument"),
+    (["--steps"], "missing value after --steps"),
+])
+def test_bad_arguments_are_errors(pf_run, tmp_path, args, needle):
+    root = _project(str(tmp_path), G.settings_cylinder_2d(), porosity=np.full((4, 5), 0.5))
+    r = _run(pf_run, "--project", root, *args)
+    assert r.returncode == 1 and needle in r.stderr, r.stderr
