@@ -29,7 +29,7 @@ option this repository exposes as `slip_y`.
 
 Run from the repository root (the reference is not needed afterwards):
 
-    PF_REFERENCE_DIR=<reference checkout> python -m tests.golden.make_reference_pin
+    PF_REFERENCE_DIR=<reference checkout> python -m tests.golden.make_reference_pin [case ...]
 """
 import os
 import re
@@ -70,7 +70,15 @@ CASES = {
     # the uniform 2D program with its commented symmetry ("slip") rows enabled
     "slip2d_12x8": ("ibm_2d_uniform_omp_cpu.f90", (12, 8), "cyl_slip", 3),
     "slip2d_13x9": ("ibm_2d_uniform_omp_cpu.f90", (13, 9), "cyl_slip", 3),
+    # the physical parameters away from the template's defaults: an inflow
+    # angle (2D: AoA/180*pi in boundary and initial_conditions; 3D: AoA/1300*pi
+    # in boundary, AoA/360*pi in initial_conditions), the second viscosity,
+    # density, outlet pressure, and (2D) no damping term
+    "physics2d_12x8": ("ibm_2d_uniform_omp_cpu.f90", (12, 8), "cyl_phys", 3),
+    "physics3d_8x6x5": ("ibm_3d_uniform_omp_cpu.f90", (8, 6, 5), "sph_phys", 3),
 }
+PHYSICS = {"cyl_phys": dict(aoa=10.0, xlambda=0.3, density=1.3, outlet_pressure=0.25, nonslip=False),
+           "sph_phys": dict(aoa=25.0, xlambda=0.2, density=0.8, outlet_pressure=-0.5)}
 
 # The commented blocks that make up the 2D symmetry option, by the comment
 # line that heads each (ibm_2d_uniform_omp_cpu.f90: boundrary_matrix :440-450,
@@ -93,9 +101,9 @@ NAMES = ["xnue", "xlambda", "density", "width", "height", "depth", "time", "inle
 def case_inputs(name):
     """(settings, shape, porosity values before the CSV round trip, steps)."""
     prog, shape, kind, steps = CASES[name]
-    if kind in ("cyl", "step", "cyl_slip"):
+    if kind in ("cyl", "step", "cyl_slip", "cyl_phys"):
         m, n = shape
-        s = G.settings_cylinder_2d(iter_max=7, slip_y=kind == "cyl_slip")
+        s = G.settings_cylinder_2d(iter_max=7, slip_y=kind == "cyl_slip", **PHYSICS.get(kind, {}))
         vals = G.cylinder_2d(m, n, radius=0.2, cx=0.6, cy=0.45)
         if kind == "step":  # an obstacle across the inlet: a non-uniform inflow profile
             vals = np.minimum(vals, G.cylinder_2d(m, n, radius=0.3, cx=0.0, cy=0.3))
@@ -110,7 +118,7 @@ def case_inputs(name):
             vals[-1, : n // 2, : m // 2] = 0.05
             vals[:, 0, m // 2:] = 0.05
         else:
-            s = G.settings_spheres_3d(iter_max=5)
+            s = G.settings_spheres_3d(iter_max=5, **PHYSICS.get(kind, {}))
             vals = G.spheres_3d(m, n, l, spheres=np.array([[0.4, 0.5, 0.5, 0.2], [0.7, 0.3, 0.6, 0.15]]))
         dt = 1e-4
     # time / istep_max is dt for the program and the oracle alike
@@ -221,7 +229,7 @@ def main():
     ref = os.environ.get("PF_REFERENCE_DIR")
     if not ref:
         raise SystemExit("set PF_REFERENCE_DIR to a checkout of the reference")
-    for name in CASES:
+    for name in sys.argv[1:] or CASES:  # given names: only those cases
         s, shape, vals_read, steps, out = run_reference(ref, name)
         np.savez_compressed(os.path.join(HERE, f"refpin_{name}.npz"), porosity=vals_read, steps=steps, **out)
         print(name, {k: float(np.abs(v).max()) for k, v in out.items()})

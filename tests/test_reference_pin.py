@@ -7,8 +7,11 @@ the uniform 2D program on even and odd grids (the linear-index colour map's
 odd-m shift included), the backstep program, the uniform 3D program on even
 and odd grids, the air-condition program with its own wall table and two
 others (set through its wall parameters), the drag
-program and the uniform 2D program with its commented symmetry ("slip")
-rows enabled, with the divergence field each program writes at the end
+program, the uniform 2D program with its commented symmetry ("slip")
+rows enabled, and the uniform 2D and 3D programs with the physical
+parameters away from the template's defaults (inflow angle, second
+viscosity, density, outlet pressure, no damping), with the divergence field
+each program writes at the end
 (output_divergent_2d/3d) and the drag program's force log after every step
 (output_force_log_2d).  The C oracle (oracle/pf_oracle.c), given the same
 settings and the porosity the program read, must reproduce every field, the
