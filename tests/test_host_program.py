@@ -319,3 +319,25 @@ def test_bad_arguments_are_errors(pf_run, tmp_path, args, needle):
     root = _project(str(tmp_path), G.settings_cylinder_2d(), porosity=np.full((4, 5), 0.5))
     r = _run(pf_run, "--project", root, *args)
     assert r.returncode == 1 and needle in r.stderr, r.stderr
+
+
+# The reference's project template (template/config/controlDict.txt of
+# PixelFlow): PF_REFERENCE_DIR names a checkout; skipped without it.
+REF_DIR = os.environ.get("PF_REFERENCE_DIR", "")
+
+
+@pytest.mark.skipif(not REF_DIR or not os.path.isfile(os.path.join(REF_DIR, "template", "config", "controlDict.txt")),
+                    reason="PF_REFERENCE_DIR not set to a checkout of the reference")
+def test_template_controldict_gives_the_defaults(pf_run, tmp_path):
+    """The template's namelists read as the Settings defaults, in both
+    readers (the defaults the readers fall back on are the template's)."""
+    import shutil
+    os.makedirs(tmp_path / "config")
+    shutil.copy(os.path.join(REF_DIR, "template", "config", "controlDict.txt"), tmp_path / "config")
+    root = _project(str(tmp_path), porosity=None, text=open(tmp_path / "config" / "controlDict.txt").read())
+    csv = os.path.join(root, "data", "porosity.csv")
+    os.makedirs(os.path.dirname(csv))
+    write_porosity_csv(csv, np.full((4, 5), 0.5))
+    py = read_settings(os.path.join(root, "config", "controlDict.txt"))
+    assert py == Settings()
+    _same_settings(_config(pf_run, root), Settings(), (5, 4))
