@@ -71,10 +71,11 @@ def build_host(force: bool = False, verbose: bool = False) -> str:
               "-lpixelflow_gb300"]
     cxx = shutil.which(os.environ.get("CXX", "g++"))
     if cxx:
-        cmd = [cxx, *common, "-Wall", "-ffp-contract=off", "-Wl,-rpath,$ORIGIN", f"-Wl,-rpath-link,{cuda_lib}"]
+        cmd = [cxx, *common, "-pthread", "-Wall", "-ffp-contract=off", "-Wl,-rpath,$ORIGIN",
+               f"-Wl,-rpath-link,{cuda_lib}"]
     else:  # nvcc hands a .cpp file to its own host compiler
-        cmd = [_nvcc(), *common, "-Xcompiler", "-Wall,-ffp-contract=off", "-Xlinker", "-rpath,$ORIGIN",
-               "-Xlinker", f"-rpath-link,{cuda_lib}"]
+        cmd = [_nvcc(), *common, "-Xcompiler", "-pthread,-Wall,-ffp-contract=off", "-Xlinker", "-rpath,$ORIGIN",
+               "-Xlinker", f"-rpath-link,{cuda_lib}", "-lpthread"]
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.check_call(cmd)
