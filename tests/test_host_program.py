@@ -241,6 +241,27 @@ def test_vtk_from_state_matches_python_writer(pf_run, tmp_path, shape, final):
     assert got == want
 
 
+@pytest.mark.parametrize("threads", ["1", "3", "8"])
+def test_vtk_from_threads_give_the_same_bytes(pf_run, tmp_path, threads):
+    """A grid of several formatting blocks (90,000 points, blocks of 65,536
+    per thread): the text equals the Python writer's for any thread count."""
+    shape = (50, 45, 40)
+    s = G.settings_spheres_3d(center_x=0.1)
+    rng = np.random.default_rng(5)
+    vals = rng.random(shape[::-1])
+    root = _project(str(tmp_path), s, porosity=vals)
+    state = {k: rng.standard_normal(tuple(x + 2 for x in shape[::-1])) for k in ("u", "v", "w", "p")}
+    write_state_file(str(tmp_path / "state.bin"), state, shape, istep=7)
+    r = subprocess.run([pf_run, "--project", root, "--vtk-from", str(tmp_path / "state.bin")],
+                       capture_output=True, text=True, timeout=300, env={**os.environ, "PF_RUN_THREADS": threads})
+    assert r.returncode == 0, r.stderr
+    got = open(os.path.join(root, s.output_folder, "output_00007.vtk"), "rb").read()
+    _, raw = read_porosity_csv(os.path.join(root, s.csv_file))
+    write_vtk(str(tmp_path / "want.vtk"), state, _padded_porosity(raw, s.threshold), read_settings(
+        os.path.join(root, "config", "controlDict.txt")))
+    assert got == open(tmp_path / "want.vtk", "rb").read()
+
+
 def test_state_file_round_trip(tmp_path):
     st = {k: np.random.default_rng(1).random((6, 7, 8)) for k in ("u", "v", "w", "p")}
     write_state_file(str(tmp_path / "s.bin"), st, (6, 5, 4), istep=17)
