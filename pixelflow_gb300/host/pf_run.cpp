@@ -379,6 +379,18 @@ Settings read_settings(const std::string& path) {
   return s;
 }
 
+// Host threads for parsing and formatting text: PF_RUN_THREADS, or the
+// hardware threads; at most 64.
+int host_threads() {
+  static const int n = [] {
+    const char* env = std::getenv("PF_RUN_THREADS");
+    long v = env ? std::strtol(env, nullptr, 10) : 0;
+    if (v <= 0) v = static_cast<long>(std::thread::hardware_concurrency());
+    return static_cast<int>(std::max(1L, std::min(v, 64L)));
+  }();
+  return n;
+}
+
 // ---------------------------------------------------------------------------
 // The porosity CSV (grid.f90:36-47, 281-294): a header "m,n[,l]" and one
 // "i, j, k, value" record per cell, stored at porosity(i, j[, k]) whatever the
@@ -426,35 +438,75 @@ Grid read_porosity_csv(const std::string& path) {
   const size_t cells = static_cast<size_t>(g.m) * g.n * g.l;
   if (cells >= (size_t(1) << 31)) die(path + ": grid too large (the library's arrays hold < 2^31 cells)");
   g.values.assign(cells, 0.0);
-  size_t pos = nl + 1;
+  // The records are parsed on all host threads, each a run of whole lines,
+  // into (cell, value) pairs that are then stored in file order, so a cell
+  // listed twice keeps its last value as in a sequential read, and an error
+  // names the first bad line of the file.
   const int nidx = g.dim;
-  while (pos < text.size()) {
-    size_t e = text.find('\n', pos);
-    if (e == std::string::npos) e = text.size();
-    std::string line = text.substr(pos, e - pos);
-    pos = e + 1;
-    const size_t hash = line.find('#');
-    if (hash != std::string::npos) line.resize(hash);
-    if (trim(line).empty()) continue;
+  auto parse = [&](size_t from, size_t to, std::vector<std::pair<size_t, double>>& out, std::string& err) {
     std::vector<double> cols;
-    size_t a = 0;
-    while (true) {
-      size_t c = line.find(',', a);
-      const std::string tok = trim(line.substr(a, c == std::string::npos ? std::string::npos : c - a));
-      char* end = nullptr;
-      const double v = std::strtod(tok.c_str(), &end);
-      if (tok.empty() || end != tok.c_str() + tok.size()) die(path + ": bad record '" + line + "'");
-      cols.push_back(v);
-      if (c == std::string::npos) break;
-      a = c + 1;
+    size_t pos = from;
+    while (pos < to) {
+      size_t e = text.find('\n', pos);
+      if (e == std::string::npos || e > to) e = to;
+      std::string line = text.substr(pos, e - pos);
+      pos = e + 1;
+      const size_t hash = line.find('#');
+      if (hash != std::string::npos) line.resize(hash);
+      if (trim(line).empty()) continue;
+      cols.clear();
+      size_t a = 0;
+      while (true) {
+        size_t c = line.find(',', a);
+        const std::string tok = trim(line.substr(a, c == std::string::npos ? std::string::npos : c - a));
+        char* end = nullptr;
+        const double v = std::strtod(tok.c_str(), &end);
+        if (tok.empty() || end != tok.c_str() + tok.size()) {
+          err = path + ": bad record '" + line + "'";
+          return;
+        }
+        cols.push_back(v);
+        if (c == std::string::npos) break;
+        a = c + 1;
+      }
+      if ((int)cols.size() < nidx + 1) {
+        err = path + ": record with too few columns '" + line + "'";
+        return;
+      }
+      for (int q = 0; q < nidx; q++)
+        if (!(cols[q] >= 1.0 && cols[q] < double(1 << 21))) {
+          err = path + ": index out of range in '" + line + "'";
+          return;
+        }
+      const long long i = static_cast<long long>(cols[0]), j = static_cast<long long>(cols[1]);
+      const long long k = g.dim == 3 ? static_cast<long long>(cols[2]) : 1;
+      if (i < 1 || i > g.m || j < 1 || j > g.n || k < 1 || k > g.l) {
+        err = path + ": index out of range in '" + line + "'";
+        return;
+      }
+      out.emplace_back((size_t)(i - 1) + (size_t)g.m * ((size_t)(j - 1) + (size_t)g.n * (size_t)(k - 1)),
+                       cols.back());
     }
-    if ((int)cols.size() < nidx + 1) die(path + ": record with too few columns '" + line + "'");
-    for (int q = 0; q < nidx; q++)
-      if (!(cols[q] >= 1.0 && cols[q] < double(1 << 21))) die(path + ": index out of range in '" + line + "'");
-    const long long i = static_cast<long long>(cols[0]), j = static_cast<long long>(cols[1]);
-    const long long k = g.dim == 3 ? static_cast<long long>(cols[2]) : 1;
-    if (i < 1 || i > g.m || j < 1 || j > g.n || k < 1 || k > g.l) die(path + ": index out of range in '" + line + "'");
-    g.values[(size_t)(i - 1) + (size_t)g.m * ((size_t)(j - 1) + (size_t)g.n * (size_t)(k - 1))] = cols.back();
+  };
+  const size_t body = nl + 1;
+  const int T = static_cast<int>(std::min<size_t>(host_threads(), std::max<size_t>(1, (text.size() - body) >> 20)));
+  std::vector<size_t> cut(T + 1, text.size());
+  cut[0] = body;
+  for (int t = 1; t < T; t++) {  // each run starts after a newline
+    size_t c = body + (text.size() - body) / T * t;
+    c = std::max(c, cut[t - 1]);
+    const size_t e = text.find('\n', c);
+    cut[t] = e == std::string::npos ? text.size() : e + 1;
+  }
+  std::vector<std::vector<std::pair<size_t, double>>> recs(T);
+  std::vector<std::string> errs(T);
+  std::vector<std::thread> pool;
+  for (int t = 1; t < T; t++) pool.emplace_back(parse, cut[t], cut[t + 1], std::ref(recs[t]), std::ref(errs[t]));
+  parse(cut[0], cut[1], recs[0], errs[0]);
+  for (auto& th : pool) th.join();
+  for (int t = 0; t < T; t++) {
+    if (!errs[t].empty()) die(errs[t]);
+    for (const auto& r : recs[t]) g.values[r.first] = r.second;
   }
   return g;
 }
@@ -612,17 +664,7 @@ std::vector<double> clamped_porosity(const Grid& g, double threshold) {
 // Formatting the text is what costs (about 13 values per point; a 256^3 file
 // is 7 GB), so each array's records are formatted on all host threads, in
 // blocks of consecutive points written in order: the bytes do not depend on
-// the thread count.  PF_RUN_THREADS sets the count (default: the hardware
-// threads, at most 64).
-int format_threads() {
-  static const int n = [] {
-    const char* env = std::getenv("PF_RUN_THREADS");
-    long v = env ? std::strtol(env, nullptr, 10) : 0;
-    if (v <= 0) v = static_cast<long>(std::thread::hardware_concurrency());
-    return static_cast<int>(std::max(1L, std::min(v, 64L)));
-  }();
-  return n;
-}
+// the thread count (host_threads).
 
 class VtkWriter {
  public:
@@ -639,7 +681,7 @@ class VtkWriter {
   template <class Fn>
   void rows(int ncols, Fn fn) {
     const long long npts = (long long)m_ * n_ * (k1_ - k0_ + 1);
-    const int T = format_threads();
+    const int T = host_threads();
     const long long block = 1 << 16;  // points per thread and round
     std::vector<std::string> parts(T);
     for (long long base = 0; base < npts; base += block * T) {

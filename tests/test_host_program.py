@@ -362,3 +362,38 @@ def test_template_controldict_gives_the_defaults(pf_run, tmp_path):
     py = read_settings(os.path.join(root, "config", "controlDict.txt"))
     assert py == Settings()
     _same_settings(_config(pf_run, root), Settings(), (5, 4))
+
+
+def test_porosity_csv_parsed_on_threads_keeps_file_order(pf_run, tmp_path):
+    """A file of several megabytes is parsed on several threads: shuffled
+    records land at their own indices, a cell listed twice keeps its last
+    value, and of two bad lines the first one in the file is reported."""
+    shape = (60, 60, 60)
+    vals = np.random.default_rng(8).random(shape[::-1])
+    root = _project(str(tmp_path), G.settings_spheres_3d(), porosity=vals)
+    csv = os.path.join(root, "data", "porosity.csv")
+    with open(csv) as f:
+        head, *recs = f.read().splitlines()
+    order = np.random.default_rng(9).permutation(len(recs))
+    lines = [head] + [recs[i] for i in order] + ["1, 1, 1, 0.25"]  # listed twice: the last value counts
+    with open(csv, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    want = vals.copy()
+    want[0, 0, 0] = 0.25
+    raw = str(tmp_path / "poro.bin")
+    env = {**os.environ, "PF_RUN_THREADS": "4"}
+    r = subprocess.run([pf_run, "--project", root, "--print-config", "--dump-porosity", raw],
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(raw, dtype=np.float64)
+    assert got[0] == 0.25 and np.allclose(got, want.ravel(), rtol=0, atol=1e-10)
+    _, py = read_porosity_csv(csv)
+    assert got.tobytes() == py.ravel().tobytes()
+    bad = list(lines)
+    bad[len(bad) // 3] = "1, 2, x, 0.5"
+    bad[len(bad) - 5] = "1, 2, 3"
+    with open(csv, "w") as f:
+        f.write("\n".join(bad) + "\n")
+    r = subprocess.run([pf_run, "--project", root, "--print-config"], capture_output=True, text=True, timeout=300,
+                       env=env)
+    assert r.returncode == 1 and "bad record '1, 2, x, 0.5'" in r.stderr, r.stderr
